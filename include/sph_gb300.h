@@ -1,0 +1,322 @@
+/*
+ * sph_gb300.h — C ABI of the GB300-native weakly-compressible delta-SPH hot path.
+ *
+ * The hot path is the one the reference CUDA solver runs every half step:
+ *   cell-list build (particle -> cell hash, stable radix sort, permutation of the particle
+ *   arrays, cell start/end)  ->  neighbour pass 1 (wall pressure extrapolation, fluid
+ *   velocity divergence)  ->  neighbour pass 2 (continuity with delta density diffusion,
+ *   momentum with pressure, acoustic damper, artificial viscosity, gravity)  ->  midpoint
+ *   predictor-corrector integrator.
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-in functions.  Same arguments, layout and meaning as the reference's host
+ *     functions (AoS float[3N] positions/velocities, int cellStart/cellEnd with -1 for an
+ *     empty cell, one thread of work per particle).  Every pointer is a caller-owned device
+ *     buffer.  Each function returns an sph_status and takes an explicit stream
+ *     (a cudaStream_t passed as void*, NULL = legacy default stream).  The reference
+ *     functions return nothing and read their constants from a __constant__ SimParams;
+ *     here the constants travel in an sph_params (by value into every kernel) or in an
+ *     sph_ctx.
+ *
+ *  2. Resident solver (sph_ctx).  Keeps the particle state on the GPU in cell-sorted SoA
+ *     order and advances whole predictor-corrector steps with fused kernels; optionally
+ *     replays each step as a CUDA graph.  This is the fast path; its physics is the same.
+ *
+ * No function here allocates device memory except sph_create (everything a context needs) and
+ * sph_set_params (only when the new grid has more cells than the context was built for).
+ * All functions are host functions; none is thread-safe on the same sph_ctx.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+typedef enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_ARG = -1,        /* bad argument (NULL pointer, n < 0, n > capacity, ...) */
+    SPH_ERR_CUDA = -2,       /* a CUDA runtime call or kernel launch failed */
+    SPH_ERR_NOMEM = -3,      /* device allocation failed (sph_create / sph_ctx_reserve) */
+    SPH_ERR_DEVICE = -4,     /* a kernel raised a device error flag (see SPH_FLAG_*) */
+    SPH_ERR_STATE = -5,      /* call out of order (e.g. sph_step before sph_upload) */
+    SPH_ERR_SCRATCH = -6     /* caller-provided scratch too small */
+} sph_status;
+
+/* Device error flags, read with sph_read_error_flags. */
+#define SPH_FLAG_OUT_OF_GRID   0x1u  /* a particle hashed outside the grid; its cell index was clamped */
+#define SPH_FLAG_KEY_RANGE     0x2u  /* a sort key was outside [0, 2^key_bits) */
+#define SPH_FLAG_NONFINITE     0x4u  /* a non-finite position was seen by the hash kernel */
+
+/* EOS selector: the reference hard-codes the linear form p = cs^2 (rho - rho0)
+ * (src/sph/sph_run.cu:467,515); TAIT is p = B((rho/rho0)^gamma - 1), B = rho0 cs^2/gamma. */
+#define SPH_EOS_LINEAR 0
+#define SPH_EOS_TAIT   1
+
+/* Particle kinds, as in the reference: 0 wall, 1 fluid, 2 rigid (every non-1 kind is
+ * treated as a boundary particle; src/sph/sph_run.cu:36). */
+#define SPH_TYPE_WALL  0
+#define SPH_TYPE_FLUID 1
+#define SPH_TYPE_RIGID 2
+
+/* ---------------------------------------------------------------- parameters */
+/* Constants of one simulation.  The reference keeps the same quantities in
+ * `SimParams` (src/header/data_struct.cuh:4-44), copied once to `__constant__ par`
+ * (src/sph/sph_run.cu:105). */
+typedef struct sph_params {
+    int   num_particles;     /* N = fluid + boundary particles */
+    int   num_boundary;      /* boundary (non-fluid) particle count, informational */
+    float dt;                /* full predictor-corrector step (timeStep) */
+    float gravity;           /* z acceleration (g, negative = down) */
+    float cell_size;         /* gridSize */
+    float grid_min[3];       /* gridxmin, gridymin, gridzmin */
+    float grid_max[3];       /* gridxmax, gridymax, gridzmax */
+    int   grid_dim[3];       /* gridxdim, gridydim, gridzdim */
+    int   num_cells;         /* gx*gy*gz; cell hash = (z*gy + y)*gx + x */
+    float dx;                /* particleR: lattice spacing */
+    float h;                 /* smoothing length */
+    float kh;                /* support radius 2h */
+    float eta;               /* 0.1 h regulariser */
+    float delta;             /* delta-SPH diffusion coefficient */
+    float alpha;             /* artificial viscosity coefficient (afa) */
+    float adh;               /* Wendland C2 3-D normalisation 21/(16 pi h^3) */
+    float mass;              /* particleMass = dx^3 rho0 */
+    float rho0;              /* restDensity */
+    float cs;                /* numerical speed of sound */
+    int   eos;               /* SPH_EOS_LINEAR or SPH_EOS_TAIT */
+    float tait_gamma;        /* gamma of the Tait EOS (7) */
+    float tait_b;            /* B = rho0 cs^2 / gamma */
+    int   clamp_density;     /* 1: rho >= rho0 after each update (reference behaviour) */
+    float escape_min[3];     /* a fluid particle outside [escape_min, escape_max] ... */
+    float escape_max[3];
+    float escape_park[3];    /* ... is parked here with v = 0, p = 0, rho = rho0 */
+    int   reserved[8];
+} sph_params;
+
+/* Inputs from which sph_params_derive computes the derived constants with the same
+ * mixed double/float rounding as the reference's main (src/sph/sph_run.cu:60-101). */
+typedef struct sph_config {
+    float  dx;               /* lattice spacing */
+    double h_factor;         /* h = h_factor * dx (reference: 1.5) */
+    float  rho0;             /* 1000 */
+    float  cs;               /* speed of sound (reference: 25) */
+    float  gravity;          /* -9.81 */
+    float  delta;            /* reference: 0.2 */
+    float  alpha;            /* reference: 0.05 */
+    float  dt;               /* > 0: fixed step; <= 0: dt = cfl * h / cs */
+    float  cfl;              /* used when dt <= 0 */
+    int    eos;              /* SPH_EOS_LINEAR / SPH_EOS_TAIT */
+    float  tait_gamma;       /* 7 */
+    float  domain_min[3];    /* tank box; the grid is this box padded by `pad` */
+    float  domain_max[3];
+    double pad;              /* reference: 0.1 m on every side */
+    double cell_factor;      /* cell size = cell_factor * kh (reference: 1) */
+    float  escape_min[3];
+    float  escape_max[3];
+    float  escape_park[3];
+    int    num_particles;
+    int    num_boundary;
+    int    clamp_density;
+} sph_config;
+
+/* Layout-compatible copy of the reference's SimParams (src/header/data_struct.cuh:4-44),
+ * so a reference driver can hand its host-side `temps` to sph_params_from_reference. */
+typedef struct sph_ref_simparams {
+    float timeStep, time;
+    int numParticles, boundary_p_num;
+    float gravity;
+    float gridSize, gridxmin, gridymin, gridzmin, gridxmax, gridymax, gridzmax;
+    int gridxdim, gridydim, gridzdim, numCells;
+    int hash_max, hash_min;
+    float pre_set_domain_x_min, pre_set_domain_x_max, pre_set_domain_y_min,
+          pre_set_domain_y_max, pre_set_domain_z_min, pre_set_domain_z_max;
+    float particleR, h, kh, eta, delta, afa;
+    float SpikyKern, LapKern, Poly6Kern;
+    float minDist;
+    float particleMass, restDensity;
+    float viscosity, stiffness;
+    float cs;
+    float adh;
+    float namuta_threshold_1, namuta_threshold_2;
+    float CFL, Ma, conc_0, conc_t, PST_R, PST_n, w_deltar;
+    int ngp, nnode, n_edge, num_vp, max_nspnode, nele;
+    float mat_para[3];
+} sph_ref_simparams;
+
+/* Derive parameters from a config.  Replaces the host block of src/sph/sph_run.cu:60-101. */
+int sph_params_derive(const sph_config* cfg, sph_params* out);
+
+/* The reference's own hard-coded case (src/sph/sph_run.cu:11-22,60-101): h = 1.5 dx,
+ * delta 0.2, alpha 0.05, cs 25, dt 2e-4, linear EOS, tank vlx*vly*vlz padded by 0.1 m,
+ * escape box x<=3.23, y<=1, z<=1 parked at (0, 0.5, -0.08) (src/sph/sph_run.cu:437-447). */
+int sph_params_reference(float dx, float vlx, float vly, float vlz,
+                         int num_particles, int num_boundary, sph_params* out);
+
+/* Convert a reference SimParams into sph_params (linear EOS, reference escape box). */
+int sph_params_from_reference(const sph_ref_simparams* in, sph_params* out);
+/* And back (fields the hot path does not use are zero). */
+int sph_params_to_reference(const sph_params* in, sph_ref_simparams* out);
+
+const char* sph_status_string(int status);
+/* Library version string. */
+const char* sph_version(void);
+
+/* ---------------------------------------------------------------- drop-in functions */
+/* calcHash (src/header/mesh.cuh:20, src/lib/mesh.cu:26-70): hash[i] = cell of pos[3i..3i+2],
+ * index[i] = i.  The cell coordinate is floorf((p - grid_min)/cell_size) in IEEE FP32,
+ * bit-identical to the reference for every in-grid position. */
+int sph_calc_hash(const sph_params* p, const float* pos, int* hash, int* index, int n,
+                  void* stream);
+
+/* sortParticles (src/header/mesh.cuh:23, src/lib/mesh.cu:73-86): stable sort of (hash, index)
+ * pairs by hash, in place.  key_bits = 32 sorts the full signed int range (same order as the
+ * reference's thrust::sort_by_key); key_bits in [1,31] requires 0 <= hash < 2^key_bits and
+ * runs ceil(key_bits/8) passes.  Scratch is caller-provided (sph_sort_scratch_bytes). */
+int sph_sort_scratch_bytes(int n, size_t* bytes);
+int sph_sort_particles(int* hash, int* index, int n, int key_bits,
+                       void* scratch, size_t scratch_bytes, void* stream);
+
+/* reorder (src/header/mesh.cuh:29, src/lib/mesh.cu:89-159): cell_start[c] = first sorted
+ * slot of cell c or -1 if empty, cell_end[c] = one past its last slot (untouched for an
+ * empty cell), and gathers pos, vel (AoS), rho, p, type, zone into sorted order.
+ * zone arrays may be NULL. */
+int sph_reorder(const sph_params* p,
+                const float* old_pos, const float* old_vel, const float* old_rho,
+                const float* old_p, const int* old_type, const int* old_zone,
+                float* s_pos, float* s_vel, float* s_rho, float* s_p, int* s_type, int* s_zone,
+                const int* hash, const int* index, int* cell_start, int* cell_end, int n,
+                void* stream);
+
+/* recover (src/header/mesh.cuh:33, src/lib/mesh.cu:162-194): scatter sorted arrays back to
+ * original order through index. zone arrays may be NULL. */
+int sph_recover(float* pos, float* vel, float* rho, float* p, int n, const int* index,
+                int* type, int* zone,
+                const float* s_pos, const float* s_vel, const float* s_rho, const float* s_p,
+                const int* s_type, const int* s_zone, void* stream);
+
+/* PC_prediction / PC_correction (src/header/sph.cuh:26,28, src/sph/sph_run.cu:425-550):
+ * midpoint predictor and corrector on sorted AoS arrays; the saved step-n state
+ * (pos_tmp, vel_tmp, rho_tmp) is indexed by original particle id index[i]. */
+int sph_pc_prediction(const sph_params* p, float* s_pos, float* s_vel, float* s_rho,
+                      float* s_p, const float* rho_dt, const float* vel_dt, const int* index,
+                      float* pos_tmp, float* vel_tmp, float* rho_tmp, int n,
+                      const int* s_type, void* stream);
+int sph_pc_correction(const sph_params* p, float* s_pos, float* s_vel, float* s_rho,
+                      float* s_p, const float* rho_dt, const float* vel_dt, const int* index,
+                      const float* pos_tmp, const float* vel_tmp, const float* rho_tmp, int n,
+                      const int* s_type, void* stream);
+
+/* ---------------------------------------------------------------- resident solver */
+typedef struct sph_ctx sph_ctx;
+
+/* Solver options (sph_ctx_set_option). */
+#define SPH_OPT_USE_GRAPH     1  /* 1: sph_step replays one captured CUDA graph per step */
+#define SPH_OPT_WALL_RATES    2  /* 1: sph_ns also fills rho_dt/vel_dt rows of boundary particles */
+#define SPH_OPT_PROFILE       3  /* 1: sph_step times each phase with CUDA events (no graph; syncs per step) */
+
+/* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
+ * [2] neighbour pass 1, [3] neighbour pass 2 + integrator; summed over half steps. */
+#define SPH_PHASE_COUNT 4
+
+/* Create a context on the current CUDA device for up to `capacity` particles (allocates all
+ * state and scratch once).  p may describe fewer particles than capacity. */
+int sph_create(const sph_params* p, int capacity, sph_ctx** out);
+int sph_destroy(sph_ctx* ctx);
+int sph_set_params(sph_ctx* ctx, const sph_params* p);
+int sph_get_params(const sph_ctx* ctx, sph_params* out);
+int sph_ctx_set_option(sph_ctx* ctx, int option, int value);
+
+/* SPH_NS_simpleversion (src/header/ns.cuh:4, src/equation/ns.cu:5-131 and :134-249): both
+ * neighbour passes on sorted AoS arrays.  Writes dofv, rho_dt, vel_dt (AoS) and, for boundary
+ * particles, the extrapolated pressure and density in place in s_p / s_rho.  rhop_sum and
+ * w_sum (the wall extrapolation sums) are written when non-NULL.  Rows of rho_dt / vel_dt
+ * for boundary particles are zero unless SPH_OPT_WALL_RATES is set (the integrator never
+ * reads them).  cell_start/cell_end/hash are the outputs of sph_reorder/sph_calc_hash. */
+int sph_ns(sph_ctx* ctx, float* s_pos, float* s_vel, float* s_rho, float* s_p,
+           const int* s_type, float* rho_dt, float* vel_dt, const int* cell_start,
+           const int* cell_end, int n, const int* hash, float* dofv, float* rhop_sum,
+           float* w_sum, void* stream);
+
+/* Load a particle state given in original order (AoS pos/vel [3n], rho, p, type [n]) from
+ * host (from_host = 1) or device memory.  Resets the step counter. */
+int sph_upload(sph_ctx* ctx, const float* pos, const float* vel, const float* rho,
+               const float* p, const int* type, int n, int from_host, void* stream);
+/* Write the current state back in original order; any pointer may be NULL. */
+int sph_download(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
+                 int to_host, void* stream);
+/* Advance nsteps full predictor-corrector steps (two cell-list builds, four neighbour passes
+ * per step), asynchronously on `stream`. */
+int sph_step(sph_ctx* ctx, int nsteps, void* stream);
+/* End-to-end call with host buffers: upload, nsteps steps, download into the same buffers;
+ * synchronises the stream before returning. */
+int sph_step_host(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
+                  int n, int nsteps, void* stream);
+/* Sorted-order views for diagnostics / tests (device pointers owned by ctx). */
+int sph_ctx_sorted_view(sph_ctx* ctx, const int** cell_start, const int** sorted_id,
+                        const int** sorted_hash);
+/* Read and clear the device error flags (synchronises the stream). */
+int sph_read_error_flags(sph_ctx* ctx, unsigned* flags, void* stream);
+/* Steps taken since the last upload. */
+int sph_steps_taken(const sph_ctx* ctx, long long* steps);
+/* Accumulated milliseconds and launch counts per phase under SPH_OPT_PROFILE
+ * (arrays of SPH_PHASE_COUNT); reset != 0 clears them. */
+int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
+
+/* ---------------------------------------------------------------- reference-signature shim */
+/* The library also exports, with C++ linkage, the reference's own host functions calcHash,
+ * sortParticles, reorder, recover, SPH_NS_simpleversion, PC_prediction, PC_correction,
+ * iDivUp and computeGridSize (src/header/mesh.cuh:14-33, ns.cuh:4, sph.cuh:26-28), forwarding
+ * to the functions above on the legacy default stream.  The reference functions read their
+ * constants from `__constant__ par`; a reference driver hands the same SimParams to the shim
+ * once, right after its cudaMemcpyToSymbol (src/sph/sph_run.cu:105). */
+int sph_shim_set_reference_params(const sph_ref_simparams* p);
+/* Or full sph_params (EOS, escape box and other options the reference hard-codes). */
+int sph_shim_set_params(const sph_params* p);
+/* Free the shim's lazily allocated scratch and context. */
+int sph_shim_release(void);
+
+/* ---------------------------------------------------------------- initial conditions */
+/* Seeded dam-break generator: fluid block on a lattice at (i+1/2)dx, `wall_layers` lattice
+ * layers outside the floor and four side walls of the tank (open top), an optional box
+ * obstacle of rigid particles, uniform jitter of +-jitter*dx per coordinate.  Replaces the
+ * reference's missing input files read by ini_fluid (src/io/io.cu:6-111). */
+typedef struct sph_dam_break {
+    float  dx;
+    float  tank[3];          /* tank interior size, origin at 0 */
+    float  block[3];         /* water block size at the x=0, y=0 corner, from the floor */
+    int    wall_layers;      /* 3 */
+    int    has_obstacle;
+    float  obstacle_min[3];  /* obstacle box (rigid particles fill it on the lattice) */
+    float  obstacle_max[3];
+    float  jitter;           /* fraction of dx */
+    unsigned long long seed;
+    int    hydrostatic;      /* 1: p = rho0 |g| (H - z) and rho from the EOS inverse */
+    float  rho0, gravity, cs;
+    int    eos;
+    float  tait_gamma;
+} sph_dam_break;
+
+/* Count particles (fluid, boundary) without generating them. */
+int sph_dam_break_count(const sph_dam_break* d, int* n_fluid, int* n_boundary);
+/* Fill host arrays (pos/vel [3n], rho, p [n], type [n]); boundary particles first, then
+ * fluid, as in the reference's input ordering (walls at indices < nb). */
+int sph_dam_break_generate(const sph_dam_break* d, float* pos, float* vel, float* rho,
+                           float* p, int* type, int n);
+/* Write the seven whitespace text files ini_fluid reads (h_pos.dat, h_vel.dat, h_ac.dat,
+ * rhop.dat, p.dat, particle_type.dat, particle_zone.dat) into directory `dir`
+ * (src/io/io.cu:10-111); zone is written as 0. */
+int sph_write_dat(const char* dir, const float* pos, const float* vel, const float* rho,
+                  const float* p, const int* type, int n);
+/* Read them back (the inverse of sph_write_dat / the reference's ini_fluid). */
+int sph_read_dat(const char* dir, float* pos, float* vel, float* ac, float* rho, float* p,
+                 int* type, int* zone, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

@@ -1,0 +1,185 @@
+"""GPU tests of the resident solver (sph_create / sph_upload / sph_step / sph_download): whole
+predictor-corrector steps against the oracle's reference step loop
+(src/sph/sph_run.cu:285-336), CUDA-graph replay against plain launches, the end-to-end host
+call, and full-size properties of the 4.96M-particle case.
+
+The resident solver keeps particles in cell order between steps, so particles that share a
+cell are summed in a different order than the reference (which returns to original order
+every half step); the fields therefore agree to FP32 rounding growth, not bit for bit."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(st, p, nsteps, graph=True, stream=None):
+    import torch
+    from tmp_sph_gb300 import api, solver as S
+    n = len(st["rho"])
+    s = stream or torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(api.SPH_OPT_USE_GRAPH, int(graph))
+        with torch.cuda.stream(s):
+            sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+            sol.step(nsteps, stream=s)
+            out = sol.download(stream=s)
+        flags = sol.error_flags(stream=s)
+        assert sol.steps_taken() == nsteps
+    return out, flags
+
+
+def field_errors(out, ref, st):
+    fl = st["type"] == 1
+    n_f = int(fl.sum())
+    return {
+        "disp": rel_l2(out["pos"][fl] - st["pos"][fl], ref["pos"][fl] - st["pos"][fl]),
+        "vel": rel_l2(out["vel"][fl], ref["vel"][fl], floor=1e-3 * np.sqrt(n_f)),
+        "drho": rel_l2(out["rho"][fl] - 1000.0, ref["rho"][fl] - 1000.0),
+        "p": rel_l2(out["p"][fl], ref["p"][fl]),
+    }
+
+
+@pytest.mark.parametrize("physics", ["reference", "config"])
+def test_steps_match_oracle(sphlib, oracle, cuda, report, physics):
+    from tmp_sph_gb300 import cases
+    st, p = cases.build("small", physics=physics, dx=0.02, jitter=0.01)
+    P = oracle.params_like(p)
+    for nsteps, tol in ((1, 1e-4), (20, 2e-3)):
+        out, flags = run_gpu(st, p, nsteps)
+        ref = oracle.run(P, st, nsteps)
+        assert flags == 0
+        e = field_errors(out, ref, st)
+        for k, v in e.items():
+            report(f"solver {physics} {nsteps} steps {k}", v, tol)
+        assert all(v < tol for v in e.values()), (nsteps, e)
+        wl = st["type"] != 1
+        assert np.array_equal(out["pos"][wl], st["pos"][wl])
+        assert np.array_equal(out["type"], st["type"])
+        np.testing.assert_allclose(out["p"][wl], ref["p"][wl], rtol=1e-3, atol=1.0)
+
+
+def test_graph_replay_is_bitwise_identical(sphlib, cuda):
+    from tmp_sph_gb300 import cases
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    a, _ = run_gpu(st, p, 7, graph=True)
+    b, _ = run_gpu(st, p, 7, graph=False)
+    for k in ("pos", "vel", "rho", "p", "type"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_upload_download_roundtrip(sphlib, cuda):
+    from tmp_sph_gb300 import cases
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    out, flags = run_gpu(st, p, 0)
+    for k in ("pos", "vel", "rho", "p", "type"):
+        assert np.array_equal(out[k], st[k]), k
+
+
+def test_step_host_matches_device_path(sphlib, cuda):
+    import torch
+    from tmp_sph_gb300 import cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    dev_out, _ = run_gpu(st, p, 3, graph=False)
+    n = len(st["rho"])
+    hst = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory().numpy()
+           for k in ("pos", "vel", "rho", "p", "type")}
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(1, 0)
+        sol.step_host(hst, 3, stream=s)
+    for k in ("pos", "vel", "rho", "p"):
+        assert np.array_equal(hst[k], dev_out[k]), k
+
+
+def test_escape_and_out_of_grid_flags(sphlib, cuda):
+    """A fluid particle above the escape box is parked (src/sph/sph_run.cu:437-447); one
+    outside the grid is clamped into it and raises SPH_FLAG_OUT_OF_GRID, without a fault."""
+    from tmp_sph_gb300 import api, cases
+    st, p = cases.build("small", physics="config", dx=0.04)
+    fl = np.nonzero(st["type"] == 1)[0]
+    st["pos"][fl[0]] = (0.5, 0.25, p.escape_max[2] + 0.02)
+    out, flags = run_gpu(st, p, 1)
+    assert np.array_equal(out["pos"][fl[0]], np.array(p.escape_park, np.float32))
+    assert flags == 0
+    st["pos"][fl[1]] = (0.5, 0.25, p.grid_max[2] + 1.0)
+    out, flags = run_gpu(st, p, 1)
+    assert flags & api.SPH_FLAG_OUT_OF_GRID
+    assert np.array_equal(out["pos"][fl[1]], np.array(p.escape_park, np.float32))
+
+
+def test_api_errors(sphlib, cuda):
+    import ctypes as C
+    from tmp_sph_gb300 import api, cases
+    _, p = cases.build("small", physics="config", dx=0.04)
+    L = api.lib()
+    h = C.c_void_p()
+    assert L.sph_create(C.byref(p), p.num_particles, C.byref(h)) == api.SPH_OK
+    try:
+        assert L.sph_step(h, 1, None) == api.SPH_ERR_STATE
+        assert L.sph_upload(h, None, None, None, None, None, p.num_particles + 1, 1, None) == api.SPH_ERR_ARG
+        assert L.sph_ctx_set_option(h, 99, 1) == api.SPH_ERR_ARG
+        bad = api.SphParams.from_buffer_copy(p)
+        bad.cell_size = bad.kh * 0.5
+        assert L.sph_set_params(h, C.byref(bad)) == api.SPH_ERR_ARG
+    finally:
+        L.sph_destroy(h)
+
+
+def test_profile_phases(sphlib, cuda):
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.02)
+    n = len(st["rho"])
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(api.SPH_OPT_PROFILE, 1)
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(3, stream=s)
+        prof = sol.profile()
+    assert set(prof) == set(api.PHASE_NAMES)
+    assert all(v["launches"] == 6 and v["ms"] > 0 for v in prof.values())
+
+
+def test_large_case_properties(sphlib, cuda, report):
+    """The 4,963,548-particle case (dx 2.5 mm, jitter 0.01 dx): five steps stay finite and
+    physical, walls stay put, the particle ids stay a permutation, the sorted cell keys are
+    sorted and the dense cell starts bracket them."""
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = cases.build("large", physics="config")
+    n = len(st["rho"])
+    assert n == 4963548
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(5, stream=s)
+        out = sol.download(stream=s)
+        cs_ptr, id_ptr, key_ptr = sol.sorted_view()
+        import ctypes as C
+        keys = np.zeros(n, np.int32)
+        ids = np.zeros(n, np.int32)
+        cs = np.zeros(p.num_cells + 1, np.int32)
+        torch.cuda.synchronize()
+        rt = C.CDLL("libcudart.so.13")  # already loaded as the library's dependency
+        rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        assert rt.cudaMemcpy(keys.ctypes.data, key_ptr, n * 4, 2) == 0
+        assert rt.cudaMemcpy(ids.ctypes.data, id_ptr, n * 4, 2) == 0
+        assert rt.cudaMemcpy(cs.ctypes.data, cs_ptr, (p.num_cells + 1) * 4, 2) == 0
+        flags = sol.error_flags(stream=s)
+    assert flags == 0
+    fl = st["type"] == 1
+    for k in ("pos", "vel", "rho", "p"):
+        assert np.isfinite(out[k]).all(), k
+    assert np.array_equal(out["pos"][~fl], st["pos"][~fl])
+    assert np.abs(out["vel"][fl]).max() < 1.0
+    assert (out["rho"][fl] >= 1000.0).all() and (out["rho"][fl] < 1050.0).all()
+    assert np.array_equal(np.sort(ids), np.arange(n))
+    assert (np.diff(keys) >= 0).all()
+    assert cs[0] == 0 and cs[-1] == n and (np.diff(cs) >= 0).all()
+    occ = np.unique(keys)
+    assert (cs[occ + 1] - cs[occ] == np.bincount(keys, minlength=p.num_cells)[occ]).all()
+    report("large 5 steps max |v|", float(np.abs(out["vel"][fl]).max()))

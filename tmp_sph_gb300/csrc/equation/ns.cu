@@ -1,0 +1,278 @@
+// ns.cu — the two neighbour passes of the weakly-compressible delta-SPH step.
+//
+// Reference counterparts: SPH_NS_simpleversion (src/equation/ns.cu:5-28) launching
+// computeBoundary_Delta_acoustic_D (pass 1, src/equation/ns.cu:30-131) and
+// computeGovering_equationD (pass 2, src/equation/ns.cu:134-249).
+//
+// Layout: particles in cell-sorted order, SoA float4 (x, y, z, kind) / (vx, vy, vz, rho),
+// pass-1 output (p, rho, dofv, 0).  Cells are walked as nine x-strips: the three cells
+// (x-1 .. x+1) of one (y, z) row are consecutive in the sorted order, so each strip is one
+// contiguous slot range [cell_start[row + x-1], cell_start[row + x+2]) — the dense
+// cell_start array gives empty cells the start of the next non-empty one.
+//
+// Kernel algebra (same quantities as the reference, simplified): with r = x_i - x_j,
+// q = |r|/h, t = 1 - q/2, the Wendland C2 gradient is grad W = c_fr t^3 r with
+// c_fr = -5 adh / h^2, which is the reference's per-component expression
+// adh(-2 t^3 (2q+1) + 2 t^4) r/(h|r|) after factoring.
+#include <cuda_runtime.h>
+
+#include "sph_internal.h"
+
+namespace sph {
+
+namespace {
+
+constexpr int NS_THREADS = 128;
+
+__device__ __forceinline__ void cell_of_key(const KParams& k, unsigned key, int& cx, int& cy,
+                                            int& cz) {
+    unsigned t = key / (unsigned)k.gx;
+    cx = (int)(key - t * (unsigned)k.gx);
+    cz = (int)(t / (unsigned)k.gy);
+    cy = (int)(t - (unsigned)cz * (unsigned)k.gy);
+}
+
+// Visit every candidate slot j of the 27 cells around (cx, cy, cz), strip by strip.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const KParams& k, const int* __restrict__ cs,
+                                                   int cx, int cy, int cz, F&& f) {
+    const int xl = cx > 0 ? cx - 1 : 0;
+    const int xh = cx < k.gx - 1 ? cx + 1 : k.gx - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = cz + dz;
+        if ((unsigned)z >= (unsigned)k.gz) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = cy + dy;
+            if ((unsigned)y >= (unsigned)k.gy) continue;
+            const int row = (z * k.gy + y) * k.gx;
+            const int j0 = max(__ldg(cs + row + xl), 0);
+            const int j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
+#pragma unroll 2
+            for (int j = j0; j < j1; j++) f(j);
+        }
+    }
+}
+
+// Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
+// particles; velocity divergence over fluid neighbours for fluid particles.
+template <bool WRITE_SUMS>
+__global__ void __launch_bounds__(NS_THREADS)
+k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
+        const int* __restrict__ cs, float4* __restrict__ aux, float* __restrict__ rhop_sum,
+        float* __restrict__ w_sum) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const float4* __restrict__ P = in.pos;
+    const float4* __restrict__ V = in.vel;
+    const float* __restrict__ PR = in.pres;
+    const float4 pi = P[i];
+    const float4 vi = V[i];
+    const bool fi = is_fluid(pi.w);
+    int cx, cy, cz;
+    cell_of_key(k, keys[i], cx, cy, cz);
+    float dofv = 0.f, rs = 0.f, ws = 0.f;
+    for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
+        const float4 pj = __ldg(P + j);
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < k.kh2 && j != i && is_fluid(pj.w)) {
+            const float rr = sqrtf(r2);
+            const float q = rr * k.inv_h;
+            const float t = 1.f - 0.5f * q;
+            const float t2 = t * t;
+            if (!fi) {
+                const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
+                const float rhoj = __ldg(&V[j].w);
+                const float pj_ = __ldg(PR + j);
+                rs += (pj_ + rhoj * k.g * dz) * w;
+                ws += w;
+            } else {
+                const float4 vj = __ldg(V + j);
+                const float fr = k.c_fr * t2 * t;
+                const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+                dofv -= fr * vdotr * (k.mass / vj.w);
+            }
+        }
+    });
+    float4 out;
+    if (fi) {
+        out = make_float4(PR[i], vi.w, dofv, 0.f);
+    } else {
+        float p = fabsf(ws) > 1.0e-8f ? rs / ws : 0.f;
+        if (p < 0.f) p = 0.f;
+        out = make_float4(p, eos_density(k, p), 0.f, 0.f);
+    }
+    aux[i] = out;
+    if (WRITE_SUMS) {
+        rhop_sum[i] = rs;
+        w_sum[i] = ws;
+    }
+}
+
+enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
+
+// Pass 2: continuity + delta density diffusion, momentum (pressure, acoustic damper,
+// artificial viscosity, gravity); then either the rates are stored (MODE_RATES) or the
+// midpoint predictor / corrector of src/sph/sph_run.cu:425-519 is applied and the updated
+// particle written to `out` with its next cell hash.
+template <int MODE>
+__global__ void __launch_bounds__(NS_THREADS)
+k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
+        const int* __restrict__ cs, const float4* __restrict__ aux, float* __restrict__ rho_dt,
+        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
+        unsigned* __restrict__ out_hash, unsigned* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const float4* __restrict__ P = in.pos;
+    const float4* __restrict__ V = in.vel;
+    const float4 pi = P[i];
+    const float4 vi = V[i];
+    const float4 ai = aux[i];  // p_i, rho_i, dofv_i
+    const bool fi = is_fluid(pi.w);
+    const float rhoi = ai.y, presi = ai.x, dofvi = ai.z;
+    float drho = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+    if (fi || (MODE == MODE_RATES && wall_rates)) {
+        int cx, cy, cz;
+        cell_of_key(k, keys[i], cx, cy, cz);
+        for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
+            const float4 pj = __ldg(P + j);
+            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < k.kh2 && j != i) {
+                const float4 vj = __ldg(V + j);
+                const float4 aj = __ldg(aux + j);
+                const float rr = sqrtf(r2);
+                const float q = rr * k.inv_h;
+                const float t = 1.f - 0.5f * q;
+                const float fr = k.c_fr * t * t * t;
+                const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+                const float m_rhoj = k.mass / aj.y;
+                const float inv_r2e = 1.f / (r2 + k.eta2);
+                drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - aj.y) * k.delta_h_cs * r2 * inv_r2e);
+                float S = -(presi + aj.x);
+                if (fi && is_fluid(pj.w))
+                    S += k.damper * (dofvi + aj.z) + k.visc * vdotr * inv_r2e;
+                const float c = fr * S * m_rhoj;
+                ax += c * dx;
+                ay += c * dy;
+                az += c * dz;
+            }
+        });
+        const float inv_rhoi = 1.f / rhoi;
+        ax *= inv_rhoi;
+        ay *= inv_rhoi;
+        az *= inv_rhoi;
+    }
+    az += k.g;
+
+    if (MODE == MODE_RATES) {
+        const bool have = fi || wall_rates;
+        rho_dt[i] = have ? drho : 0.f;
+        vel_dt[3 * i] = have ? ax : 0.f;
+        vel_dt[3 * i + 1] = have ? ay : 0.f;
+        vel_dt[3 * i + 2] = have ? az : 0.f;
+        return;
+    }
+
+    float4 np = pi, nv;
+    float npres;
+    float4 tp, tv;
+    if (fi) {
+        if (escaped(k, pi.x, pi.y, pi.z)) {
+            np = make_float4(k.park_x, k.park_y, k.park_z, pi.w);
+            nv = make_float4(0.f, 0.f, 0.f, k.rho0);
+            npres = 0.f;
+            tp = make_float4(np.x, np.y, np.z, k.rho0);
+            tv = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else if (MODE == MODE_PRED) {
+            tp = make_float4(pi.x, pi.y, pi.z, rhoi);
+            tv = make_float4(vi.x, vi.y, vi.z, 0.f);
+            float rho = rhoi + drho * k.half_dt;
+            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+            np.x = pi.x + vi.x * k.half_dt;
+            np.y = pi.y + vi.y * k.half_dt;
+            np.z = pi.z + vi.z * k.half_dt;
+            nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt, rho);
+            npres = eos_pressure(k, rho);
+        } else {
+            tp = in.tpos[i];
+            tv = in.tvel[i];
+            float rho = tp.w + drho * k.half_dt;
+            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+            const float xs = tp.x + vi.x * k.half_dt;
+            const float ys = tp.y + vi.y * k.half_dt;
+            const float zs = tp.z + vi.z * k.half_dt;
+            const float uxs = tv.x + ax * k.half_dt;
+            const float uys = tv.y + ay * k.half_dt;
+            const float uzs = tv.z + az * k.half_dt;
+            rho = 2.f * rho - tp.w;
+            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+            np.x = 2.f * xs - tp.x;
+            np.y = 2.f * ys - tp.y;
+            np.z = 2.f * zs - tp.z;
+            nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, rho);
+            npres = eos_pressure(k, rho);
+        }
+    } else {
+        // boundary particles do not move; they keep the extrapolated pressure and density
+        nv = make_float4(vi.x, vi.y, vi.z, rhoi);
+        npres = presi;
+        tp = make_float4(pi.x, pi.y, pi.z, rhoi);
+        tv = make_float4(vi.x, vi.y, vi.z, 0.f);
+    }
+    out.pos[i] = np;
+    out.vel[i] = nv;
+    out.pres[i] = npres;
+    out.id[i] = in.id[i];
+    if (MODE == MODE_PRED) {
+        out.tpos[i] = tp;
+        out.tvel[i] = tv;
+    }
+    unsigned f = 0;
+    out_hash[i] = (unsigned)cell_hash_clamped(k, np.x, np.y, np.z, &f);
+    raise_flags(err, f);
+}
+
+inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* keys,
+                         const int* cs, float4* aux, float* rhop_sum, float* w_sum,
+                         cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    if (rhop_sum && w_sum)
+        k_pass1<true><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in, keys, cs, aux,
+                                                                         rhop_sum, w_sum);
+    else
+        k_pass1<false><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in, keys, cs, aux,
+                                                                          nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in, const unsigned* keys,
+                               const int* cs, const float4* aux, float* rho_dt, float* vel_dt,
+                               int wall_rates, cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    k_pass2<MODE_RATES><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
+        k, in, keys, cs, aux, rho_dt, vel_dt, wall_rates, ParticleSet{}, nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
+                              const unsigned* keys, const int* cs, const float4* aux,
+                              ParticleSet out, unsigned* out_hash, unsigned* err,
+                              cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    if (half == HALF_PREDICT)
+        k_pass2<MODE_PRED><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
+            k, in, keys, cs, aux, nullptr, nullptr, 0, out, out_hash, err);
+    else
+        k_pass2<MODE_CORR><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
+            k, in, keys, cs, aux, nullptr, nullptr, 0, out, out_hash, err);
+    return cudaGetLastError();
+}
+
+}  // namespace sph

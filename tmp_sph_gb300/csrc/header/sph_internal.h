@@ -1,0 +1,122 @@
+// sph_internal.h — host-side declarations shared by the library's translation units:
+// the resident-solver context and the launchers each .cu file provides.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sph_gb300.h"
+#include "sph_device.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------- radix sort (lib/mesh.cu)
+// Stable LSD radix sort of 32-bit unsigned keys with int values, 8-bit digits, keys sorted on
+// bits [0, key_bits).  Scratch layout and size come from sort_scratch_bytes(); no allocation.
+// vals_in == NULL means the values are the identity 0..n-1.  The sorted output lands in
+// keys_out / vals_out (which may alias keys_in / vals_in).  err (may be NULL) receives
+// SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.
+size_t sort_scratch_bytes(int n);
+cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
+                             int* vals_out, int n, int key_bits, void* scratch,
+                             size_t scratch_bytes, unsigned* err, cudaStream_t s);
+int key_bits_for(int num_cells);
+
+// ---------------------------------------------------------------- cell list (lib/mesh.cu)
+// Dense cell starts: cell_start[c] = first sorted slot whose key >= c, for c in [0, C];
+// cell_start[C] = n.  Keys must be sorted and < C.
+cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
+                              int* cell_start, cudaStream_t s);
+
+// ---------------------------------------------------------------- resident state
+// One particle set in SoA form.  pos.w holds the particle kind as a float, vel.w the
+// density; tpos/tvel hold the predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
+struct ParticleSet {
+    float4* pos = nullptr;
+    float4* vel = nullptr;
+    float* pres = nullptr;
+    int* id = nullptr;
+    float4* tpos = nullptr;
+    float4* tvel = nullptr;
+};
+
+enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
+
+// Neighbour passes (equation/ns.cu).
+//  pass 1: aux[i] = (p, rho, dofv, 0) — boundary particles get the extrapolated p and rho,
+//          fluid particles their own p, rho and the velocity divergence.  rhop_sum / w_sum are
+//          written when non-NULL.
+//  pass 2: either rates only (rho_dt, AoS vel_dt) or rates + the predictor/corrector update
+//          written into `out` (slot-aligned with `in`) with the next cell hash.
+cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
+                         const int* cell_start, float4* aux, float* rhop_sum, float* w_sum,
+                         cudaStream_t s);
+cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
+                               const unsigned* sorted_keys, const int* cell_start,
+                               const float4* aux, float* rho_dt, float* vel_dt, int wall_rates,
+                               cudaStream_t s);
+cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
+                              const unsigned* sorted_keys, const int* cell_start,
+                              const float4* aux, ParticleSet out, unsigned* out_hash,
+                              unsigned* err, cudaStream_t s);
+
+// Resident-state glue (lib/mesh.cu).
+cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
+                          ParticleSet dst, int with_tmp, cudaStream_t s);
+cudaError_t launch_upload_convert(const KParams& k, const float* pos, const float* vel,
+                                  const float* rho, const float* p, const int* type,
+                                  ParticleSet dst, unsigned* hash, unsigned* err,
+                                  cudaStream_t s);
+cudaError_t launch_download_convert(const KParams& k, const ParticleSet& src, float* pos,
+                                    float* vel, float* rho, float* p, int* type,
+                                    cudaStream_t s);
+// Drop-in sph_ns glue: AoS sorted arrays -> SoA set (and back for the outputs).
+cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,
+                              const float* s_rho, const float* s_p, const int* s_type,
+                              const int* hash, ParticleSet dst, unsigned* keys,
+                              unsigned* err, cudaStream_t s);
+cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* aux,
+                                float* s_rho, float* s_p, float* dofv, cudaStream_t s);
+
+// Per-phase device timing of sph_step (SPH_OPT_PROFILE).
+enum Phase { PH_SORT = 0, PH_GATHER, PH_PASS1, PH_PASS2, PH_COUNT };
+
+}  // namespace sph
+
+// The resident-solver context (sph/solver.cu).
+struct sph_ctx {
+    sph_params P{};
+    int capacity = 0;
+    int n = 0;
+    int device = 0;
+    bool loaded = false;
+    long long steps = 0;
+
+    sph::ParticleSet x;   // integrator output, slot-aligned with the previous sorted order
+    sph::ParticleSet y;   // cell-sorted order the neighbour passes read
+    unsigned* hash_x = nullptr;      // next cell of every slot of x
+    unsigned* keys_sorted = nullptr; // sorted cell keys of y
+    int* perm = nullptr;             // y slot k came from x slot perm[k]
+    float4* aux = nullptr;           // pass-1 output
+    int* cell_start = nullptr;       // [num_cells + 1]
+    int cell_capacity = 0;
+    void* sort_scratch = nullptr;
+    size_t sort_scratch_bytes = 0;
+    unsigned* err = nullptr;         // device error word
+
+    // drop-in sph_ns buffers are the y set plus these
+    float* tmp_rho_dt = nullptr;
+
+    // graph replay of one full step
+    int opt_use_graph = 1;
+    int opt_wall_rates = 0;
+    int opt_profile = 0;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    int graph_n = -1;
+    // profiling events / accumulated milliseconds per phase
+    cudaEvent_t ev[2 * sph::PH_COUNT * 2] = {};
+    double phase_ms[sph::PH_COUNT] = {};
+    long long phase_launches[sph::PH_COUNT] = {};
+};

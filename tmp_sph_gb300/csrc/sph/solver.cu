@@ -1,0 +1,385 @@
+// solver.cu — the resident solver: one context per simulation, state kept on the GPU in
+// cell-sorted SoA order, whole predictor-corrector steps advanced with fused kernels.
+//
+// Reference counterpart: the step loop of src/sph/sph_run.cu:285-336 (hash, sort, reorder,
+// SPH_NS, PC_prediction, recover, then the same for PC_correction).  Here one half step is
+//
+//   radix sort (cell key, slot)  ->  gather x -> y in cell order + dense cell starts
+//   ->  pass 1 (y -> aux)  ->  pass 2 + integrator (y, aux -> x, next cell keys)
+//
+// so the state never returns to original order inside a step (the original particle id
+// travels with it and is used only by sph_download), there is no separate hash kernel
+// (pass 2 writes the next keys), and no host synchronisation: a full step is 2 x 7 kernel
+// launches plus 2 memsets, captured once as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "sph_internal.h"
+
+using namespace sph;
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void**>(p), (count > 0 ? count : 1) * sizeof(T));
+}
+
+void free_set(ParticleSet& s) {
+    cudaFree(s.pos); cudaFree(s.vel); cudaFree(s.pres); cudaFree(s.id);
+    cudaFree(s.tpos); cudaFree(s.tvel);
+    s = ParticleSet{};
+}
+
+cudaError_t alloc_set(ParticleSet& s, int cap) {
+    cudaError_t e;
+    if ((e = dalloc(&s.pos, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.vel, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.pres, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.id, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.tpos, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.tvel, cap)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+void drop_graph(sph_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_stream = nullptr;
+    c->graph_n = -1;
+}
+
+void release(sph_ctx* c) {
+    drop_graph(c);
+    free_set(c->x);
+    free_set(c->y);
+    cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm); cudaFree(c->aux);
+    cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+}
+
+int to_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
+
+bool params_ok(const sph_params* p) {
+    return p && p->num_cells > 0 && p->grid_dim[0] > 0 && p->grid_dim[1] > 0 &&
+           p->grid_dim[2] > 0 && p->cell_size > 0.f && p->h > 0.f && p->kh > 0.f &&
+           p->rho0 > 0.f && p->cs > 0.f &&
+           // the 27-cell walk needs cells at least as wide as the support radius
+           p->cell_size >= p->kh &&
+           (long long)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2] == p->num_cells &&
+           p->num_cells < (1 << 30);
+}
+
+// One half step (see the file comment).  `ev` (may be NULL) receives 5 timestamps.
+cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev) {
+    const KParams k = make_kparams(c->P, c->n);
+    const int bits = key_bits_for(c->P.num_cells);
+    cudaError_t e;
+    if (ev) cudaEventRecord(ev[0], s);
+    e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
+                         c->sort_scratch_bytes, c->err, s);
+    if (e != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[1], s);
+    if ((e = launch_gather(k, c->perm, c->x, c->y, half == HALF_CORRECT, s)) != cudaSuccess) return e;
+    if ((e = build_cell_starts(c->keys_sorted, c->n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
+        return e;
+    if (ev) cudaEventRecord(ev[2], s);
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, c->aux, nullptr, nullptr, s)) !=
+        cudaSuccess)
+        return e;
+    if (ev) cudaEventRecord(ev[3], s);
+    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, c->aux, c->x, c->hash_x,
+                          c->err, s);
+    if (ev) cudaEventRecord(ev[4], s);
+    return e;
+}
+
+cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
+    cudaError_t e = half_step(c, HALF_PREDICT, s, ev);
+    if (e != cudaSuccess) return e;
+    return half_step(c, HALF_CORRECT, s, ev ? ev + 5 : nullptr);
+}
+
+}  // namespace
+
+extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
+    if (!out) return SPH_ERR_ARG;
+    *out = nullptr;
+    if (!params_ok(p) || capacity < 0 || p->num_particles > capacity) return SPH_ERR_ARG;
+    sph_ctx* c = new (std::nothrow) sph_ctx();
+    if (!c) return SPH_ERR_NOMEM;
+    c->P = *p;
+    c->capacity = capacity;
+    cudaGetDevice(&c->device);
+    cudaError_t e = cudaSuccess;
+    const int cap = capacity;
+    if (e == cudaSuccess) e = alloc_set(c->x, cap);
+    if (e == cudaSuccess) e = alloc_set(c->y, cap);
+    if (e == cudaSuccess) e = dalloc(&c->hash_x, cap);
+    if (e == cudaSuccess) e = dalloc(&c->keys_sorted, cap);
+    if (e == cudaSuccess) e = dalloc(&c->perm, cap);
+    if (e == cudaSuccess) e = dalloc(&c->aux, cap);
+    if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)p->num_cells + 1);
+    c->cell_capacity = p->num_cells;
+    c->sort_scratch_bytes = sort_scratch_bytes(cap);
+    if (e == cudaSuccess) e = cudaMalloc(&c->sort_scratch, c->sort_scratch_bytes);
+    if (e == cudaSuccess) e = dalloc(&c->err, 1);
+    if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
+    for (auto& ev : c->ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) {
+        release(c);
+        delete c;
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SPH_ERR_NOMEM : SPH_ERR_CUDA;
+    }
+    *out = c;
+    return SPH_OK;
+}
+
+extern "C" int sph_destroy(sph_ctx* c) {
+    if (!c) return SPH_ERR_ARG;
+    release(c);
+    delete c;
+    return SPH_OK;
+}
+
+extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
+    if (!c || !params_ok(p)) return SPH_ERR_ARG;
+    if (p->num_cells > c->cell_capacity) {
+        // the one place besides sph_create that allocates: a grid with more cells
+        int* cs = nullptr;
+        if (dalloc(&cs, (size_t)p->num_cells + 1) != cudaSuccess) {
+            cudaGetLastError();
+            return SPH_ERR_NOMEM;
+        }
+        cudaFree(c->cell_start);
+        c->cell_start = cs;
+        c->cell_capacity = p->num_cells;
+    }
+    c->P = *p;
+    drop_graph(c);
+    return SPH_OK;
+}
+
+extern "C" int sph_get_params(const sph_ctx* c, sph_params* out) {
+    if (!c || !out) return SPH_ERR_ARG;
+    *out = c->P;
+    return SPH_OK;
+}
+
+extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
+    if (!c) return SPH_ERR_ARG;
+    switch (option) {
+        case SPH_OPT_USE_GRAPH: c->opt_use_graph = value != 0; drop_graph(c); return SPH_OK;
+        case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
+        case SPH_OPT_PROFILE: c->opt_profile = value != 0; return SPH_OK;
+        default: return SPH_ERR_ARG;
+    }
+}
+
+extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const float* rho,
+                          const float* p, const int* type, int n, int from_host, void* stream) {
+    if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
+    if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n != c->n) drop_graph(c);
+    c->n = n;
+    c->steps = 0;
+    c->loaded = true;
+    if (n == 0) return SPH_OK;
+    const float* dpos = pos;
+    const float* dvel = vel;
+    const float* drho = rho;
+    const float* dp = p;
+    const int* dtype = type;
+    if (from_host) {
+        // stage the host arrays in the (free) sorted set's memory
+        float* spos = reinterpret_cast<float*>(c->y.pos);
+        float* svel = reinterpret_cast<float*>(c->y.vel);
+        float* srho = c->y.pres;
+        float* sp = reinterpret_cast<float*>(c->y.tpos);
+        int* stype = c->y.id;
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(spos, pos, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(svel, vel, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(srho, rho, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(sp, p, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(stype, type, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return SPH_ERR_CUDA;
+        dpos = spos; dvel = svel; drho = srho; dp = sp; dtype = stype;
+    }
+    KParams k = make_kparams(c->P, n);
+    return to_status(launch_upload_convert(k, dpos, dvel, drho, dp, dtype, c->x, c->hash_x, c->err, s));
+}
+
+extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, float* p, int* type,
+                            int to_host, void* stream) {
+    if (!c) return SPH_ERR_ARG;
+    if (!c->loaded) return SPH_ERR_STATE;
+    const int n = c->n;
+    if (n == 0) return SPH_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    KParams k = make_kparams(c->P, n);
+    if (!to_host)
+        return to_status(launch_download_convert(k, c->x, pos, vel, rho, p, type, s));
+    float* spos = pos ? reinterpret_cast<float*>(c->y.pos) : nullptr;
+    float* svel = vel ? reinterpret_cast<float*>(c->y.vel) : nullptr;
+    float* srho = rho ? c->y.pres : nullptr;
+    float* sp = p ? reinterpret_cast<float*>(c->y.tpos) : nullptr;
+    int* stype = type ? c->y.id : nullptr;
+    cudaError_t e = launch_download_convert(k, c->x, spos, svel, srho, sp, stype, s);
+    if (e != cudaSuccess) return SPH_ERR_CUDA;
+    if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (vel && cudaMemcpyAsync(vel, svel, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (rho && cudaMemcpyAsync(rho, srho, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (p && cudaMemcpyAsync(p, sp, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (type && cudaMemcpyAsync(type, stype, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess))
+        return SPH_ERR_CUDA;
+    return SPH_OK;
+}
+
+extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
+    if (!c || nsteps < 0) return SPH_ERR_ARG;
+    if (!c->loaded) return SPH_ERR_STATE;
+    if (c->n == 0 || nsteps == 0) {
+        c->steps += nsteps;
+        return SPH_OK;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (c->opt_profile) {
+        for (int i = 0; i < nsteps; i++) {
+            cudaError_t e = full_step(c, s, c->ev);
+            if (e != cudaSuccess) return SPH_ERR_CUDA;
+            if (cudaEventSynchronize(c->ev[9]) != cudaSuccess) return SPH_ERR_CUDA;
+            for (int h = 0; h < 2; h++)
+                for (int ph = 0; ph < PH_COUNT; ph++) {
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, c->ev[5 * h + ph], c->ev[5 * h + ph + 1]);
+                    c->phase_ms[ph] += ms;
+                    c->phase_launches[ph] += 1;
+                }
+            c->steps++;
+        }
+        return SPH_OK;
+    }
+    const bool graph_ok = c->opt_use_graph && s != nullptr;
+    if (!graph_ok) {
+        for (int i = 0; i < nsteps; i++) {
+            if (full_step(c, s, nullptr) != cudaSuccess) return SPH_ERR_CUDA;
+            c->steps++;
+        }
+        return SPH_OK;
+    }
+    if (!c->graph || c->graph_stream != s || c->graph_n != c->n) {
+        drop_graph(c);
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return SPH_ERR_CUDA;
+        cudaError_t e = full_step(c, s, nullptr);
+        cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return SPH_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            c->graph = nullptr;
+            return SPH_ERR_CUDA;
+        }
+        c->graph_stream = s;
+        c->graph_n = c->n;
+    }
+    for (int i = 0; i < nsteps; i++) {
+        if (cudaGraphLaunch(c->graph, s) != cudaSuccess) return SPH_ERR_CUDA;
+        c->steps++;
+    }
+    return SPH_OK;
+}
+
+extern "C" int sph_step_host(sph_ctx* c, float* pos, float* vel, float* rho, float* p, int* type,
+                             int n, int nsteps, void* stream) {
+    int st = sph_upload(c, pos, vel, rho, p, type, n, 1, stream);
+    if (st != SPH_OK) return st;
+    st = sph_step(c, nsteps, stream);
+    if (st != SPH_OK) return st;
+    st = sph_download(c, pos, vel, rho, p, nullptr, 1, stream);
+    if (st != SPH_OK) return st;
+    return cudaStreamSynchronize((cudaStream_t)stream) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_ctx_sorted_view(sph_ctx* c, const int** cell_start, const int** sorted_id,
+                                   const int** sorted_hash) {
+    if (!c) return SPH_ERR_ARG;
+    if (cell_start) *cell_start = c->cell_start;
+    if (sorted_id) *sorted_id = c->y.id;
+    if (sorted_hash) *sorted_hash = reinterpret_cast<const int*>(c->keys_sorted);
+    return SPH_OK;
+}
+
+extern "C" int sph_read_error_flags(sph_ctx* c, unsigned* flags, void* stream) {
+    if (!c || !flags) return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess ||
+        cudaMemsetAsync(c->err, 0, sizeof(unsigned), s) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    *flags = h;
+    return SPH_OK;
+}
+
+extern "C" int sph_steps_taken(const sph_ctx* c, long long* steps) {
+    if (!c || !steps) return SPH_ERR_ARG;
+    *steps = c->steps;
+    return SPH_OK;
+}
+
+extern "C" int sph_profile_read(sph_ctx* c, double* ms, long long* launches, int reset) {
+    if (!c) return SPH_ERR_ARG;
+    for (int i = 0; i < PH_COUNT; i++) {
+        if (ms) ms[i] = c->phase_ms[i];
+        if (launches) launches[i] = c->phase_launches[i];
+        if (reset) {
+            c->phase_ms[i] = 0.0;
+            c->phase_launches[i] = 0;
+        }
+    }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------- drop-in SPH_NS
+extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, float* s_p,
+                      const int* s_type, float* rho_dt, float* vel_dt, const int* cell_start,
+                      const int* cell_end, int n, const int* hash, float* dofv, float* rhop_sum,
+                      float* w_sum, void* stream) {
+    (void)cell_start;
+    (void)cell_end;  // the dense cell starts are rebuilt from the sorted hash
+    if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
+    if (n == 0) return SPH_OK;
+    if (!s_pos || !s_vel || !s_rho || !s_p || !s_type || !rho_dt || !vel_dt || !hash || !dofv)
+        return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    KParams k = make_kparams(c->P, n);
+    cudaError_t e;
+    if ((e = launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->y, c->keys_sorted,
+                               c->err, s)) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, c->aux, rhop_sum, w_sum, s)) !=
+        cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, c->aux, rho_dt, vel_dt,
+                                c->opt_wall_rates, s)) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((e = launch_ns_writeback(k, s_type, c->aux, s_rho, s_p, dofv, s)) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    return SPH_OK;
+}

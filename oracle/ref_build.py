@@ -1,0 +1,89 @@
+"""Recipe for oracle/_ref: the reference solver's own kernels, compiled from its sources.
+TEST INFRASTRUCTURE ONLY.
+
+  build_fatbin()  — where the reference sources are present (this container): compiles the
+                    reference's src/ tree (lib/mesh.cu, equation/ns.cu, sph/sph_run.cu with
+                    its main renamed) as one translation unit into an sm_103a fatbin,
+                    oracle/_ref/ref_src.fatbin.  Device code does not depend on the host CPU,
+                    so the same file serves the aarch64 GPU hosts, where the sources are absent.
+  build_harness() — anywhere with nvcc: compiles oracle/ref_harness.cu (this project's
+                    driver-API loader) into oracle/_ref/libref_harness.so.
+
+Nothing from the reference is copied: the unity file holds three #include lines that point
+into the reference tree, and outputs go only to oracle/_ref/ (git-ignored).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REFERENCE = "/root/reference"
+FATBIN = os.path.join(OUT, "ref_src.fatbin")
+HARNESS = os.path.join(OUT, "libref_harness.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for c in ("/usr/local/cuda/bin/nvcc", shutil.which("nvcc") or ""):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def reference_present() -> bool:
+    return os.path.isdir(os.path.join(REFERENCE, "src", "equation"))
+
+
+def build_fatbin(force: bool = False) -> str | None:
+    if not reference_present():
+        return FATBIN if os.path.exists(FATBIN) else None
+    if os.path.exists(FATBIN) and not force:
+        return FATBIN
+    os.makedirs(OUT, exist_ok=True)
+    unity = os.path.join(OUT, "unity_src.cu")
+    with open(unity, "w") as f:
+        f.write('#define main reference_main\n#include "lib/mesh.cu"\n'
+                '#include "equation/ns.cu"\n#include "sph/sph_run.cu"\n')
+    src = os.path.join(REFERENCE, "src")
+    cmd = [nvcc(), "-fatbin", *ARCH, "-O3", "-w", "-I" + src, "-I" + os.path.join(src, "header"),
+           unity, "-o", FATBIN + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference fatbin build failed:\n{r.stderr[-3000:]}")
+    os.replace(FATBIN + ".tmp", FATBIN)
+    return FATBIN
+
+
+def build_harness(force: bool = False) -> str:
+    src = os.path.join(HERE, "ref_harness.cu")
+    if (os.path.exists(HARNESS) and not force
+            and os.path.getmtime(HARNESS) > os.path.getmtime(src)
+            and _machine_stamp_ok()):
+        return HARNESS
+    os.makedirs(OUT, exist_ok=True)
+    cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", src,
+           "-o", HARNESS + ".tmp", "-lcuda"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"harness build failed:\n{r.stderr[-3000:]}")
+    os.replace(HARNESS + ".tmp", HARNESS)
+    with open(os.path.join(OUT, "harness.machine"), "w") as f:
+        f.write(os.uname().machine)
+    return HARNESS
+
+
+def _machine_stamp_ok() -> bool:
+    p = os.path.join(OUT, "harness.machine")
+    return os.path.exists(p) and open(p).read().strip() == os.uname().machine
+
+
+def build(force: bool = False) -> dict:
+    return {"fatbin": build_fatbin(force), "harness": build_harness(force)}
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,130 @@
+"""Generate the golden fixtures that pin the CPU oracle to the reference.
+
+Runs the reference solver's own kernels (src/, compiled from its sources into
+oracle/_ref/ref_src.fatbin and launched by oracle/ref_harness.cu with the reference's launch
+shapes, thrust::sort_by_key for the sort) on a GPU, on seeded inputs from the dam-break
+generator, and stores inputs and outputs as compressed .npz files next to this script:
+
+  ref_cells_<case>.npz  calcHash -> sortParticles -> reorder: hash (unsorted and sorted),
+                        index, cellStart, cellEnd, gathered arrays
+  ref_ns_<case>.npz     SPH_NS_simpleversion on the reorder output (perturbed velocities and
+                        densities): densitydt, Veldt, dofv, rhop_sum, w_sum, wall p / rho
+  ref_pc_<case>.npz     PC_prediction then PC_correction with given rates
+  ref_run_<case>.npz    whole steps of the src step loop: state after 1 and after 5 steps
+
+Usage (on a machine with a CUDA GPU and the fatbin):
+    python tests/golden/make_golden.py [outdir]
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+# (name, case, dx, jitter, physics): small enough to keep each fixture at a few hundred kB
+CASES = [
+    ("tank_dx30", "small", 0.03, 0.01, "reference"),
+    ("tank_tait_dx30", "small", 0.03, 0.01, "config"),
+    ("refcase_dx50", "refcase", 0.05, 0.02, "reference"),
+]
+
+
+def gen_state(case, dx, jitter, physics):
+    from tmp_sph_gb300 import cases
+    st, p = cases.build(case, physics=physics, dx=dx, jitter=jitter, seed=12345)
+    return st, p
+
+
+def perturb(st, seed=7):
+    rng = np.random.default_rng(seed)
+    out = {k: v.copy() for k, v in st.items() if isinstance(v, np.ndarray)}
+    fl = out["type"] == 1
+    out["vel"][fl] = rng.uniform(-0.3, 0.3, (fl.sum(), 3)).astype(np.float32)
+    out["rho"][fl] = (1000.0 * (1.0 + rng.uniform(0, 0.02, fl.sum()))).astype(np.float32)
+    out["p"][fl] = (625.0 * (out["rho"][fl] - 1000.0)).astype(np.float32)
+    return out
+
+
+def params_arrays(P) -> dict:
+    return {"param_" + k: np.asarray(v) for k, v in P.as_dict().items()}
+
+
+def main(outdir=HERE):
+    import torch
+    from oracle import oracle as O
+    from oracle.ref_harness import RefHarness
+    cuda = torch.device("cuda:0")
+    H = RefHarness()
+    os.makedirs(outdir, exist_ok=True)
+    for name, case, dx, jitter, physics in CASES:
+        st, p = gen_state(case, dx, jitter, physics)
+        P = O.params_like(p)
+        n = len(st["rho"])
+        if physics != "reference":
+            # the reference kernels only know the linear EOS; Tait cases pin the cell list and
+            # the neighbour pass on a Tait-consistent state (p given), not the integrator
+            pass
+        H.set_params(P, n)
+        host = lambda t: t.detach().cpu().numpy()
+        common = params_arrays(P)
+        # ---- cell list
+        d, s, w, tmp = H.alloc(perturb(st), cuda)
+        H.calc_hash(d["pos"], w["hash"], w["index"])
+        H.sync()
+        hash_unsorted = host(w["hash"]).copy()
+        H.sort(w["hash"], w["index"])
+        H.reorder(d, s, w["hash"], w["index"], w["cs"], w["ce"])
+        H.sync()
+        pst = perturb(st)
+        np.savez_compressed(
+            os.path.join(outdir, f"ref_cells_{name}.npz"), **common,
+            in_pos=pst["pos"], in_vel=pst["vel"], in_rho=pst["rho"], in_p=pst["p"], in_type=pst["type"],
+            hash_unsorted=hash_unsorted, hash=host(w["hash"]), index=host(w["index"]),
+            cell_start=host(w["cs"]), cell_end=host(w["ce"]),
+            s_pos=host(s["pos"]), s_vel=host(s["vel"]), s_rho=host(s["rho"]), s_p=host(s["p"]),
+            s_type=host(s["type"]))
+        # ---- neighbour passes on the sorted, perturbed state
+        H.ns(s, w, w["cs"], w["ce"], w["hash"])
+        H.sync()
+        np.savez_compressed(
+            os.path.join(outdir, f"ref_ns_{name}.npz"),
+            rho_dt=host(w["rho_dt"]), vel_dt=host(w["vel_dt"]), dofv=host(w["dofv"]),
+            rhop_sum=host(w["rhop_sum"]), w_sum=host(w["w_sum"]), p_after=host(s["p"]),
+            rho_after=host(s["rho"]))
+        if physics == "reference":
+            # ---- integrator with the rates just computed
+            before = {k: host(s[k]).copy() for k in ("pos", "vel", "rho", "p")}
+            H.pc(0, s, w, w["index"], tmp)
+            H.sync()
+            pred = {k: host(s[k]).copy() for k in ("pos", "vel", "rho", "p")}
+            tmp_pred = {k: host(v).copy() for k, v in tmp.items()}
+            H.pc(1, s, w, w["index"], tmp)
+            H.sync()
+            np.savez_compressed(
+                os.path.join(outdir, f"ref_pc_{name}.npz"),
+                **{"before_" + k: v for k, v in before.items()},
+                **{"pred_" + k: v for k, v in pred.items()},
+                **{"tmp_" + k: v for k, v in tmp_pred.items()},
+                **{"corr_" + k: host(s[k]) for k in ("pos", "vel", "rho", "p")})
+            # ---- whole steps from the unperturbed (hydrostatic) state
+            d, s, w, tmp = H.alloc(st, cuda)
+            H.step(d, s, w, tmp, 1)
+            H.sync()
+            one = {k: host(d[k]).copy() for k in ("pos", "vel", "rho", "p")}
+            H.step(d, s, w, tmp, 4)
+            H.sync()
+            np.savez_compressed(
+                os.path.join(outdir, f"ref_run_{name}.npz"), **common,
+                in_pos=st["pos"], in_vel=st["vel"], in_rho=st["rho"], in_p=st["p"], in_type=st["type"],
+                **{"step1_" + k: v for k, v in one.items()},
+                **{"step5_" + k: host(d[k]) for k in ("pos", "vel", "rho", "p")})
+        print(f"{name}: n={n} cells={P.num_cells}", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE)

@@ -16,8 +16,8 @@ from gpu_util import dev, host, perturbed
 
 pytestmark = pytest.mark.gpu
 
-TOL_RATE = 2e-4   # rho_dt, vel_dt, dofv
-TOL_WALL = 1e-5   # extrapolated wall pressure / density, rhop_sum, w_sum
+TOL_RATE = 5e-5   # rho_dt, vel_dt, dofv (measured <= 1e-5)
+TOL_WALL = 2e-6   # wall pressure / density, rhop_sum, w_sum (measured <= 4e-7)
 
 
 def run_both(oracle, cuda, st, p, wall_rates=False):

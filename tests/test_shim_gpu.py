@@ -92,9 +92,9 @@ def test_reference_step_loop_through_shim(sphlib, oracle, cuda, report, physics)
     e_x = rel_l2(out["pos"][fl] - st["pos"][fl], ref["pos"][fl] - st["pos"][fl])
     e_v = rel_l2(out["vel"][fl], ref["vel"][fl], floor=1e-3 * np.sqrt(fl.sum()))
     e_r = rel_l2(out["rho"][fl] - 1000, ref["rho"][fl] - 1000)
-    report(f"shim step {physics} disp", e_x, 1e-4)
-    report(f"shim step {physics} vel", e_v, 1e-4)
-    report(f"shim step {physics} drho", e_r, 1e-4)
-    assert e_x < 1e-4 and e_v < 1e-4 and e_r < 1e-4
+    report(f"shim step {physics} disp", e_x, 2e-5)
+    report(f"shim step {physics} vel", e_v, 2e-5)
+    report(f"shim step {physics} drho", e_r, 2e-5)
+    assert e_x < 2e-5 and e_v < 2e-5 and e_r < 2e-5
     assert np.array_equal(out["type"], st["type"])
     api.call("sph_shim_release")

@@ -72,10 +72,17 @@ def geometry(name: str, *, dx: float | None = None, block=None, tank=None,
     return d
 
 
+def lattice_extent(length: float, dx: float) -> float:
+    """Extent actually covered by the generator's lattice along one tank axis
+    (round(length/dx) cells of width dx)."""
+    return math.floor(float(length) / float(dx) + 0.5) * float(dx)
+
+
 def config(d: api.SphDamBreak, physics: str = "config", n: int = 0, nb: int = 0,
            cell_factor: float = 1.0) -> api.SphConfig:
-    """Physics configuration for a generated geometry (escape box = the tank, 5 cm above
-    its rim; parking point 8 cm below the floor, as in the reference)."""
+    """Physics configuration for a generated geometry: grid = tank padded by 0.1 m (more when
+    the wall layers are thicker than that), escape box = the lattice tank, 5 cm above its rim,
+    parking point 8 cm below the floor as in the reference."""
     c = api.SphConfig()
     c.dx = d.dx
     c.rho0 = 1000.0
@@ -89,13 +96,15 @@ def config(d: api.SphDamBreak, physics: str = "config", n: int = 0, nb: int = 0,
     else:
         raise ValueError(physics)
     c.tait_gamma = 7.0
+    tank = [lattice_extent(t, d.dx) for t in d.tank]
     c.domain_min = api.F3(0.0, 0.0, 0.0)
-    c.domain_max = api.F3(*d.tank)
-    c.pad = 0.1
+    c.domain_max = api.F3(*tank)
+    # the wall layers (and a cell of margin) must stay inside the padded grid
+    c.pad = max(0.1, (d.wall_layers + 1.5) * float(d.dx))
     c.cell_factor = cell_factor
     c.escape_min = api.F3(0.0, 0.0, 0.0)
-    c.escape_max = api.F3(d.tank[0], d.tank[1], d.tank[2] + 0.05)
-    c.escape_park = api.F3(0.0, 0.5 * d.tank[1], -0.08)
+    c.escape_max = api.F3(tank[0], tank[1], tank[2] + 0.05)
+    c.escape_park = api.F3(0.0, 0.5 * tank[1], -0.08 - (c.pad - 0.1))
     c.num_particles = n
     c.num_boundary = nb
     c.clamp_density = 1

@@ -64,6 +64,28 @@ void release(sph_ctx* c) {
 
 int to_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
 
+// Device staging for host transfers, carved from buffers that hold nothing between steps
+// (the predictor's saved state of the sorted set and the pass-1 output), so the sorted view
+// of the last step (y.pos/vel/id, sorted keys, cell starts) survives an upload/download.
+struct Staging {
+    float* pos;   // 3n floats
+    float* vel;   // 3n floats
+    float* rho;   // n
+    float* p;     // n
+    int* type;    // n
+};
+
+Staging staging(sph_ctx* c, int n) {
+    Staging s;
+    s.pos = reinterpret_cast<float*>(c->y.tpos);
+    s.vel = reinterpret_cast<float*>(c->y.tvel);
+    float* a = reinterpret_cast<float*>(c->aux);
+    s.rho = a;
+    s.p = a + n;
+    s.type = reinterpret_cast<int*>(a + 2 * (size_t)n);
+    return s;
+}
+
 bool params_ok(const sph_params* p) {
     return p && p->num_cells > 0 && p->grid_dim[0] > 0 && p->grid_dim[1] > 0 &&
            p->grid_dim[2] > 0 && p->cell_size > 0.f && p->h > 0.f && p->kh > 0.f &&
@@ -109,7 +131,7 @@ cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
 extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (!out) return SPH_ERR_ARG;
     *out = nullptr;
-    if (!params_ok(p) || capacity < 0 || p->num_particles > capacity) return SPH_ERR_ARG;
+    if (!params_ok(p) || capacity < 0) return SPH_ERR_ARG;
     sph_ctx* c = new (std::nothrow) sph_ctx();
     if (!c) return SPH_ERR_NOMEM;
     c->P = *p;
@@ -198,12 +220,12 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
     const float* dp = p;
     const int* dtype = type;
     if (from_host) {
-        // stage the host arrays in the (free) sorted set's memory
-        float* spos = reinterpret_cast<float*>(c->y.pos);
-        float* svel = reinterpret_cast<float*>(c->y.vel);
-        float* srho = c->y.pres;
-        float* sp = reinterpret_cast<float*>(c->y.tpos);
-        int* stype = c->y.id;
+        Staging st = staging(c, n);
+        float* spos = st.pos;
+        float* svel = st.vel;
+        float* srho = st.rho;
+        float* sp = st.p;
+        int* stype = st.type;
         cudaError_t e;
         if ((e = cudaMemcpyAsync(spos, pos, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
             (e = cudaMemcpyAsync(svel, vel, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
@@ -227,11 +249,12 @@ extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, floa
     KParams k = make_kparams(c->P, n);
     if (!to_host)
         return to_status(launch_download_convert(k, c->x, pos, vel, rho, p, type, s));
-    float* spos = pos ? reinterpret_cast<float*>(c->y.pos) : nullptr;
-    float* svel = vel ? reinterpret_cast<float*>(c->y.vel) : nullptr;
-    float* srho = rho ? c->y.pres : nullptr;
-    float* sp = p ? reinterpret_cast<float*>(c->y.tpos) : nullptr;
-    int* stype = type ? c->y.id : nullptr;
+    Staging st = staging(c, n);
+    float* spos = pos ? st.pos : nullptr;
+    float* svel = vel ? st.vel : nullptr;
+    float* srho = rho ? st.rho : nullptr;
+    float* sp = p ? st.p : nullptr;
+    int* stype = type ? st.type : nullptr;
     cudaError_t e = launch_download_convert(k, c->x, spos, svel, srho, sp, stype, s);
     if (e != cudaSuccess) return SPH_ERR_CUDA;
     if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||

@@ -43,9 +43,11 @@ UNIT = "particle-steps/s"
 # neighbour pass 2 60, integrator 102 (mean of predictor 108 and corrector 96).
 B_HASH, B_SORT, B_PERMUTE, B_PASS1, B_PASS2, B_INTEGRATE = 20, 16, 80, 52, 60, 102
 # Phase -> algorithmic bytes per particle per launch of the fused kernels
-PHASE_BYTES = {"sort": B_SORT, "gather_cells": B_PERMUTE, "pass1": B_PASS1,
+PHASE_BYTES = {"sort": B_SORT, "gather_cells": B_PERMUTE, "nbr_build": 16, "pass1": B_PASS1,
                "pass2_integrate": B_PASS2 + B_INTEGRATE + B_HASH}
-PHASE_KERNEL = {"sort": "k_rs_upsweep/k_rs_scan/k_rs_downsweep", "gather_cells": "k_gather + k_cell_mark/k_cell_fill",
+PHASE_KERNEL = {"sort": "k_rs_upsweep/k_rs_scan/k_rs_downsweep",
+                "gather_cells": "k_gather + k_cell_mark/k_cell_fill",
+                "nbr_build": "k_nbr_build (one cell walk; positions read once = 16 B)",
                 "pass1": "k_pass1", "pass2_integrate": "k_pass2<MODE_PRED|MODE_CORR>"}
 
 
@@ -143,8 +145,9 @@ def launches_per_step(p) -> int:
     while bits < 31 and (1 << bits) < p.num_cells:
         bits += 1
     passes = (bits + 7) // 8
-    # per half step: 3 kernels per radix pass, gather, cell mark, cell fill, pass 1, pass 2
-    return 2 * (3 * passes + 5)
+    # per half step: 3 kernels per radix pass, gather, cell mark, cell fill, neighbour-list
+    # build, pass 1, pass 2
+    return 2 * (3 * passes + 6)
 
 
 def cpu_baseline(st, p, budget_s: float = 20.0) -> dict:

@@ -51,6 +51,8 @@ typedef enum sph_status {
 #define SPH_FLAG_OUT_OF_GRID   0x1u  /* a particle hashed outside the grid; its cell index was clamped */
 #define SPH_FLAG_KEY_RANGE     0x2u  /* a sort key was outside [0, 2^key_bits) */
 #define SPH_FLAG_NONFINITE     0x4u  /* a non-finite position was seen by the hash kernel */
+#define SPH_FLAG_NEIGHBOR_OVERFLOW 0x8u  /* a particle had more neighbours than the list holds;
+                                            it walked its cells instead (results unaffected) */
 
 /* EOS selector: the reference hard-codes the linear form p = cs^2 (rho - rho0)
  * (src/sph/sph_run.cu:467,515); TAIT is p = B((rho/rho0)^gamma - 1), B = rho0 cs^2/gamma. */
@@ -217,10 +219,15 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_USE_GRAPH     1  /* 1: sph_step replays one captured CUDA graph per step */
 #define SPH_OPT_WALL_RATES    2  /* 1: sph_ns also fills rho_dt/vel_dt rows of boundary particles */
 #define SPH_OPT_PROFILE       3  /* 1: sph_step times each phase with CUDA events (no graph; syncs per step) */
+#define SPH_OPT_NEIGHBOR_LIST 4  /* 1 (default): one cell walk per half step fills a neighbour
+                                    list both passes iterate; 0: each pass walks the cells */
+#define SPH_OPT_NEIGHBOR_CAP  5  /* list slots per particle; 0 (default) = 1.5x the lattice
+                                    neighbours of the support sphere (reallocates the list) */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
- * [2] neighbour pass 1, [3] neighbour pass 2 + integrator; summed over half steps. */
-#define SPH_PHASE_COUNT 4
+ * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;
+ * summed over half steps. */
+#define SPH_PHASE_COUNT 5
 
 /* Create a context on the current CUDA device for up to `capacity` particles (allocates all
  * state and scratch once).  p may describe fewer particles than capacity. */

@@ -1,0 +1,151 @@
+"""Pins of the CPU oracle against the reference itself.
+
+The fixtures in tests/golden/ were produced by running the reference solver's own kernels
+(src/, compiled from its sources, launched with its own launch shapes and
+thrust::sort_by_key) on a GB300 — tests/golden/make_golden.py is the generating script.  The
+oracle must reproduce them: the cell list bit for bit, the neighbour passes, the integrator
+and whole steps within the float-rounding tolerances stated below (the reference build
+contracts multiply-adds into FMAs; the oracle rounds every operation).  The reference kernels
+implement only the linear EOS, so the Tait-constants case is compared with eos = 0."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_l2
+
+GOLD = os.path.join(ROOT, "tests", "golden")
+CASES = sorted({os.path.basename(f)[len("ref_cells_"):-4]
+                for f in glob.glob(os.path.join(GOLD, "ref_cells_*.npz"))})
+
+TOL_NS = 2e-6     # relative L2, neighbour-pass outputs
+TOL_PC = 1e-6     # relative L2 of the state change, predictor / corrector
+TOL_RUN1 = 1e-5   # relative L2 after one whole step
+TOL_RUN5 = 1e-4   # after five
+
+
+def load(kind, case):
+    path = os.path.join(GOLD, f"ref_{kind}_{case}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"no {kind} fixture for {case}")
+    return np.load(path)
+
+
+def oracle_params(O, d):
+    P = O.OrParams()
+    for name, ctype in O.OrParams._fields_:
+        v = d["param_" + name]
+        setattr(P, name, ctype(*v.tolist()) if v.ndim else v.item())
+    P.eos = 0
+    return P
+
+
+def inputs(d):
+    return {"pos": d["in_pos"].copy(), "vel": d["in_vel"].copy(), "rho": d["in_rho"].copy(),
+            "p": d["in_p"].copy(), "type": d["in_type"].copy()}
+
+
+def test_fixtures_present():
+    assert len(CASES) >= 3, CASES
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cell_list_bit_exact(oracle, case):
+    d = load("cells", case)
+    P = oracle_params(oracle, d)
+    st = inputs(d)
+    h, idx = oracle.calc_hash(P, st["pos"])
+    assert np.array_equal(h, d["hash_unsorted"]) and np.array_equal(idx, np.arange(len(h)))
+    c = oracle.cell_list(P, st)
+    assert np.array_equal(c["hash"], d["hash"])
+    assert np.array_equal(c["index"], d["index"])
+    assert np.array_equal(c["cell_start"], d["cell_start"])
+    occ = d["cell_start"] >= 0
+    assert np.array_equal(c["cell_end"][occ], d["cell_end"][occ])
+    for k in ("pos", "vel", "rho", "p", "type"):
+        assert np.array_equal(c[k], d["s_" + k]), k
+
+
+def sorted_state(d):
+    return {"pos": d["s_pos"].copy(), "vel": d["s_vel"].copy(), "rho": d["s_rho"].copy(),
+            "p": d["s_p"].copy(), "type": d["s_type"].copy(), "hash": d["hash"].copy(),
+            "index": d["index"].copy(), "cell_start": d["cell_start"].copy(),
+            "cell_end": d["cell_end"].copy()}
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_neighbour_passes(oracle, report, case):
+    d = load("cells", case)
+    g = load("ns", case)
+    P = oracle_params(oracle, d)
+    s = sorted_state(d)
+    r = oracle.sph_ns(P, s)
+    fl = s["type"] == 1
+    wl = ~fl
+    e = {
+        "rho_dt": rel_l2(r["rho_dt"][fl], g["rho_dt"][fl]),
+        "vel_dt": rel_l2(r["vel_dt"], g["vel_dt"], floor=9.81 * np.sqrt(len(fl))),
+        "dofv": rel_l2(r["dofv"][fl], g["dofv"][fl]),
+        "rhop_sum": rel_l2(r["rhop_sum"][wl], g["rhop_sum"][wl]),
+        "w_sum": rel_l2(r["w_sum"][wl], g["w_sum"][wl]),
+        "wall_p": rel_l2(s["p"][wl], g["p_after"][wl]),
+        "wall_rho": rel_l2(s["rho"][wl], g["rho_after"][wl]),
+    }
+    for k, v in e.items():
+        report(f"oracle vs reference {case} {k}", v, TOL_NS)
+    assert all(v < TOL_NS for v in e.values()), e
+    assert np.array_equal(s["p"][fl], g["p_after"][fl])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES
+                                  if os.path.exists(os.path.join(GOLD, f"ref_pc_{c}.npz"))])
+def test_predictor_corrector(oracle, report, case):
+    d = load("cells", case)
+    g = load("ns", case)
+    pc = load("pc", case)
+    P = oracle_params(oracle, d)
+    n = len(d["index"])
+    s = {k: pc["before_" + k].copy() for k in ("pos", "vel", "rho", "p")}
+    s.update(type=d["s_type"].copy(), index=d["index"].copy())
+    rates = {"rho_dt": g["rho_dt"], "vel_dt": g["vel_dt"]}
+    tmp = {"pos": np.zeros((n, 3), np.float32), "vel": np.zeros((n, 3), np.float32),
+           "rho": np.zeros(n, np.float32)}
+    oracle.pc_prediction(P, s, rates, tmp)
+    fl = s["type"] == 1
+    for k in ("pos", "vel", "rho", "p"):
+        e = rel_l2((s[k] - pc["before_" + k])[fl], (pc["pred_" + k] - pc["before_" + k])[fl])
+        report(f"oracle vs reference {case} predictor {k}", e, TOL_PC)
+        assert e < TOL_PC, (k, e)
+    for k in ("pos", "vel", "rho"):
+        assert np.array_equal(tmp[k], pc["tmp_" + k]), k
+    s = {k: pc["pred_" + k].copy() for k in ("pos", "vel", "rho", "p")}
+    s.update(type=d["s_type"].copy(), index=d["index"].copy())
+    tmp = {k: pc["tmp_" + k].copy() for k in ("pos", "vel", "rho")}
+    oracle.pc_correction(P, s, rates, tmp)
+    for k in ("pos", "vel", "rho", "p"):
+        e = rel_l2((s[k] - pc["pred_" + k])[fl], (pc["corr_" + k] - pc["pred_" + k])[fl])
+        report(f"oracle vs reference {case} corrector {k}", e, TOL_PC)
+        assert e < TOL_PC, (k, e)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES
+                                  if os.path.exists(os.path.join(GOLD, f"ref_run_{c}.npz"))])
+def test_whole_steps(oracle, report, case):
+    d = load("run", case)
+    P = oracle_params(oracle, d)
+    st = inputs(d)
+    fl = st["type"] == 1
+    for nsteps, tol in ((1, TOL_RUN1), (5, TOL_RUN5)):
+        out = oracle.run(P, st, nsteps)
+        e = {
+            "disp": rel_l2((out["pos"] - st["pos"])[fl], (d[f"step{nsteps}_pos"] - st["pos"])[fl]),
+            "vel": rel_l2(out["vel"][fl], d[f"step{nsteps}_vel"][fl]),
+            "drho": rel_l2(out["rho"][fl] - 1000, d[f"step{nsteps}_rho"][fl] - 1000),
+        }
+        for k, v in e.items():
+            report(f"oracle vs reference {case} {nsteps} steps {k}", v, tol)
+        assert all(v < tol for v in e.values()), (nsteps, e)
+        assert np.array_equal(out["pos"][~fl], d[f"step{nsteps}_pos"][~fl])

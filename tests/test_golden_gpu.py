@@ -1,0 +1,116 @@
+"""The CUDA library against the reference's own outputs (tests/golden/, produced by the
+reference's kernels on a GB300 — see tests/golden/make_golden.py): bit-exact cell lists,
+neighbour passes and whole steps within float-rounding tolerance."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from gpu_util import dev, host
+from test_golden import CASES, GOLD, inputs, load
+
+pytestmark = pytest.mark.gpu
+
+
+def product_params(d):
+    from tmp_sph_gb300 import api
+    p = api.SphParams()
+    for name, ctype in api.SphParams._fields_:
+        v = d["param_" + name]
+        setattr(p, name, ctype(*v.tolist()) if v.ndim else v.item())
+    p.eos = api.SPH_EOS_LINEAR  # the reference kernels implement only the linear EOS
+    return p
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_cells_match_reference(sphlib, cuda, case):
+    import torch
+    from tmp_sph_gb300 import solver as S
+    d = load("cells", case)
+    p = product_params(d)
+    st = inputs(d)
+    n = len(st["rho"])
+    pos = dev(st["pos"], cuda)
+    h = torch.empty(n, dtype=torch.int32, device=cuda)
+    idx = torch.empty(n, dtype=torch.int32, device=cuda)
+    S.calc_hash(p, pos, h, idx, n)
+    assert np.array_equal(host(h), d["hash_unsorted"])
+    S.sort_particles(h, idx, n)
+    out = {k: torch.empty_like(dev(st[k], cuda)) for k in ("pos", "vel", "rho", "p", "type")}
+    cs = torch.empty(p.num_cells, dtype=torch.int32, device=cuda)
+    ce = torch.full((p.num_cells,), -7, dtype=torch.int32, device=cuda)
+    S.reorder(p, pos, dev(st["vel"], cuda), dev(st["rho"], cuda), dev(st["p"], cuda),
+              dev(st["type"], cuda), None, out["pos"], out["vel"], out["rho"], out["p"],
+              out["type"], None, h, idx, cs, ce, n)
+    assert np.array_equal(host(h), d["hash"])
+    assert np.array_equal(host(idx), d["index"])
+    assert np.array_equal(host(cs), d["cell_start"])
+    occ = d["cell_start"] >= 0
+    assert np.array_equal(host(ce)[occ], d["cell_end"][occ])
+    for k in out:
+        assert np.array_equal(host(out[k]), d["s_" + k]), k
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ns_matches_reference(sphlib, cuda, report, case):
+    import torch
+    from tmp_sph_gb300 import solver as S
+    d = load("cells", case)
+    g = load("ns", case)
+    p = product_params(d)
+    n = len(d["index"])
+    s = {k: dev(d["s_" + k], cuda) for k in ("pos", "vel", "rho", "p", "type")}
+    h = dev(d["hash"], cuda)
+    cs = dev(d["cell_start"], cuda)
+    ce = dev(d["cell_end"], cuda)
+    out = {"rho_dt": torch.zeros(n, device=cuda), "vel_dt": torch.zeros((n, 3), device=cuda),
+           "dofv": torch.zeros(n, device=cuda), "rhop_sum": torch.zeros(n, device=cuda),
+           "w_sum": torch.zeros(n, device=cuda)}
+    with S.Solver(p, n) as sol:
+        sol.ns(s["pos"], s["vel"], s["rho"], s["p"], s["type"], out["rho_dt"], out["vel_dt"], cs,
+               ce, n, h, out["dofv"], out["rhop_sum"], out["w_sum"])
+    o = {k: host(v) for k, v in out.items()}
+    fl = d["s_type"] == 1
+    wl = ~fl
+    e = {
+        "rho_dt": rel_l2(o["rho_dt"][fl], g["rho_dt"][fl]),
+        "vel_dt": rel_l2(o["vel_dt"][fl], g["vel_dt"][fl], floor=9.81 * np.sqrt(fl.sum())),
+        "dofv": rel_l2(o["dofv"][fl], g["dofv"][fl]),
+        "wall_p": rel_l2(host(s["p"])[wl], g["p_after"][wl]),
+        "wall_rho": rel_l2(host(s["rho"])[wl], g["rho_after"][wl]),
+        "rhop_sum": rel_l2(o["rhop_sum"][wl], g["rhop_sum"][wl]),
+        "w_sum": rel_l2(o["w_sum"][wl], g["w_sum"][wl]),
+    }
+    for k, v in e.items():
+        report(f"gpu vs reference {case} {k}", v, 5e-6)
+    assert all(v < 5e-6 for v in e.values()), e
+
+
+@pytest.mark.parametrize("case", [c for c in CASES
+                                  if os.path.exists(os.path.join(GOLD, f"ref_run_{c}.npz"))])
+def test_resident_steps_match_reference(sphlib, cuda, report, case):
+    import torch
+    from tmp_sph_gb300 import solver as S
+    d = load("run", case)
+    p = product_params(d)
+    st = inputs(d)
+    n = len(st["rho"])
+    fl = st["type"] == 1
+    s = torch.cuda.Stream()
+    for nsteps, tol in ((1, 2e-5), (5, 2e-4)):
+        with S.Solver(p, n) as sol:
+            sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+            sol.step(nsteps, stream=s)
+            out = sol.download(stream=s)
+        e = {
+            "disp": rel_l2((out["pos"] - st["pos"])[fl], (d[f"step{nsteps}_pos"] - st["pos"])[fl]),
+            "vel": rel_l2(out["vel"][fl], d[f"step{nsteps}_vel"][fl]),
+            "drho": rel_l2(out["rho"][fl] - 1000, d[f"step{nsteps}_rho"][fl] - 1000),
+        }
+        for k, v in e.items():
+            report(f"gpu resident vs reference {case} {nsteps} steps {k}", v, tol)
+        assert all(v < tol for v in e.values()), (nsteps, e)
+        assert np.array_equal(out["pos"][~fl], d[f"step{nsteps}_pos"][~fl])

@@ -36,8 +36,11 @@ SPH_TYPE_RIGID = 2
 SPH_OPT_USE_GRAPH = 1
 SPH_OPT_WALL_RATES = 2
 SPH_OPT_PROFILE = 3
-SPH_PHASE_COUNT = 4
-PHASE_NAMES = ("sort", "gather_cells", "pass1", "pass2_integrate")
+SPH_OPT_NEIGHBOR_LIST = 4
+SPH_OPT_NEIGHBOR_CAP = 5
+SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
+SPH_PHASE_COUNT = 5
+PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")
 
 F3 = C.c_float * 3
 I3 = C.c_int * 3

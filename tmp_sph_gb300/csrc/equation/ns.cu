@@ -10,6 +10,15 @@
 // contiguous slot range [cell_start[row + x-1], cell_start[row + x+2]) — the dense
 // cell_start array gives empty cells the start of the next non-empty one.
 //
+// Neighbour list.  About 15% of the ~475 candidates of a 27-cell walk lie inside the
+// support radius, and the lanes of a warp (particles of two or three adjacent cells) almost
+// always have at least one hit per candidate, so a pass that tests and evaluates in one loop
+// pays the full pair body for every candidate.  k_nbr_build therefore walks the candidates
+// once per half step and stores the hits, slot-major (idx[c * n + i], one coalesced row per
+// neighbour rank c), in walk order; both passes then iterate only true neighbours, in the
+// same order, so the sums are the same as a walking pass.  A particle with more hits than
+// the list capacity is marked and walks the cells itself (same order again).
+//
 // Kernel algebra (same quantities as the reference, simplified): with r = x_i - x_j,
 // q = |r|/h, t = 1 - q/2, the Wendland C2 gradient is grad W = c_fr t^3 r with
 // c_fr = -5 adh / h^2, which is the reference's per-component expression
@@ -30,6 +39,12 @@ __device__ __forceinline__ void cell_of_key(const KParams& k, unsigned key, int&
     cx = (int)(key - t * (unsigned)k.gx);
     cz = (int)(t / (unsigned)k.gy);
     cy = (int)(t - (unsigned)cz * (unsigned)k.gy);
+}
+
+// Squared distance with an explicit rounding sequence, so the in-range test gives the same
+// answer in the list build, in the walking passes and in the list passes.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
 // Visit every candidate slot j of the 27 cells around (cx, cy, cz), strip by strip.
@@ -55,13 +70,74 @@ __device__ __forceinline__ void for_each_candidate(const KParams& k, const int* 
     }
 }
 
+// Walk the cells of particle i and call f(j, pj, dx, dy, dz, r2) for every j != i within the
+// support radius.
+template <class F>
+__device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restrict__ cs,
+                                           const unsigned* __restrict__ keys,
+                                           const float4* __restrict__ P, int i, const float4& pi,
+                                           F&& f) {
+    int cx, cy, cz;
+    cell_of_key(k, keys[i], cx, cy, cz);
+    for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
+        const float4 pj = __ldg(P + j);
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float r2 = dist2(dx, dy, dz);
+        if (r2 < k.kh2 && j != i) f(j, pj, dx, dy, dz, r2);
+    });
+}
+
+// Neighbours of i from the list (or by walking the cells when i overflowed it).
+template <bool LIST, class F>
+__device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restrict__ cs,
+                                            const unsigned* __restrict__ keys,
+                                            const NbrList& nl, const float4* __restrict__ P,
+                                            int i, const float4& pi, F&& f) {
+    if (LIST) {
+        const int cnt = __ldg(nl.count + i);
+        if (cnt <= nl.cap) {
+            const int* __restrict__ col = nl.idx + i;
+#pragma unroll 2
+            for (int c = 0; c < cnt; c++) {
+                const int j = __ldg(col + (size_t)c * (size_t)nl.stride);
+                const float4 pj = __ldg(P + j);
+                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                f(j, pj, dx, dy, dz, dist2(dx, dy, dz));
+            }
+            return;
+        }
+    }
+    walk_pairs(k, cs, keys, P, i, pi, f);
+}
+
+// Neighbour-list build: every boundary particle keeps its fluid neighbours (all that pass 1
+// needs), every fluid particle all of them; with walls_all, boundary particles keep all.
+__global__ void __launch_bounds__(NS_THREADS)
+k_nbr_build(KParams k, const float4* __restrict__ P, const unsigned* __restrict__ keys,
+            const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k.n) return;
+    const float4 pi = P[i];
+    const bool keep_all = is_fluid(pi.w) || walls_all;
+    int cnt = 0;
+    int* __restrict__ col = nl.idx + i;
+    walk_pairs(k, cs, keys, P, i, pi, [&](int j, const float4& pj, float, float, float, float) {
+        if (keep_all || is_fluid(pj.w)) {
+            if (cnt < nl.cap) col[(size_t)cnt * (size_t)nl.stride] = j;
+            cnt++;
+        }
+    });
+    nl.count[i] = cnt;
+    raise_flags(err, cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
+}
+
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
 // particles; velocity divergence over fluid neighbours for fluid particles.
-template <bool WRITE_SUMS>
+template <bool WRITE_SUMS, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
 k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, float4* __restrict__ aux, float* __restrict__ rhop_sum,
-        float* __restrict__ w_sum) {
+        const int* __restrict__ cs, NbrList nl, float4* __restrict__ aux,
+        float* __restrict__ rhop_sum, float* __restrict__ w_sum) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const float4* __restrict__ P = in.pos;
@@ -70,30 +146,25 @@ k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     const float4 pi = P[i];
     const float4 vi = V[i];
     const bool fi = is_fluid(pi.w);
-    int cx, cy, cz;
-    cell_of_key(k, keys[i], cx, cy, cz);
     float dofv = 0.f, rs = 0.f, ws = 0.f;
-    for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-        const float4 pj = __ldg(P + j);
-        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 < k.kh2 && j != i && is_fluid(pj.w)) {
-            const float rr = sqrtf(r2);
-            const float q = rr * k.inv_h;
-            const float t = 1.f - 0.5f * q;
-            const float t2 = t * t;
-            if (!fi) {
-                const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
-                const float rhoj = __ldg(&V[j].w);
-                const float pj_ = __ldg(PR + j);
-                rs += (pj_ + rhoj * k.g * dz) * w;
-                ws += w;
-            } else {
-                const float4 vj = __ldg(V + j);
-                const float fr = k.c_fr * t2 * t;
-                const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                dofv -= fr * vdotr * (k.mass / vj.w);
-            }
+    visit_pairs<LIST>(k, cs, keys, nl, P, i, pi,
+                      [&](int j, const float4& pj, float dx, float dy, float dz, float r2) {
+        if (!is_fluid(pj.w)) return;
+        const float rr = sqrtf(r2);
+        const float q = rr * k.inv_h;
+        const float t = 1.f - 0.5f * q;
+        const float t2 = t * t;
+        if (!fi) {
+            const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
+            const float rhoj = __ldg(&V[j].w);
+            const float pj_ = __ldg(PR + j);
+            rs += (pj_ + rhoj * k.g * dz) * w;
+            ws += w;
+        } else {
+            const float4 vj = __ldg(V + j);
+            const float fr = k.c_fr * t2 * t;
+            const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            dofv -= fr * vdotr * (k.mass / vj.w);
         }
     });
     float4 out;
@@ -117,11 +188,11 @@ enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
 // artificial viscosity, gravity); then either the rates are stored (MODE_RATES) or the
 // midpoint predictor / corrector of src/sph/sph_run.cu:425-519 is applied and the updated
 // particle written to `out` with its next cell hash.
-template <int MODE>
+template <int MODE, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
 k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, const float4* __restrict__ aux, float* __restrict__ rho_dt,
-        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
+        const int* __restrict__ cs, NbrList nl, const float4* __restrict__ aux,
+        float* __restrict__ rho_dt, float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
         unsigned* __restrict__ out_hash, unsigned* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
@@ -134,31 +205,24 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     const float rhoi = ai.y, presi = ai.x, dofvi = ai.z;
     float drho = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
     if (fi || (MODE == MODE_RATES && wall_rates)) {
-        int cx, cy, cz;
-        cell_of_key(k, keys[i], cx, cy, cz);
-        for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-            const float4 pj = __ldg(P + j);
-            const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < k.kh2 && j != i) {
-                const float4 vj = __ldg(V + j);
-                const float4 aj = __ldg(aux + j);
-                const float rr = sqrtf(r2);
-                const float q = rr * k.inv_h;
-                const float t = 1.f - 0.5f * q;
-                const float fr = k.c_fr * t * t * t;
-                const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-                const float m_rhoj = k.mass / aj.y;
-                const float inv_r2e = 1.f / (r2 + k.eta2);
-                drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - aj.y) * k.delta_h_cs * r2 * inv_r2e);
-                float S = -(presi + aj.x);
-                if (fi && is_fluid(pj.w))
-                    S += k.damper * (dofvi + aj.z) + k.visc * vdotr * inv_r2e;
-                const float c = fr * S * m_rhoj;
-                ax += c * dx;
-                ay += c * dy;
-                az += c * dz;
-            }
+        visit_pairs<LIST>(k, cs, keys, nl, P, i, pi,
+                          [&](int j, const float4& pj, float dx, float dy, float dz, float r2) {
+            const float4 vj = __ldg(V + j);
+            const float4 aj = __ldg(aux + j);
+            const float rr = sqrtf(r2);
+            const float q = rr * k.inv_h;
+            const float t = 1.f - 0.5f * q;
+            const float fr = k.c_fr * t * t * t;
+            const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            const float m_rhoj = k.mass / aj.y;
+            const float inv_r2e = 1.f / (r2 + k.eta2);
+            drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - aj.y) * k.delta_h_cs * r2 * inv_r2e);
+            float S = -(presi + aj.x);
+            if (fi && is_fluid(pj.w)) S += k.damper * (dofvi + aj.z) + k.visc * vdotr * inv_r2e;
+            const float c = fr * S * m_rhoj;
+            ax += c * dx;
+            ay += c * dy;
+            az += c * dz;
         });
         const float inv_rhoi = 1.f / rhoi;
         ax *= inv_rhoi;
@@ -237,41 +301,79 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
 
 inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
 
+template <bool LIST>
+void pass1_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
+                  const NbrList& nl, float4* aux, float* rhop_sum, float* w_sum, cudaStream_t s) {
+    const int b = blocks_for(k.n, NS_THREADS);
+    if (rhop_sum && w_sum)
+        k_pass1<true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, aux, rhop_sum, w_sum);
+    else
+        k_pass1<false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, aux, nullptr, nullptr);
+}
+
+template <int MODE>
+void pass2_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
+                  const NbrList* nl, const float4* aux, float* rho_dt, float* vel_dt,
+                  int wall_rates, ParticleSet out, unsigned* out_hash, unsigned* err,
+                  cudaStream_t s) {
+    const int b = blocks_for(k.n, NS_THREADS);
+    if (nl)
+        k_pass2<MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, aux, rho_dt, vel_dt,
+                                                      wall_rates, out, out_hash, err);
+    else
+        k_pass2<MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, aux, rho_dt,
+                                                       vel_dt, wall_rates, out, out_hash, err);
+}
+
 }  // namespace
 
-cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* keys,
-                         const int* cs, float4* aux, float* rhop_sum, float* w_sum,
-                         cudaStream_t s) {
+int nbr_capacity_for(const sph_params& p) {
+    // 1.5x the particles of a lattice inside the support sphere, rounded up to 16
+    const double r = (double)p.kh / (double)p.dx;
+    const double lattice = 4.18879020478639 * r * r * r;
+    int cap = (int)(1.5 * lattice) + 16;
+    cap = (cap + 15) & ~15;
+    return cap < 32 ? 32 : cap;
+}
+
+cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* keys,
+                             const int* cs, const NbrList& nl, int walls_all, unsigned* err,
+                             cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    if (rhop_sum && w_sum)
-        k_pass1<true><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in, keys, cs, aux,
-                                                                         rhop_sum, w_sum);
+    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.pos, keys, cs, nl,
+                                                                   walls_all, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* keys,
+                         const int* cs, const NbrList* nl, float4* aux, float* rhop_sum,
+                         float* w_sum, cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    if (nl)
+        pass1_launch<true>(k, in, keys, cs, *nl, aux, rhop_sum, w_sum, s);
     else
-        k_pass1<false><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in, keys, cs, aux,
-                                                                          nullptr, nullptr);
+        pass1_launch<false>(k, in, keys, cs, NbrList{}, aux, rhop_sum, w_sum, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in, const unsigned* keys,
-                               const int* cs, const float4* aux, float* rho_dt, float* vel_dt,
-                               int wall_rates, cudaStream_t s) {
+                               const int* cs, const NbrList* nl, const float4* aux,
+                               float* rho_dt, float* vel_dt, int wall_rates, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_pass2<MODE_RATES><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
-        k, in, keys, cs, aux, rho_dt, vel_dt, wall_rates, ParticleSet{}, nullptr, nullptr);
+    pass2_launch<MODE_RATES>(k, in, keys, cs, nl, aux, rho_dt, vel_dt, wall_rates, ParticleSet{},
+                             nullptr, nullptr, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
-                              const unsigned* keys, const int* cs, const float4* aux,
-                              ParticleSet out, unsigned* out_hash, unsigned* err,
-                              cudaStream_t s) {
+                              const unsigned* keys, const int* cs, const NbrList* nl,
+                              const float4* aux, ParticleSet out, unsigned* out_hash,
+                              unsigned* err, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (half == HALF_PREDICT)
-        k_pass2<MODE_PRED><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
-            k, in, keys, cs, aux, nullptr, nullptr, 0, out, out_hash, err);
+        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, aux, nullptr, nullptr, 0, out, out_hash, err, s);
     else
-        k_pass2<MODE_CORR><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(
-            k, in, keys, cs, aux, nullptr, nullptr, 0, out, out_hash, err);
+        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, aux, nullptr, nullptr, 0, out, out_hash, err, s);
     return cudaGetLastError();
 }
 

@@ -43,23 +43,38 @@ struct ParticleSet {
 
 enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 
-// Neighbour passes (equation/ns.cu).
+// Per-half-step neighbour list: idx[c * stride + i] is the c-th neighbour of slot i (walk
+// order), count[i] how many; count[i] > cap means the list overflowed for i and the passes
+// walk the cells for it instead.
+struct NbrList {
+    int* idx = nullptr;
+    int* count = nullptr;
+    int cap = 0;
+    int stride = 0;  // >= n (the context capacity)
+};
+int nbr_capacity_for(const sph_params& p);
+
+// Neighbour passes (equation/ns.cu).  nl == NULL walks the cells in every pass.
+//  build : fills nl for the sorted set (walls keep only fluid neighbours unless walls_all).
 //  pass 1: aux[i] = (p, rho, dofv, 0) — boundary particles get the extrapolated p and rho,
 //          fluid particles their own p, rho and the velocity divergence.  rhop_sum / w_sum are
 //          written when non-NULL.
 //  pass 2: either rates only (rho_dt, AoS vel_dt) or rates + the predictor/corrector update
 //          written into `out` (slot-aligned with `in`) with the next cell hash.
+cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
+                             const int* cell_start, const NbrList& nl, int walls_all,
+                             unsigned* err, cudaStream_t s);
 cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
-                         const int* cell_start, float4* aux, float* rhop_sum, float* w_sum,
-                         cudaStream_t s);
+                         const int* cell_start, const NbrList* nl, float4* aux, float* rhop_sum,
+                         float* w_sum, cudaStream_t s);
 cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
                                const unsigned* sorted_keys, const int* cell_start,
-                               const float4* aux, float* rho_dt, float* vel_dt, int wall_rates,
-                               cudaStream_t s);
+                               const NbrList* nl, const float4* aux, float* rho_dt,
+                               float* vel_dt, int wall_rates, cudaStream_t s);
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
                               const unsigned* sorted_keys, const int* cell_start,
-                              const float4* aux, ParticleSet out, unsigned* out_hash,
-                              unsigned* err, cudaStream_t s);
+                              const NbrList* nl, const float4* aux, ParticleSet out,
+                              unsigned* out_hash, unsigned* err, cudaStream_t s);
 
 // Resident-state glue (lib/mesh.cu).
 cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
@@ -80,7 +95,7 @@ cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float
                                 float* s_rho, float* s_p, float* dofv, cudaStream_t s);
 
 // Per-phase device timing of sph_step (SPH_OPT_PROFILE).
-enum Phase { PH_SORT = 0, PH_GATHER, PH_PASS1, PH_PASS2, PH_COUNT };
+enum Phase { PH_SORT = 0, PH_GATHER, PH_NBR, PH_PASS1, PH_PASS2, PH_COUNT };
 
 }  // namespace sph
 
@@ -105,18 +120,20 @@ struct sph_ctx {
     size_t sort_scratch_bytes = 0;
     unsigned* err = nullptr;         // device error word
 
-    // drop-in sph_ns buffers are the y set plus these
-    float* tmp_rho_dt = nullptr;
+    // neighbour list of the current half step
+    sph::NbrList nl;
 
     // graph replay of one full step
     int opt_use_graph = 1;
     int opt_wall_rates = 0;
     int opt_profile = 0;
+    int opt_nbr_list = 1;
+    int opt_nbr_cap = 0;  // 0: nbr_capacity_for(P)
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;
-    // profiling events / accumulated milliseconds per phase
-    cudaEvent_t ev[2 * sph::PH_COUNT * 2] = {};
+    // profiling events (PH_COUNT + 1 per half step) / accumulated milliseconds per phase
+    cudaEvent_t ev[2 * (sph::PH_COUNT + 1)] = {};
     double phase_ms[sph::PH_COUNT] = {};
     long long phase_launches[sph::PH_COUNT] = {};
 };

@@ -58,6 +58,8 @@ void release(sph_ctx* c) {
     free_set(c->y);
     cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm); cudaFree(c->aux);
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
+    cudaFree(c->nl.idx); cudaFree(c->nl.count);
+    c->nl = NbrList{};
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -96,34 +98,63 @@ bool params_ok(const sph_params* p) {
            p->num_cells < (1 << 30);
 }
 
-// One half step (see the file comment).  `ev` (may be NULL) receives 5 timestamps.
+constexpr int EV_PER_HALF = PH_COUNT + 1;
+
+// The neighbour list to use this half step, or NULL to walk the cells in every pass.
+const NbrList* list_for(sph_ctx* c) { return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr; }
+
+// One half step (see the file comment).  `ev` (may be NULL) receives PH_COUNT + 1 timestamps.
 cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev) {
     const KParams k = make_kparams(c->P, c->n);
     const int bits = key_bits_for(c->P.num_cells);
+    const NbrList* nl = list_for(c);
     cudaError_t e;
-    if (ev) cudaEventRecord(ev[0], s);
+    if (ev) cudaEventRecord(ev[PH_SORT], s);
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
                          c->sort_scratch_bytes, c->err, s);
     if (e != cudaSuccess) return e;
-    if (ev) cudaEventRecord(ev[1], s);
+    if (ev) cudaEventRecord(ev[PH_GATHER], s);
     if ((e = launch_gather(k, c->perm, c->x, c->y, half == HALF_CORRECT, s)) != cudaSuccess) return e;
     if ((e = build_cell_starts(c->keys_sorted, c->n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
         return e;
-    if (ev) cudaEventRecord(ev[2], s);
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, c->aux, nullptr, nullptr, s)) !=
-        cudaSuccess)
+    if (ev) cudaEventRecord(ev[PH_NBR], s);
+    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s)) !=
+                  cudaSuccess)
         return e;
-    if (ev) cudaEventRecord(ev[3], s);
-    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, c->aux, c->x, c->hash_x,
-                          c->err, s);
-    if (ev) cudaEventRecord(ev[4], s);
+    if (ev) cudaEventRecord(ev[PH_PASS1], s);
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, nullptr, nullptr,
+                          s)) != cudaSuccess)
+        return e;
+    if (ev) cudaEventRecord(ev[PH_PASS2], s);
+    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->aux, c->x,
+                          c->hash_x, c->err, s);
+    if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
 }
 
 cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
     cudaError_t e = half_step(c, HALF_PREDICT, s, ev);
     if (e != cudaSuccess) return e;
-    return half_step(c, HALF_CORRECT, s, ev ? ev + 5 : nullptr);
+    return half_step(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr);
+}
+
+cudaError_t alloc_list(sph_ctx* c) {
+    const int cap = c->opt_nbr_cap > 0 ? c->opt_nbr_cap : nbr_capacity_for(c->P);
+    if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
+    cudaFree(c->nl.idx);
+    cudaFree(c->nl.count);
+    c->nl = NbrList{};
+    cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * (size_t)(c->capacity > 0 ? c->capacity : 1));
+    if (e == cudaSuccess) e = dalloc(&c->nl.count, c->capacity);
+    if (e != cudaSuccess) {
+        cudaFree(c->nl.idx);
+        cudaFree(c->nl.count);
+        c->nl = NbrList{};
+        return e;
+    }
+    c->nl.cap = cap;
+    c->nl.stride = c->capacity;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -151,6 +182,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sort_scratch, c->sort_scratch_bytes);
     if (e == cudaSuccess) e = dalloc(&c->err, 1);
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = alloc_list(c);
     for (auto& ev : c->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
     if (e != cudaSuccess) {
@@ -185,6 +217,11 @@ extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     }
     c->P = *p;
     drop_graph(c);
+    // and the neighbour list, when the support radius holds more lattice neighbours
+    if (alloc_list(c) != cudaSuccess) {
+        cudaGetLastError();
+        return SPH_ERR_NOMEM;
+    }
     return SPH_OK;
 }
 
@@ -200,6 +237,16 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
         case SPH_OPT_USE_GRAPH: c->opt_use_graph = value != 0; drop_graph(c); return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_PROFILE: c->opt_profile = value != 0; return SPH_OK;
+        case SPH_OPT_NEIGHBOR_LIST: c->opt_nbr_list = value != 0; drop_graph(c); return SPH_OK;
+        case SPH_OPT_NEIGHBOR_CAP:
+            if (value < 0) return SPH_ERR_ARG;
+            c->opt_nbr_cap = value;
+            drop_graph(c);
+            if (alloc_list(c) != cudaSuccess) {
+                cudaGetLastError();
+                return SPH_ERR_NOMEM;
+            }
+            return SPH_OK;
         default: return SPH_ERR_ARG;
     }
 }
@@ -278,11 +325,13 @@ extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
         for (int i = 0; i < nsteps; i++) {
             cudaError_t e = full_step(c, s, c->ev);
             if (e != cudaSuccess) return SPH_ERR_CUDA;
-            if (cudaEventSynchronize(c->ev[9]) != cudaSuccess) return SPH_ERR_CUDA;
+            if (cudaEventSynchronize(c->ev[2 * EV_PER_HALF - 1]) != cudaSuccess) return SPH_ERR_CUDA;
             for (int h = 0; h < 2; h++)
                 for (int ph = 0; ph < PH_COUNT; ph++) {
+                    if (ph == PH_NBR && !list_for(c)) continue;
                     float ms = 0.f;
-                    cudaEventElapsedTime(&ms, c->ev[5 * h + ph], c->ev[5 * h + ph + 1]);
+                    cudaEventElapsedTime(&ms, c->ev[EV_PER_HALF * h + ph],
+                                         c->ev[EV_PER_HALF * h + ph + 1]);
                     c->phase_ms[ph] += ms;
                     c->phase_launches[ph] += 1;
                 }
@@ -396,11 +445,15 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
         return SPH_ERR_CUDA;
     if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, c->aux, rhop_sum, w_sum, s)) !=
-        cudaSuccess)
+    const NbrList* nl = list_for(c);
+    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl,
+                                    c->opt_wall_rates, c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, c->aux, rho_dt, vel_dt,
-                                c->opt_wall_rates, s)) != cudaSuccess)
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, rhop_sum, w_sum,
+                          s)) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, rho_dt,
+                                vel_dt, c->opt_wall_rates, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     if ((e = launch_ns_writeback(k, s_type, c->aux, s_rho, s_p, dofv, s)) != cudaSuccess)
         return SPH_ERR_CUDA;

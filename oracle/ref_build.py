@@ -26,6 +26,22 @@ FATBIN = os.path.join(OUT, "ref_src.fatbin")
 HARNESS = os.path.join(OUT, "libref_harness.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
+# The reference's six code trees: the baseline and its five optimisation snapshots.  Flags
+# follow each tree's CMakeLists.txt (v0-v4 cap registers at 64; v3 and v4 use std::vector
+# without including it; v4 adds lib/mem.cu).
+VERSIONS = {
+    "src": ("src", []),
+    "v0": ("opt_src_v0", ["-maxrregcount", "64"]),
+    "v1": ("opt_src_v1", ["-maxrregcount", "64"]),
+    "v2": ("opt_src_v2", ["-maxrregcount", "64"]),
+    "v3": ("opt_src_v3", ["-maxrregcount", "64"]),
+    "v4": ("opt_src_v4", ["-maxrregcount", "64"]),
+}
+
+
+def fatbin_path(version: str) -> str:
+    return FATBIN if version == "src" else os.path.join(OUT, f"ref_{version}.fatbin")
+
 
 def nvcc() -> str:
     for c in ("/usr/local/cuda/bin/nvcc", shutil.which("nvcc") or ""):
@@ -38,24 +54,32 @@ def reference_present() -> bool:
     return os.path.isdir(os.path.join(REFERENCE, "src", "equation"))
 
 
-def build_fatbin(force: bool = False) -> str | None:
+def build_fatbin(force: bool = False, version: str = "src") -> str | None:
+    out = fatbin_path(version)
     if not reference_present():
-        return FATBIN if os.path.exists(FATBIN) else None
-    if os.path.exists(FATBIN) and not force:
-        return FATBIN
+        return out if os.path.exists(out) else None
+    if os.path.exists(out) and not force:
+        return out
+    tree, flags = VERSIONS[version]
     os.makedirs(OUT, exist_ok=True)
-    unity = os.path.join(OUT, "unity_src.cu")
+    src = os.path.join(REFERENCE, tree)
+    unity = os.path.join(OUT, f"unity_{version}.cu")
     with open(unity, "w") as f:
         f.write('#define main reference_main\n#include "lib/mesh.cu"\n'
                 '#include "equation/ns.cu"\n#include "sph/sph_run.cu"\n')
-    src = os.path.join(REFERENCE, "src")
-    cmd = [nvcc(), "-fatbin", *ARCH, "-O3", "-w", "-I" + src, "-I" + os.path.join(src, "header"),
-           unity, "-o", FATBIN + ".tmp"]
+        if os.path.exists(os.path.join(src, "lib", "mem.cu")):
+            f.write('#include "lib/mem.cu"\n')
+    cmd = [nvcc(), "-fatbin", *ARCH, "-O3", "-w", "-include", "vector", *flags, "-I" + src,
+           "-I" + os.path.join(src, "header"), unity, "-o", out + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"reference fatbin build failed:\n{r.stderr[-3000:]}")
-    os.replace(FATBIN + ".tmp", FATBIN)
-    return FATBIN
+        raise RuntimeError(f"reference fatbin build failed ({version}):\n{r.stderr[-3000:]}")
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_all_fatbins(force: bool = False) -> dict:
+    return {v: build_fatbin(force, v) for v in VERSIONS}
 
 
 def build_harness(force: bool = False) -> str:
@@ -82,7 +106,7 @@ def _machine_stamp_ok() -> bool:
 
 
 def build(force: bool = False) -> dict:
-    return {"fatbin": build_fatbin(force), "harness": build_harness(force)}
+    return {"fatbins": build_all_fatbins(force), "harness": build_harness(force)}
 
 
 if __name__ == "__main__":

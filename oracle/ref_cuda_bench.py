@@ -1,13 +1,13 @@
-"""Time the reference solver's own CUDA step loop on this GPU.  TEST INFRASTRUCTURE.
+"""Time the reference solver's own CUDA step loops on this GPU.  TEST INFRASTRUCTURE.
 
-Runs the reference's src/ kernels (oracle/_ref/ref_src.fatbin through oracle/ref_harness.cu:
-calcHash, thrust::sort_by_key, reorder, both neighbour kernels, PC_prediction, recover, then
-the same for PC_correction — src/sph/sph_run.cu:285-336) on the same seeded workload as
-bench.py, with the reference's own constants (h = 1.5 dx, linear EOS, cs 25) or the
-benchmark's (h = 1.3 dx; only the neighbour count differs for the timing), and prints one
-JSON line with particle-steps/s measured by CUDA events on the default stream.
+Runs each of the reference's code trees — the baseline src/ and the optimisation snapshots
+opt_src_v0..v4 — from its fatbin (oracle/_ref, launched by oracle/ref_harness.cu with the
+reference's own launch shapes and thrust::sort_by_key) on the same seeded workload as bench.py
+and prints one JSON line per version: particle-steps/s by CUDA events on the default stream,
+plus the relative L2 of its fluid velocity and density perturbation after the timed steps
+against the baseline src/ run (v4's half-precision distance test is inexact at these spacings).
 
-    python -m oracle.ref_cuda_bench [--case large] [--steps 10] [--warmup 2] [--physics config]
+    python -m oracle.ref_cuda_bench [--case large] [--steps 10] [--warmup 2] [--versions src,v0,...]
 """
 from __future__ import annotations
 
@@ -16,8 +16,16 @@ import json
 import os
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
 def main():
@@ -26,6 +34,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--physics", default="config")
+    ap.add_argument("--versions", default="src,v0,v1,v2,v3,v4")
     args = ap.parse_args()
     import torch
     from tmp_sph_gb300 import cases
@@ -36,22 +45,35 @@ def main():
     P = O.params_like(p)
     P.eos = 0  # the reference kernels implement only the linear EOS
     n = len(st["rho"])
-    H = RefHarness()
-    H.set_params(P, n)
-    d, s, w, tmp = H.alloc(st, cuda)
-    H.step(d, s, w, tmp, args.warmup)
-    H.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(torch.cuda.default_stream())
-    H.step(d, s, w, tmp, args.steps)
-    e1.record(torch.cuda.default_stream())
-    H.sync()
-    ms = e0.elapsed_time(e1)
-    out = {"impl": "reference_cuda_src", "case": args.case, "physics": args.physics,
-           "particles": n, "steps": args.steps, "ms_per_step": ms / args.steps,
-           "particle_steps_per_s": n * args.steps / (ms / 1e3),
-           "finite": bool(torch.isfinite(d["vel"]).all().item())}
-    print(json.dumps(out), flush=True)
+    fl = st["type"] == 1
+    base = None
+    for v in args.versions.split(","):
+        H = RefHarness(v)
+        H.set_params(P, n)
+        d, s, w, tmp = H.alloc(st, cuda)
+        H.init_ids(d)
+        H.step(d, s, w, tmp, args.warmup)
+        H.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.default_stream())
+        H.step(d, s, w, tmp, args.steps)
+        e1.record(torch.cuda.default_stream())
+        H.sync()
+        ms = e0.elapsed_time(e1)
+        out = H.state(d, s)
+        res = {"impl": f"reference_cuda_{v}", "case": args.case, "physics": args.physics,
+               "particles": n, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": ms / args.steps,
+               "particle_steps_per_s": n * args.steps / (ms / 1e3),
+               "finite": bool(np.isfinite(out["vel"]).all())}
+        if base is None:
+            base = out
+        else:
+            res["vel_rel_l2_vs_src"] = rel(out["vel"][fl], base["vel"][fl])
+            res["drho_rel_l2_vs_src"] = rel(out["rho"][fl] - 1000.0, base["rho"][fl] - 1000.0)
+        print(json.dumps(res), flush=True)
+        del d, s, w, tmp
+        torch.cuda.empty_cache()
 
 
 if __name__ == "__main__":

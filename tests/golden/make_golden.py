@@ -85,7 +85,7 @@ def main(outdir=HERE):
             os.path.join(outdir, f"ref_cells_{name}.npz"), **common,
             in_pos=pst["pos"], in_vel=pst["vel"], in_rho=pst["rho"], in_p=pst["p"], in_type=pst["type"],
             hash_unsorted=hash_unsorted, hash=host(w["hash"]), index=host(w["index"]),
-            cell_start=host(w["cs"]), cell_end=host(w["ce"]),
+            cell_start=host(w["cs"])[:P.num_cells], cell_end=host(w["ce"])[:P.num_cells],
             s_pos=host(s["pos"]), s_vel=host(s["vel"]), s_rho=host(s["rho"]), s_p=host(s["p"]),
             s_type=host(s["type"]))
         # ---- neighbour passes on the sorted, perturbed state

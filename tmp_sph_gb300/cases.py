@@ -116,9 +116,8 @@ def build(name: str, physics: str = "config", **kw) -> tuple[dict, api.SphParams
     d = geometry(name, physics=physics, **kw)
     st = api.dam_break_generate(d)
     n = st["n_fluid"] + st["n_boundary"]
-    if physics == "reference" and name == "refcase":
-        p = api.params_reference(d.dx, d.tank[0], d.tank[1], d.tank[2], n, st["n_boundary"])
-    else:
-        p = api.params_derive(config(d, physics, n, st["n_boundary"]))
+    # config() keeps the reference's 0.1 m pad unless the wall layers are thicker than that
+    # (coarse test spacings), so every particle hashes into the grid
+    p = api.params_derive(config(d, physics, n, st["n_boundary"]))
     st["geometry"] = d
     return st, p

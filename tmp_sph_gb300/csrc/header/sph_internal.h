@@ -43,14 +43,13 @@ struct ParticleSet {
 
 enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 
-// Per-half-step neighbour list: idx[c * stride + i] is the c-th neighbour of slot i (walk
+// Per-half-step neighbour list: idx[i * cap + c] is the c-th neighbour of slot i (walk
 // order), count[i] how many; count[i] > cap means the list overflowed for i and the passes
-// walk the cells for it instead.
+// walk the cells for it instead.  cap is a multiple of 16 (rows are 16-byte aligned).
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
     int cap = 0;
-    int stride = 0;  // >= n (the context capacity)
 };
 int nbr_capacity_for(const sph_params& p);
 

@@ -139,7 +139,8 @@ cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
 }
 
 cudaError_t alloc_list(sph_ctx* c) {
-    const int cap = c->opt_nbr_cap > 0 ? c->opt_nbr_cap : nbr_capacity_for(c->P);
+    // the option is rounded up to a multiple of 16 so rows stay 16-byte aligned
+    const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15 : nbr_capacity_for(c->P);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
     cudaFree(c->nl.idx);
     cudaFree(c->nl.count);
@@ -153,7 +154,6 @@ cudaError_t alloc_list(sph_ctx* c) {
         return e;
     }
     c->nl.cap = cap;
-    c->nl.stride = c->capacity;
     return cudaSuccess;
 }
 

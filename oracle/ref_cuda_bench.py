@@ -67,10 +67,11 @@ def main():
                "particle_steps_per_s": n * args.steps / (ms / 1e3),
                "finite": bool(np.isfinite(out["vel"]).all())}
         if base is None:
-            base = out
+            base, base_name = out, v
         else:
-            res["vel_rel_l2_vs_src"] = rel(out["vel"][fl], base["vel"][fl])
-            res["drho_rel_l2_vs_src"] = rel(out["rho"][fl] - 1000.0, base["rho"][fl] - 1000.0)
+            res[f"vel_rel_l2_vs_{base_name}"] = rel(out["vel"][fl], base["vel"][fl])
+            res[f"drho_rel_l2_vs_{base_name}"] = rel(out["rho"][fl] - 1000.0,
+                                                     base["rho"][fl] - 1000.0)
         print(json.dumps(res), flush=True)
         del d, s, w, tmp
         torch.cuda.empty_cache()

@@ -4,11 +4,19 @@
 // computeBoundary_Delta_acoustic_D (pass 1, src/equation/ns.cu:30-131) and
 // computeGovering_equationD (pass 2, src/equation/ns.cu:134-249).
 //
-// Layout: particles in cell-sorted order, SoA float4 (x, y, z, kind) / (vx, vy, vz, rho),
-// pass-1 output (p, rho, dofv, 0).  Cells are walked as nine x-strips: the three cells
-// (x-1 .. x+1) of one (y, z) row are consecutive in the sorted order, so each strip is one
-// contiguous slot range [cell_start[row + x-1], cell_start[row + x+2]) — the dense
-// cell_start array gives empty cells the start of the next non-empty one.
+// Layout.  Particles are in cell-sorted order; each is one 32-byte record of two float4,
+// rec[2i] = (x, y, z, p) and rec[2i+1] = (vx, vy, vz, ±rho) with the sign of rho marking a
+// fluid (+) or boundary (-) particle, so everything a neighbour contributes to pass 1 is one
+// aligned 32-byte sector.  Pass 1 writes the record pass 2 gathers, nrec[2i] = (x, y, z, q),
+// nrec[2i+1] = (vx, vy, vz, ±rho'), where q = p' - rho0 cs h dofv: the acoustic-damper term of a
+// fluid-fluid pair, rho0 cs h (dofv_i + dofv_j), splits into an i part and a j part, and the j
+// part is folded into the neighbour's pressure (boundary particles have dofv = 0, so q = p').
+// It also writes self[i] = (p', rho', dofv, 0) for the particle's own side.
+//
+// Cells are walked as nine x-strips: the three cells (x-1 .. x+1) of one (y, z) row are
+// consecutive in the sorted order, so each strip is one contiguous slot range
+// [cell_start[row + x-1], cell_start[row + x+2]) — the dense cell_start array gives empty cells
+// the start of the next non-empty one.
 //
 // Neighbour list.  About 15% of the ~475 candidates of a 27-cell walk lie inside the
 // support radius, and the lanes of a warp (particles of two or three adjacent cells) almost
@@ -70,29 +78,29 @@ __device__ __forceinline__ void for_each_candidate(const KParams& k, const int* 
     }
 }
 
-// Walk the cells of particle i and call f(j, pj, dx, dy, dz, r2) for every j != i within the
-// support radius.
+// Walk the cells of particle i and call f(j, dx, dy, dz, r2) for every j != i within the
+// support radius; R holds the particles' records (position in R[2j].xyz).
 template <class F>
 __device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restrict__ cs,
                                            const unsigned* __restrict__ keys,
-                                           const float4* __restrict__ P, int i, const float4& pi,
+                                           const float4* __restrict__ R, int i, const float4& pi,
                                            F&& f) {
     int cx, cy, cz;
     cell_of_key(k, keys[i], cx, cy, cz);
     for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-        const float4 pj = __ldg(P + j);
+        const float4 pj = __ldg(R + 2 * (size_t)j);
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dist2(dx, dy, dz);
-        if (r2 < k.kh2 && j != i) f(j, pj, dx, dy, dz, r2);
+        if (r2 < k.kh2 && j != i) f(j, dx, dy, dz, r2);
     });
 }
 
 // Neighbours of i from the list (or by walking the cells when i overflowed it).  The list row
-// of i is read as 16-byte vectors of four neighbour slots.
+// of i is read as 16-byte vectors of four neighbour slots; R supplies the positions.
 template <bool LIST, class F>
 __device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restrict__ cs,
                                             const unsigned* __restrict__ keys,
-                                            const NbrList& nl, const float4* __restrict__ P,
+                                            const NbrList& nl, const float4* __restrict__ R,
                                             int i, const float4& pi, F&& f) {
     if (LIST) {
         const int cnt = __ldg(nl.count + i);
@@ -100,9 +108,9 @@ __device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restr
             const int4* __restrict__ row =
                 reinterpret_cast<const int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
             auto one = [&](int j) {
-                const float4 pj = __ldg(P + j);
+                const float4 pj = __ldg(R + 2 * (size_t)j);
                 const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                f(j, pj, dx, dy, dz, dist2(dx, dy, dz));
+                f(j, dx, dy, dz, dist2(dx, dy, dz));
             };
 #pragma unroll 1
             for (int c = 0; c < cnt; c += 4) {
@@ -115,26 +123,28 @@ __device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restr
             return;
         }
     }
-    walk_pairs(k, cs, keys, P, i, pi, f);
+    walk_pairs(k, cs, keys, R, i, pi, f);
 }
+
+__device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho > 0.f; }
 
 // Neighbour-list build: every boundary particle keeps its fluid neighbours (all that pass 1
 // needs), every fluid particle all of them; with walls_all, boundary particles keep all.
 // Rows are particle-major (row i = idx + i * cap) and written as 16-byte vectors of four
 // slots, buffered in registers, so a warp store moves 512 B instead of 128 B.
 __global__ void __launch_bounds__(NS_THREADS)
-k_nbr_build(KParams k, const float4* __restrict__ P, const unsigned* __restrict__ keys,
+k_nbr_build(KParams k, const float4* __restrict__ R, const unsigned* __restrict__ keys,
             const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4 pi = P[i];
-    const bool keep_all = is_fluid(pi.w) || walls_all;
+    const float4 pi = R[2 * (size_t)i];
+    const bool keep_all = fluid_rec(R[2 * (size_t)i + 1].w) || walls_all;
     int cnt = 0;
     int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     int4* __restrict__ row = reinterpret_cast<int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
     const int cap = nl.cap;
-    walk_pairs(k, cs, keys, P, i, pi, [&](int j, const float4& pj, float, float, float, float) {
-        if (keep_all || is_fluid(pj.w)) {
+    walk_pairs(k, cs, keys, R, i, pi, [&](int j, float, float, float, float) {
+        if (keep_all || fluid_rec(__ldg(&R[2 * (size_t)j + 1].w))) {
             const int slot = cnt & 3;
             b0 = slot == 0 ? j : b0;
             b1 = slot == 1 ? j : b1;
@@ -150,50 +160,51 @@ k_nbr_build(KParams k, const float4* __restrict__ P, const unsigned* __restrict_
 }
 
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
-// particles; velocity divergence over fluid neighbours for fluid particles.
+// particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
+// neighbour record and the particle's own (p', rho', dofv).
 template <bool WRITE_SUMS, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
 k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, NbrList nl, float4* __restrict__ aux,
-        float* __restrict__ rhop_sum, float* __restrict__ w_sum) {
+        const int* __restrict__ cs, NbrList nl, Pass1Out out, float* __restrict__ rhop_sum,
+        float* __restrict__ w_sum) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4* __restrict__ P = in.pos;
-    const float4* __restrict__ V = in.vel;
-    const float* __restrict__ PR = in.pres;
-    const float4 pi = P[i];
-    const float4 vi = V[i];
-    const bool fi = is_fluid(pi.w);
+    const float4* __restrict__ R = in.rec;
+    const float4 pi = R[2 * (size_t)i];      // x, y, z, p
+    const float4 vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
+    const bool fi = fluid_rec(vi.w);
     float dofv = 0.f, rs = 0.f, ws = 0.f;
-    visit_pairs<LIST>(k, cs, keys, nl, P, i, pi,
-                      [&](int j, const float4& pj, float dx, float dy, float dz, float r2) {
-        if (!is_fluid(pj.w)) return;
+    visit_pairs<LIST>(k, cs, keys, nl, R, i, pi, [&](int j, float dx, float dy, float dz, float r2) {
+        const float4 vj = __ldg(R + 2 * (size_t)j + 1);
+        if (!fluid_rec(vj.w)) return;
         const float rr = sqrtf(r2);
         const float q = rr * k.inv_h;
         const float t = 1.f - 0.5f * q;
         const float t2 = t * t;
         if (!fi) {
             const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
-            const float rhoj = __ldg(&V[j].w);
-            const float pj_ = __ldg(PR + j);
-            rs += (pj_ + rhoj * k.g * dz) * w;
+            const float pj_ = __ldg(&R[2 * (size_t)j].w);
+            rs += (pj_ + vj.w * k.g * dz) * w;
             ws += w;
         } else {
-            const float4 vj = __ldg(V + j);
             const float fr = k.c_fr * t2 * t;
             const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
             dofv -= fr * vdotr * (k.mass / vj.w);
         }
     });
-    float4 out;
+    float p, rho;
     if (fi) {
-        out = make_float4(PR[i], vi.w, dofv, 0.f);
+        p = pi.w;
+        rho = vi.w;
     } else {
-        float p = fabsf(ws) > 1.0e-8f ? rs / ws : 0.f;
+        p = fabsf(ws) > 1.0e-8f ? rs / ws : 0.f;
         if (p < 0.f) p = 0.f;
-        out = make_float4(p, eos_density(k, p), 0.f, 0.f);
+        rho = eos_density(k, p);
     }
-    aux[i] = out;
+    const float qv = fi ? p - k.damper * dofv : p;
+    out.nrec[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, qv);
+    out.nrec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, fi ? rho : -rho);
+    out.self[i] = make_float4(p, rho, dofv, 0.f);
     if (WRITE_SUMS) {
         rhop_sum[i] = rs;
         w_sum[i] = ws;
@@ -209,34 +220,40 @@ enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
 template <int MODE, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
 k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, NbrList nl, const float4* __restrict__ aux,
-        float* __restrict__ rho_dt, float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
+        const int* __restrict__ cs, NbrList nl, Pass1Out p1, float* __restrict__ rho_dt,
+        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
         unsigned* __restrict__ out_hash, unsigned* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4* __restrict__ P = in.pos;
-    const float4* __restrict__ V = in.vel;
-    const float4 pi = P[i];
-    const float4 vi = V[i];
-    const float4 ai = aux[i];  // p_i, rho_i, dofv_i
-    const bool fi = is_fluid(pi.w);
-    const float rhoi = ai.y, presi = ai.x, dofvi = ai.z;
+    const float4* __restrict__ NR = p1.nrec;
+    const float4 pi = NR[2 * (size_t)i];
+    const float4 vi = NR[2 * (size_t)i + 1];
+    const float4 si = p1.self[i];  // p_i, rho_i, dofv_i
+    const bool fi = fluid_rec(vi.w);
+    const float rhoi = si.y, presi = si.x, dofvi = si.z;
     float drho = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
     if (fi || (MODE == MODE_RATES && wall_rates)) {
-        visit_pairs<LIST>(k, cs, keys, nl, P, i, pi,
-                          [&](int j, const float4& pj, float dx, float dy, float dz, float r2) {
-            const float4 vj = __ldg(V + j);
-            const float4 aj = __ldg(aux + j);
+        const float damp_i = k.damper * dofvi;
+        visit_pairs<LIST>(k, cs, keys, nl, NR, i, pi, [&](int j, float dx, float dy, float dz, float r2) {
+            const float4 aj = __ldg(NR + 2 * (size_t)j);      // x, y, z, q
+            const float4 vj = __ldg(NR + 2 * (size_t)j + 1);  // vx, vy, vz, ±rho
+            const bool fj = fluid_rec(vj.w);
+            const float rhoj = fabsf(vj.w);
             const float rr = sqrtf(r2);
             const float q = rr * k.inv_h;
             const float t = 1.f - 0.5f * q;
             const float fr = k.c_fr * t * t * t;
             const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            const float m_rhoj = k.mass / aj.y;
+            const float m_rhoj = k.mass / rhoj;
             const float inv_r2e = 1.f / (r2 + k.eta2);
-            drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - aj.y) * k.delta_h_cs * r2 * inv_r2e);
-            float S = -(presi + aj.x);
-            if (fi && is_fluid(pj.w)) S += k.damper * (dofvi + aj.z) + k.visc * vdotr * inv_r2e;
+            drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e);
+            float S;
+            if (fi) {
+                S = -presi - aj.w;
+                if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
+            } else {
+                S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
+            }
             const float c = fr * S * m_rhoj;
             ax += c * dx;
             ay += c * dy;
@@ -259,13 +276,14 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     }
 
     float4 np = pi, nv;
-    float npres;
+    float npres, nrho;
     float4 tp, tv;
     if (fi) {
         if (escaped(k, pi.x, pi.y, pi.z)) {
-            np = make_float4(k.park_x, k.park_y, k.park_z, pi.w);
-            nv = make_float4(0.f, 0.f, 0.f, k.rho0);
+            np = make_float4(k.park_x, k.park_y, k.park_z, 0.f);
+            nv = make_float4(0.f, 0.f, 0.f, 0.f);
             npres = 0.f;
+            nrho = k.rho0;
             tp = make_float4(np.x, np.y, np.z, k.rho0);
             tv = make_float4(0.f, 0.f, 0.f, 0.f);
         } else if (MODE == MODE_PRED) {
@@ -276,7 +294,8 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
             np.x = pi.x + vi.x * k.half_dt;
             np.y = pi.y + vi.y * k.half_dt;
             np.z = pi.z + vi.z * k.half_dt;
-            nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt, rho);
+            nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt, 0.f);
+            nrho = rho;
             npres = eos_pressure(k, rho);
         } else {
             tp = in.tpos[i];
@@ -294,19 +313,21 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
             np.x = 2.f * xs - tp.x;
             np.y = 2.f * ys - tp.y;
             np.z = 2.f * zs - tp.z;
-            nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, rho);
+            nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, 0.f);
+            nrho = rho;
             npres = eos_pressure(k, rho);
         }
     } else {
         // boundary particles do not move; they keep the extrapolated pressure and density
-        nv = make_float4(vi.x, vi.y, vi.z, rhoi);
+        nv = make_float4(vi.x, vi.y, vi.z, 0.f);
         npres = presi;
+        nrho = rhoi;
         tp = make_float4(pi.x, pi.y, pi.z, rhoi);
         tv = make_float4(vi.x, vi.y, vi.z, 0.f);
     }
-    out.pos[i] = np;
-    out.vel[i] = nv;
-    out.pres[i] = npres;
+    out.rec[2 * (size_t)i] = make_float4(np.x, np.y, np.z, npres);
+    out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+    out.type[i] = in.type[i];
     out.id[i] = in.id[i];
     if (MODE == MODE_PRED) {
         out.tpos[i] = tp;
@@ -321,25 +342,26 @@ inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
 
 template <bool LIST>
 void pass1_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
-                  const NbrList& nl, float4* aux, float* rhop_sum, float* w_sum, cudaStream_t s) {
+                  const NbrList& nl, const Pass1Out& o, float* rhop_sum, float* w_sum,
+                  cudaStream_t s) {
     const int b = blocks_for(k.n, NS_THREADS);
     if (rhop_sum && w_sum)
-        k_pass1<true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, aux, rhop_sum, w_sum);
+        k_pass1<true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, rhop_sum, w_sum);
     else
-        k_pass1<false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, aux, nullptr, nullptr);
+        k_pass1<false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, nullptr, nullptr);
 }
 
 template <int MODE>
 void pass2_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
-                  const NbrList* nl, const float4* aux, float* rho_dt, float* vel_dt,
+                  const NbrList* nl, const Pass1Out& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSet out, unsigned* out_hash, unsigned* err,
                   cudaStream_t s) {
     const int b = blocks_for(k.n, NS_THREADS);
     if (nl)
-        k_pass2<MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, aux, rho_dt, vel_dt,
+        k_pass2<MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt, vel_dt,
                                                       wall_rates, out, out_hash, err);
     else
-        k_pass2<MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, aux, rho_dt,
+        k_pass2<MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, p1, rho_dt,
                                                        vel_dt, wall_rates, out, out_hash, err);
 }
 
@@ -358,40 +380,40 @@ cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsi
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.pos, keys, cs, nl,
+    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.rec, keys, cs, nl,
                                                                    walls_all, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* keys,
-                         const int* cs, const NbrList* nl, float4* aux, float* rhop_sum,
+                         const int* cs, const NbrList* nl, const Pass1Out& out, float* rhop_sum,
                          float* w_sum, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (nl)
-        pass1_launch<true>(k, in, keys, cs, *nl, aux, rhop_sum, w_sum, s);
+        pass1_launch<true>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
     else
-        pass1_launch<false>(k, in, keys, cs, NbrList{}, aux, rhop_sum, w_sum, s);
+        pass1_launch<false>(k, in, keys, cs, NbrList{}, out, rhop_sum, w_sum, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in, const unsigned* keys,
-                               const int* cs, const NbrList* nl, const float4* aux,
+                               const int* cs, const NbrList* nl, const Pass1Out& p1,
                                float* rho_dt, float* vel_dt, int wall_rates, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    pass2_launch<MODE_RATES>(k, in, keys, cs, nl, aux, rho_dt, vel_dt, wall_rates, ParticleSet{},
+    pass2_launch<MODE_RATES>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, ParticleSet{},
                              nullptr, nullptr, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
                               const unsigned* keys, const int* cs, const NbrList* nl,
-                              const float4* aux, ParticleSet out, unsigned* out_hash,
+                              const Pass1Out& p1, ParticleSet out, unsigned* out_hash,
                               unsigned* err, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (half == HALF_PREDICT)
-        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, aux, nullptr, nullptr, 0, out, out_hash, err, s);
+        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err, s);
     else
-        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, aux, nullptr, nullptr, 0, out, out_hash, err, s);
+        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err, s);
     return cudaGetLastError();
 }
 

@@ -30,15 +30,25 @@ cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
                               int* cell_start, cudaStream_t s);
 
 // ---------------------------------------------------------------- resident state
-// One particle set in SoA form.  pos.w holds the particle kind as a float, vel.w the
-// density; tpos/tvel hold the predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
+// One particle set.  rec holds two float4 per particle, rec[2i] = (x, y, z, p) and
+// rec[2i+1] = (vx, vy, vz, ±rho) with rho negated for boundary (non-fluid) particles: one
+// aligned 32-byte record, the unit a neighbour gather reads.  type keeps the particle kind as
+// given (0 wall, 1 fluid, 2 rigid, ...), id the original particle index; tpos/tvel hold the
+// predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
 struct ParticleSet {
-    float4* pos = nullptr;
-    float4* vel = nullptr;
-    float* pres = nullptr;
+    float4* rec = nullptr;
+    int* type = nullptr;
     int* id = nullptr;
     float4* tpos = nullptr;
     float4* tvel = nullptr;
+};
+
+// Pass-1 output.  nrec[2i] = (x, y, z, q) with q = p' - rho0 cs h dofv for fluid particles and
+// q = p' for boundary particles, nrec[2i+1] = (vx, vy, vz, ±rho'): the record pass 2 gathers per
+// neighbour.  self[i] = (p', rho', dofv, 0): the particle's own side.
+struct Pass1Out {
+    float4* nrec = nullptr;
+    float4* self = nullptr;
 };
 
 enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
@@ -55,8 +65,8 @@ int nbr_capacity_for(const sph_params& p);
 
 // Neighbour passes (equation/ns.cu).  nl == NULL walks the cells in every pass.
 //  build : fills nl for the sorted set (walls keep only fluid neighbours unless walls_all).
-//  pass 1: aux[i] = (p, rho, dofv, 0) — boundary particles get the extrapolated p and rho,
-//          fluid particles their own p, rho and the velocity divergence.  rhop_sum / w_sum are
+//  pass 1: fills a Pass1Out — boundary particles get the extrapolated p and rho, fluid
+//          particles their own p, rho and the velocity divergence.  rhop_sum / w_sum are
 //          written when non-NULL.
 //  pass 2: either rates only (rho_dt, AoS vel_dt) or rates + the predictor/corrector update
 //          written into `out` (slot-aligned with `in`) with the next cell hash.
@@ -64,15 +74,15 @@ cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsi
                              const int* cell_start, const NbrList& nl, int walls_all,
                              unsigned* err, cudaStream_t s);
 cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
-                         const int* cell_start, const NbrList* nl, float4* aux, float* rhop_sum,
-                         float* w_sum, cudaStream_t s);
+                         const int* cell_start, const NbrList* nl, const Pass1Out& out,
+                         float* rhop_sum, float* w_sum, cudaStream_t s);
 cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
                                const unsigned* sorted_keys, const int* cell_start,
-                               const NbrList* nl, const float4* aux, float* rho_dt,
+                               const NbrList* nl, const Pass1Out& p1, float* rho_dt,
                                float* vel_dt, int wall_rates, cudaStream_t s);
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
                               const unsigned* sorted_keys, const int* cell_start,
-                              const NbrList* nl, const float4* aux, ParticleSet out,
+                              const NbrList* nl, const Pass1Out& p1, ParticleSet out,
                               unsigned* out_hash, unsigned* err, cudaStream_t s);
 
 // Resident-state glue (lib/mesh.cu).
@@ -90,7 +100,7 @@ cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float*
                               const float* s_rho, const float* s_p, const int* s_type,
                               const int* hash, ParticleSet dst, unsigned* keys,
                               unsigned* err, cudaStream_t s);
-cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* aux,
+cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* self,
                                 float* s_rho, float* s_p, float* dofv, cudaStream_t s);
 
 // Per-phase device timing of sph_step (SPH_OPT_PROFILE).
@@ -112,7 +122,7 @@ struct sph_ctx {
     unsigned* hash_x = nullptr;      // next cell of every slot of x
     unsigned* keys_sorted = nullptr; // sorted cell keys of y
     int* perm = nullptr;             // y slot k came from x slot perm[k]
-    float4* aux = nullptr;           // pass-1 output
+    sph::Pass1Out p1;                // pass-1 output
     int* cell_start = nullptr;       // [num_cells + 1]
     int cell_capacity = 0;
     void* sort_scratch = nullptr;

@@ -354,15 +354,20 @@ __global__ void k_recover(float* __restrict__ pos, float* __restrict__ vel,
 }
 
 // ---------------------------------------------------------------- resident-state kernels
+// Signed density of a record: negative marks a boundary (non-fluid) particle.
+__device__ __forceinline__ float signed_rho(int type, float rho) {
+    return type == SPH_TYPE_FLUID ? rho : -rho;
+}
+
 __global__ void k_gather(int n, const int* __restrict__ perm, ParticleSet src, ParticleSet dst,
                          int with_tmp) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int s = perm[k];
     if ((unsigned)s >= (unsigned)n) s = k;  // a consistent permutation never takes this
-    dst.pos[k] = src.pos[s];
-    dst.vel[k] = src.vel[s];
-    dst.pres[k] = src.pres[s];
+    dst.rec[2 * (size_t)k] = src.rec[2 * (size_t)s];
+    dst.rec[2 * (size_t)k + 1] = src.rec[2 * (size_t)s + 1];
+    dst.type[k] = src.type[s];
     dst.id[k] = src.id[s];
     if (with_tmp) {
         dst.tpos[k] = src.tpos[s];
@@ -376,13 +381,15 @@ __global__ void k_upload_convert(KParams kp, const float* __restrict__ pos,
                                  ParticleSet dst, unsigned* __restrict__ hash, unsigned* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
-    float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    dst.pos[i] = make_float4(x, y, z, (float)type[i]);
-    dst.vel[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], rho[i]);
-    dst.pres[i] = p[i];
+    const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    const float vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
+    const int t = type[i];
+    dst.rec[2 * (size_t)i] = make_float4(x, y, z, p[i]);
+    dst.rec[2 * (size_t)i + 1] = make_float4(vx, vy, vz, signed_rho(t, rho[i]));
+    dst.type[i] = t;
     dst.id[i] = i;
     dst.tpos[i] = make_float4(x, y, z, rho[i]);
-    dst.tvel[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0f);
+    dst.tvel[i] = make_float4(vx, vy, vz, 0.0f);
     unsigned f = 0;
     hash[i] = (unsigned)cell_hash_clamped(kp, x, y, z, &f);
     raise_flags(err, f);
@@ -395,12 +402,12 @@ __global__ void k_download_convert(int n, ParticleSet src, float* __restrict__ p
     if (k >= n) return;
     int r = src.id[k];
     if ((unsigned)r >= (unsigned)n) return;
-    float4 a = src.pos[k], v = src.vel[k];
+    const float4 a = src.rec[2 * (size_t)k], v = src.rec[2 * (size_t)k + 1];
     if (pos) { pos[3 * r] = a.x; pos[3 * r + 1] = a.y; pos[3 * r + 2] = a.z; }
     if (vel) { vel[3 * r] = v.x; vel[3 * r + 1] = v.y; vel[3 * r + 2] = v.z; }
-    if (rho) rho[r] = v.w;
-    if (p) p[r] = src.pres[k];
-    if (type) type[r] = (int)a.w;
+    if (rho) rho[r] = fabsf(v.w);
+    if (p) p[r] = a.w;
+    if (type) type[r] = src.type[k];
 }
 
 // A sorted hash outside [0, num_cells) (a particle outside the grid) is clamped to the
@@ -412,9 +419,11 @@ __global__ void k_aos_to_set(int n, int num_cells, const float* __restrict__ s_p
                              unsigned* __restrict__ keys, unsigned* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    dst.pos[i] = make_float4(s_pos[3 * i], s_pos[3 * i + 1], s_pos[3 * i + 2], (float)s_type[i]);
-    dst.vel[i] = make_float4(s_vel[3 * i], s_vel[3 * i + 1], s_vel[3 * i + 2], s_rho[i]);
-    dst.pres[i] = s_p[i];
+    const int t = s_type[i];
+    dst.rec[2 * (size_t)i] = make_float4(s_pos[3 * i], s_pos[3 * i + 1], s_pos[3 * i + 2], s_p[i]);
+    dst.rec[2 * (size_t)i + 1] =
+        make_float4(s_vel[3 * i], s_vel[3 * i + 1], s_vel[3 * i + 2], signed_rho(t, s_rho[i]));
+    dst.type[i] = t;
     int h = hash[i];
     unsigned f = 0;
     if (h < 0 || h >= num_cells) {
@@ -426,11 +435,11 @@ __global__ void k_aos_to_set(int n, int num_cells, const float* __restrict__ s_p
 }
 
 __global__ void k_ns_writeback(int n, const int* __restrict__ s_type,
-                               const float4* __restrict__ aux, float* __restrict__ s_rho,
+                               const float4* __restrict__ self, float* __restrict__ s_rho,
                                float* __restrict__ s_p, float* __restrict__ dofv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float4 a = aux[i];
+    const float4 a = self[i];
     if (s_type[i] != SPH_TYPE_FLUID) {
         s_p[i] = a.x;
         s_rho[i] = a.y;
@@ -550,10 +559,10 @@ cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float*
     return cudaGetLastError();
 }
 
-cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* aux,
+cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* self,
                                 float* s_rho, float* s_p, float* dofv, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_ns_writeback<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, s_type, aux, s_rho, s_p, dofv);
+    k_ns_writeback<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, s_type, self, s_rho, s_p, dofv);
     return cudaGetLastError();
 }
 

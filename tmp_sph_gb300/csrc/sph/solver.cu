@@ -5,12 +5,13 @@
 // SPH_NS, PC_prediction, recover, then the same for PC_correction).  Here one half step is
 //
 //   radix sort (cell key, slot)  ->  gather x -> y in cell order + dense cell starts
-//   ->  pass 1 (y -> aux)  ->  pass 2 + integrator (y, aux -> x, next cell keys)
+//   ->  neighbour-list build (y)  ->  pass 1 (y -> neighbour records p1)
+//   ->  pass 2 + integrator (p1 -> x, next cell keys)
 //
 // so the state never returns to original order inside a step (the original particle id
 // travels with it and is used only by sph_download), there is no separate hash kernel
-// (pass 2 writes the next keys), and no host synchronisation: a full step is 2 x 7 kernel
-// launches plus 2 memsets, captured once as a CUDA graph and replayed.
+// (pass 2 writes the next keys), and no host synchronisation: a full step is 2 x 15 kernel
+// launches plus 2 x 2 memsets, captured once as a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -29,16 +30,15 @@ cudaError_t dalloc(T** p, size_t count) {
 }
 
 void free_set(ParticleSet& s) {
-    cudaFree(s.pos); cudaFree(s.vel); cudaFree(s.pres); cudaFree(s.id);
+    cudaFree(s.rec); cudaFree(s.type); cudaFree(s.id);
     cudaFree(s.tpos); cudaFree(s.tvel);
     s = ParticleSet{};
 }
 
 cudaError_t alloc_set(ParticleSet& s, int cap) {
     cudaError_t e;
-    if ((e = dalloc(&s.pos, cap)) != cudaSuccess) return e;
-    if ((e = dalloc(&s.vel, cap)) != cudaSuccess) return e;
-    if ((e = dalloc(&s.pres, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.rec, 2 * (size_t)cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.type, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.id, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tpos, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tvel, cap)) != cudaSuccess) return e;
@@ -56,7 +56,9 @@ void release(sph_ctx* c) {
     drop_graph(c);
     free_set(c->x);
     free_set(c->y);
-    cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm); cudaFree(c->aux);
+    cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm);
+    cudaFree(c->p1.nrec); cudaFree(c->p1.self);
+    c->p1 = Pass1Out{};
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
     cudaFree(c->nl.idx); cudaFree(c->nl.count);
     c->nl = NbrList{};
@@ -67,8 +69,9 @@ void release(sph_ctx* c) {
 int to_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
 
 // Device staging for host transfers, carved from buffers that hold nothing between steps
-// (the predictor's saved state of the sorted set and the pass-1 output), so the sorted view
-// of the last step (y.pos/vel/id, sorted keys, cell starts) survives an upload/download.
+// (the predictor's saved state of the sorted set and the pass-1 neighbour records), so the
+// sorted view of the last step (y.rec/type/id, sorted keys, cell starts) survives an
+// upload/download.
 struct Staging {
     float* pos;   // 3n floats
     float* vel;   // 3n floats
@@ -81,7 +84,7 @@ Staging staging(sph_ctx* c, int n) {
     Staging s;
     s.pos = reinterpret_cast<float*>(c->y.tpos);
     s.vel = reinterpret_cast<float*>(c->y.tvel);
-    float* a = reinterpret_cast<float*>(c->aux);
+    float* a = reinterpret_cast<float*>(c->p1.nrec);  // 8n floats
     s.rho = a;
     s.p = a + n;
     s.type = reinterpret_cast<int*>(a + 2 * (size_t)n);
@@ -122,11 +125,11 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
                   cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, nullptr, nullptr,
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, nullptr, nullptr,
                           s)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_PASS2], s);
-    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->aux, c->x,
+    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->p1, c->x,
                           c->hash_x, c->err, s);
     if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
@@ -175,7 +178,8 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = dalloc(&c->hash_x, cap);
     if (e == cudaSuccess) e = dalloc(&c->keys_sorted, cap);
     if (e == cudaSuccess) e = dalloc(&c->perm, cap);
-    if (e == cudaSuccess) e = dalloc(&c->aux, cap);
+    if (e == cudaSuccess) e = dalloc(&c->p1.nrec, 2 * (size_t)cap);
+    if (e == cudaSuccess) e = dalloc(&c->p1.self, cap);
     if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)p->num_cells + 1);
     c->cell_capacity = p->num_cells;
     c->sort_scratch_bytes = sort_scratch_bytes(cap);
@@ -449,13 +453,13 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl,
                                     c->opt_wall_rates, c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, rhop_sum, w_sum,
+    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
                           s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, nl, c->aux, rho_dt,
+    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt,
                                 vel_dt, c->opt_wall_rates, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_ns_writeback(k, s_type, c->aux, s_rho, s_p, dofv, s)) != cudaSuccess)
+    if ((e = launch_ns_writeback(k, s_type, c->p1.self, s_rho, s_p, dofv, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     return SPH_OK;
 }

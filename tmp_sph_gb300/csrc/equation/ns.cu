@@ -78,39 +78,53 @@ __device__ __forceinline__ void for_each_candidate(const KParams& k, const int* 
     }
 }
 
-// Walk the cells of particle i and call f(j, dx, dy, dz, r2) for every j != i within the
-// support radius; R holds the particles' records (position in R[2j].xyz).
+// One 32-byte record (two float4) in a single 256-bit read-only load: a neighbour gather
+// touches one L1 sector with one request.  R is 32-byte aligned (cudaMalloc'd, two float4 per
+// particle).
+__device__ __forceinline__ void ld_rec(const float4* __restrict__ R, int j, float4& a,
+                                       float4& b) {
+    const float4* p = R + 2 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
+// Walk the cells of particle i over the dense positions X (x, y, z, ±1) and call
+// f(j, pj, dx, dy, dz, r2) for every j != i within the support radius.
 template <class F>
 __device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restrict__ cs,
                                            const unsigned* __restrict__ keys,
-                                           const float4* __restrict__ R, int i, const float4& pi,
+                                           const float4* __restrict__ X, int i, const float4& pi,
                                            F&& f) {
     int cx, cy, cz;
     cell_of_key(k, keys[i], cx, cy, cz);
     for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-        const float4 pj = __ldg(R + 2 * (size_t)j);
+        const float4 pj = __ldg(X + j);
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dist2(dx, dy, dz);
-        if (r2 < k.kh2 && j != i) f(j, dx, dy, dz, r2);
+        if (r2 < k.kh2 && j != i) f(j, pj, dx, dy, dz, r2);
     });
 }
 
-// Neighbours of i from the list (or by walking the cells when i overflowed it).  The list row
-// of i is read as 16-byte vectors of four neighbour slots; R supplies the positions.
+// Neighbours of i with their records R[2j], R[2j+1]: from the list (one 256-bit record load
+// per neighbour, list rows read as 16-byte vectors of four slots), or by walking the cells
+// over X when i overflowed the list.  f(j, a, b, dx, dy, dz, r2).
 template <bool LIST, class F>
-__device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restrict__ cs,
-                                            const unsigned* __restrict__ keys,
-                                            const NbrList& nl, const float4* __restrict__ R,
-                                            int i, const float4& pi, F&& f) {
+__device__ __forceinline__ void visit_records(const KParams& k, const int* __restrict__ cs,
+                                              const unsigned* __restrict__ keys,
+                                              const NbrList& nl, const float4* __restrict__ X,
+                                              const float4* __restrict__ R, int i,
+                                              const float4& pi, F&& f) {
     if (LIST) {
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             const int4* __restrict__ row =
                 reinterpret_cast<const int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
             auto one = [&](int j) {
-                const float4 pj = __ldg(R + 2 * (size_t)j);
-                const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                f(j, dx, dy, dz, dist2(dx, dy, dz));
+                float4 a, b;
+                ld_rec(R, j, a, b);
+                const float dx = pi.x - a.x, dy = pi.y - a.y, dz = pi.z - a.z;
+                f(j, a, b, dx, dy, dz, dist2(dx, dy, dz));
             };
 #pragma unroll 1
             for (int c = 0; c < cnt; c += 4) {
@@ -123,7 +137,12 @@ __device__ __forceinline__ void visit_pairs(const KParams& k, const int* __restr
             return;
         }
     }
-    walk_pairs(k, cs, keys, R, i, pi, f);
+    walk_pairs(k, cs, keys, X, i, pi, [&](int j, const float4&, float dx, float dy, float dz,
+                                          float r2) {
+        float4 a, b;
+        ld_rec(R, j, a, b);
+        f(j, a, b, dx, dy, dz, r2);
+    });
 }
 
 __device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho > 0.f; }
@@ -133,18 +152,18 @@ __device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho 
 // Rows are particle-major (row i = idx + i * cap) and written as 16-byte vectors of four
 // slots, buffered in registers, so a warp store moves 512 B instead of 128 B.
 __global__ void __launch_bounds__(NS_THREADS)
-k_nbr_build(KParams k, const float4* __restrict__ R, const unsigned* __restrict__ keys,
+k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict__ keys,
             const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4 pi = R[2 * (size_t)i];
-    const bool keep_all = fluid_rec(R[2 * (size_t)i + 1].w) || walls_all;
+    const float4 pi = X[i];
+    const bool keep_all = fluid_rec(pi.w) || walls_all;
     int cnt = 0;
     int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     int4* __restrict__ row = reinterpret_cast<int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
     const int cap = nl.cap;
-    walk_pairs(k, cs, keys, R, i, pi, [&](int j, float, float, float, float) {
-        if (keep_all || fluid_rec(__ldg(&R[2 * (size_t)j + 1].w))) {
+    walk_pairs(k, cs, keys, X, i, pi, [&](int j, const float4& pj, float, float, float, float) {
+        if (keep_all || fluid_rec(pj.w)) {
             const int slot = cnt & 3;
             b0 = slot == 0 ? j : b0;
             b1 = slot == 1 ? j : b1;
@@ -174,8 +193,9 @@ k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     const float4 vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
     const bool fi = fluid_rec(vi.w);
     float dofv = 0.f, rs = 0.f, ws = 0.f;
-    visit_pairs<LIST>(k, cs, keys, nl, R, i, pi, [&](int j, float dx, float dy, float dz, float r2) {
-        const float4 vj = __ldg(R + 2 * (size_t)j + 1);
+    visit_records<LIST>(k, cs, keys, nl, in.xyz, R, i, pi,
+                        [&](int, const float4& aj, const float4& vj, float dx, float dy, float dz,
+                            float r2) {
         if (!fluid_rec(vj.w)) return;
         const float rr = sqrtf(r2);
         const float q = rr * k.inv_h;
@@ -183,8 +203,7 @@ k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
         const float t2 = t * t;
         if (!fi) {
             const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
-            const float pj_ = __ldg(&R[2 * (size_t)j].w);
-            rs += (pj_ + vj.w * k.g * dz) * w;
+            rs += (aj.w + vj.w * k.g * dz) * w;
             ws += w;
         } else {
             const float fr = k.c_fr * t2 * t;
@@ -234,9 +253,10 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     float drho = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
     if (fi || (MODE == MODE_RATES && wall_rates)) {
         const float damp_i = k.damper * dofvi;
-        visit_pairs<LIST>(k, cs, keys, nl, NR, i, pi, [&](int j, float dx, float dy, float dz, float r2) {
-            const float4 aj = __ldg(NR + 2 * (size_t)j);      // x, y, z, q
-            const float4 vj = __ldg(NR + 2 * (size_t)j + 1);  // vx, vy, vz, ±rho
+        // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour
+        visit_records<LIST>(k, cs, keys, nl, in.xyz, NR, i, pi,
+                            [&](int j, const float4& aj, const float4& vj, float dx, float dy,
+                                float dz, float r2) {
             const bool fj = fluid_rec(vj.w);
             const float rhoj = fabsf(vj.w);
             const float rr = sqrtf(r2);
@@ -380,7 +400,7 @@ cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsi
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.rec, keys, cs, nl,
+    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.xyz, keys, cs, nl,
                                                                    walls_all, err);
     return cudaGetLastError();
 }

@@ -37,6 +37,7 @@ cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
 // predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
 struct ParticleSet {
     float4* rec = nullptr;
+    float4* xyz = nullptr;  // sorted set only: dense (x, y, z, ±1) for candidate walks
     int* type = nullptr;
     int* id = nullptr;
     float4* tpos = nullptr;

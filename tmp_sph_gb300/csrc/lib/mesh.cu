@@ -365,8 +365,10 @@ __global__ void k_gather(int n, const int* __restrict__ perm, ParticleSet src, P
     if (k >= n) return;
     int s = perm[k];
     if ((unsigned)s >= (unsigned)n) s = k;  // a consistent permutation never takes this
-    dst.rec[2 * (size_t)k] = src.rec[2 * (size_t)s];
-    dst.rec[2 * (size_t)k + 1] = src.rec[2 * (size_t)s + 1];
+    const float4 a = src.rec[2 * (size_t)s], b = src.rec[2 * (size_t)s + 1];
+    dst.rec[2 * (size_t)k] = a;
+    dst.rec[2 * (size_t)k + 1] = b;
+    dst.xyz[k] = make_float4(a.x, a.y, a.z, b.w > 0.f ? 1.f : -1.f);
     dst.type[k] = src.type[s];
     dst.id[k] = src.id[s];
     if (with_tmp) {
@@ -423,6 +425,8 @@ __global__ void k_aos_to_set(int n, int num_cells, const float* __restrict__ s_p
     dst.rec[2 * (size_t)i] = make_float4(s_pos[3 * i], s_pos[3 * i + 1], s_pos[3 * i + 2], s_p[i]);
     dst.rec[2 * (size_t)i + 1] =
         make_float4(s_vel[3 * i], s_vel[3 * i + 1], s_vel[3 * i + 2], signed_rho(t, s_rho[i]));
+    dst.xyz[i] = make_float4(s_pos[3 * i], s_pos[3 * i + 1], s_pos[3 * i + 2],
+                             t == SPH_TYPE_FLUID ? 1.f : -1.f);
     dst.type[i] = t;
     int h = hash[i];
     unsigned f = 0;

@@ -30,7 +30,7 @@ cudaError_t dalloc(T** p, size_t count) {
 }
 
 void free_set(ParticleSet& s) {
-    cudaFree(s.rec); cudaFree(s.type); cudaFree(s.id);
+    cudaFree(s.rec); cudaFree(s.xyz); cudaFree(s.type); cudaFree(s.id);
     cudaFree(s.tpos); cudaFree(s.tvel);
     s = ParticleSet{};
 }
@@ -38,6 +38,7 @@ void free_set(ParticleSet& s) {
 cudaError_t alloc_set(ParticleSet& s, int cap) {
     cudaError_t e;
     if ((e = dalloc(&s.rec, 2 * (size_t)cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.xyz, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.type, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.id, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tpos, cap)) != cudaSuccess) return e;

@@ -161,9 +161,11 @@ def launches_per_step(p) -> int:
     while bits < 31 and (1 << bits) < p.num_cells:
         bits += 1
     passes = (bits + 7) // 8
-    # per half step: 3 kernels per radix pass, gather, cell mark, cell fill, neighbour-list
-    # build, pass 1, pass 2
-    return 2 * (3 * passes + 6)
+    # per half step, all launched whether or not the lists are rebuilt (gated kernels return
+    # at once when they are not): rebuild decision, sort-totals clear, 3 kernels per radix
+    # pass, gather + copy back, cell-start clear, mark and fill, neighbour-list build,
+    # pass 1, pass 2
+    return 2 * (3 * passes + 10)
 
 
 def cpu_baseline(st, p, budget_s: float = 20.0) -> dict:
@@ -226,7 +228,8 @@ def config_block(args, p, n):
             "fluid_particles": n - p.num_boundary, "dx_m": p.dx, "h_over_dx": 1.3,
             "cells": p.num_cells, "eos": "tait", "dt_s": p.dt,
             "parallelism": f"replicas x{dist_env()[0]}",
-            "l2": "state larger than L2 (no flush needed)"}
+            "l2": "state larger than L2 (no flush needed)",
+            "neighbour_list_skin_over_kh": args.skin / 1000.0}
 
 
 def main():
@@ -239,6 +242,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--skin", type=int, default=100,
+                    help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -257,6 +262,7 @@ def main():
     n = len(st["rho"])
     stream = torch.cuda.Stream()
     sol = S.Solver(p, n)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
 
     def barrier():
@@ -267,6 +273,7 @@ def main():
         sol.step(args.warmup, stream=stream)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    rebuilds0 = sol.rebuild_count(stream=stream)
     with ClockSampler(gpu_uuid(local)) as clk:
         barrier()
         torch.cuda.synchronize()
@@ -281,7 +288,22 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     flags = sol.error_flags(stream=stream)
+    rebuilds = sol.rebuild_count(stream=stream) - rebuilds0
     value = n * ws * args.steps / (ms / 1e3)
+
+    # the same solver rebuilding its lists every half step (no skin): the cost a fast flow
+    # approaches, for comparison with the reuse measured above
+    k0 = min(args.steps, 50)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
+    sol.step(3, stream=stream)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    sol.step(k0, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms0 = ev0.elapsed_time(ev1)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+    no_reuse = {"value": n * k0 / (ms0 / 1e3), "ms_per_step": ms0 / k0, "steps": k0}
 
     # per-kernel device time from CUDA events around every phase, same stream
     prof_steps = min(args.steps, 20)
@@ -351,6 +373,9 @@ def main():
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
         "gpu_launches": launches_per_step(p) * args.steps,
+        "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
+                          "skin_permille": args.skin},
+        "rebuild_every_half_step": no_reuse,
         "clocks": clk.summary(),
         "device_error_flags": flags,
     }

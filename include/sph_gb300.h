@@ -222,7 +222,13 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_NEIGHBOR_LIST 4  /* 1 (default): one cell walk per half step fills a neighbour
                                     list both passes iterate; 0: each pass walks the cells */
 #define SPH_OPT_NEIGHBOR_CAP  5  /* list slots per particle; 0 (default) = 1.5x the lattice
-                                    neighbours of the support sphere (reallocates the list) */
+                                    neighbours of the list sphere (reallocates the list) */
+#define SPH_OPT_SKIN_PERMILLE 6  /* neighbour-list skin in thousandths of the support radius kh
+                                    (default 100).  The list keeps every pair closer than
+                                    kh (1 + skin) and is rebuilt, cell list included, only when
+                                    some particle has moved more than skin/2 since the last
+                                    build (decided on the GPU each half step); 0 rebuilds every
+                                    half step as the reference does */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
  * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;
@@ -262,9 +268,11 @@ int sph_step(sph_ctx* ctx, int nsteps, void* stream);
  * synchronises the stream before returning. */
 int sph_step_host(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
                   int n, int nsteps, void* stream);
-/* Sorted-order views for diagnostics / tests (device pointers owned by ctx). */
+/* Views of the last cell-list rebuild for diagnostics / tests (device pointers owned by ctx):
+ * dense cell starts [num_cells + 1], original id per slot, sorted cell key per slot, and the
+ * number of cells of the solver's grid (cells of kh (1 + skin)). */
 int sph_ctx_sorted_view(sph_ctx* ctx, const int** cell_start, const int** sorted_id,
-                        const int** sorted_hash);
+                        const int** sorted_hash, int* num_cells);
 /* Read and clear the device error flags (synchronises the stream). */
 int sph_read_error_flags(sph_ctx* ctx, unsigned* flags, void* stream);
 /* Steps taken since the last upload. */
@@ -272,6 +280,8 @@ int sph_steps_taken(const sph_ctx* ctx, long long* steps);
 /* Accumulated milliseconds and launch counts per phase under SPH_OPT_PROFILE
  * (arrays of SPH_PHASE_COUNT); reset != 0 clears them. */
 int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
+/* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream). */
+int sph_read_rebuild_count(sph_ctx* ctx, unsigned* count, void* stream);
 
 /* ---------------------------------------------------------------- reference-signature shim */
 /* The library also exports, with C++ linkage, the reference's own host functions calcHash,

@@ -82,32 +82,78 @@ def run_opts(st, p, nsteps, opts):
         sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
         sol.step(nsteps, stream=s)
         out = sol.download(stream=s)
+        out["rebuilds"] = sol.rebuild_count(stream=s)
         flags = sol.error_flags(stream=s)
     return out, flags
 
 
 def test_neighbor_list_matches_cell_walk(sphlib, cuda):
-    """The neighbour-list passes visit the same pairs in the same order as passes that walk
-    the cells themselves, so the steps agree bit for bit."""
+    """Without a skin the list is rebuilt every half step and the list passes visit the same
+    pairs in the same order as passes that walk the cells themselves: bit-identical steps."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    a, fa = run_opts(st, p, 5, {api.SPH_OPT_NEIGHBOR_LIST: 1})
-    b, fb = run_opts(st, p, 5, {api.SPH_OPT_NEIGHBOR_LIST: 0})
+    a, fa = run_opts(st, p, 5, {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 1})
+    b, fb = run_opts(st, p, 5, {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 0})
     assert fa == 0 and fb == 0
     for k in ("pos", "vel", "rho", "p"):
         assert np.array_equal(a[k], b[k]), k
 
 
 def test_neighbor_list_overflow_falls_back(sphlib, cuda):
-    """With an 8-slot list every fluid particle overflows: it is flagged and walks its cells,
+    """With a 16-slot list every fluid particle overflows: it is flagged and walks its cells,
     giving the same result."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    a, fa = run_opts(st, p, 3, {api.SPH_OPT_NEIGHBOR_CAP: 8})
-    b, fb = run_opts(st, p, 3, {api.SPH_OPT_NEIGHBOR_LIST: 0})
-    assert fa & api.SPH_FLAG_NEIGHBOR_OVERFLOW and fb == 0
-    for k in ("pos", "vel", "rho", "p"):
-        assert np.array_equal(a[k], b[k]), k
+    for skin in (0, 100):
+        a, fa = run_opts(st, p, 3, {api.SPH_OPT_SKIN_PERMILLE: skin, api.SPH_OPT_NEIGHBOR_CAP: 8})
+        b, fb = run_opts(st, p, 3, {api.SPH_OPT_SKIN_PERMILLE: skin})
+        assert fa & api.SPH_FLAG_NEIGHBOR_OVERFLOW and fb == 0
+        for k in ("pos", "vel", "rho", "p"):
+            assert np.array_equal(a[k], b[k]), (skin, k)
+
+
+@pytest.mark.parametrize("skin", [100, 300])
+def test_skin_reuse_matches_oracle(sphlib, oracle, cuda, report, skin):
+    """Reusing the cell and neighbour lists while particles stay within skin/2 evaluates the
+    same pairs (r < kh) as rebuilding every half step: 20 steps agree with the oracle within
+    float rounding, and the lists were rebuilt fewer times than there were half steps."""
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    n = len(st["rho"])
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(20, stream=s)
+        out = sol.download(stream=s)
+        rebuilds = sol.rebuild_count(stream=s)
+        flags = sol.error_flags(stream=s)
+    ref = oracle.run(oracle.params_like(p), st, 20)
+    e = field_errors(out, ref, st)
+    for k, v in e.items():
+        report(f"skin {skin} 20 steps {k}", v, 2e-4)
+    report(f"skin {skin} rebuilds in 40 half steps", rebuilds)
+    assert flags == 0
+    assert all(v < 2e-4 for v in e.values()), e
+    assert 1 <= rebuilds < 40
+
+
+def test_skin_reuse_fast_flow(sphlib, oracle, cuda, report):
+    """Fast random velocities (±2 m/s) force frequent rebuilds; results still match."""
+    from tmp_sph_gb300 import api, cases
+    from gpu_util import perturbed
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    st = perturbed(st, vamp=2.0, ramp=0.0)
+    out, flags = run_opts(st, p, 6, {api.SPH_OPT_SKIN_PERMILLE: 100})
+    ref = oracle.run(oracle.params_like(p), st, 6)
+    e = field_errors(out, ref, st)
+    for k, v in e.items():
+        report(f"skin fast flow 6 steps {k}", v, 2e-4)
+    report("skin fast flow rebuilds in 12 half steps", out["rebuilds"])
+    assert flags == 0
+    assert all(v < 2e-4 for v in e.values()), e
+    assert out["rebuilds"] >= 2
 
 
 def test_upload_download_roundtrip(sphlib, cuda):
@@ -197,17 +243,17 @@ def test_large_case_properties(sphlib, cuda, report):
         sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
         sol.step(5, stream=s)
         out = sol.download(stream=s)
-        cs_ptr, id_ptr, key_ptr = sol.sorted_view()
+        cs_ptr, id_ptr, key_ptr, ncells = sol.sorted_view()
         import ctypes as C
         keys = np.zeros(n, np.int32)
         ids = np.zeros(n, np.int32)
-        cs = np.zeros(p.num_cells + 1, np.int32)
+        cs = np.zeros(ncells + 1, np.int32)
         torch.cuda.synchronize()
         rt = C.CDLL("libcudart.so.13")  # already loaded as the library's dependency
         rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
         assert rt.cudaMemcpy(keys.ctypes.data, key_ptr, n * 4, 2) == 0
         assert rt.cudaMemcpy(ids.ctypes.data, id_ptr, n * 4, 2) == 0
-        assert rt.cudaMemcpy(cs.ctypes.data, cs_ptr, (p.num_cells + 1) * 4, 2) == 0
+        assert rt.cudaMemcpy(cs.ctypes.data, cs_ptr, (ncells + 1) * 4, 2) == 0
         flags = sol.error_flags(stream=s)
     assert flags == 0
     fl = st["type"] == 1
@@ -220,5 +266,5 @@ def test_large_case_properties(sphlib, cuda, report):
     assert (np.diff(keys) >= 0).all()
     assert cs[0] == 0 and cs[-1] == n and (np.diff(cs) >= 0).all()
     occ = np.unique(keys)
-    assert (cs[occ + 1] - cs[occ] == np.bincount(keys, minlength=p.num_cells)[occ]).all()
+    assert (cs[occ + 1] - cs[occ] == np.bincount(keys, minlength=ncells)[occ]).all()
     report("large 5 steps max |v|", float(np.abs(out["vel"][fl]).max()))

@@ -38,6 +38,7 @@ SPH_OPT_WALL_RATES = 2
 SPH_OPT_PROFILE = 3
 SPH_OPT_NEIGHBOR_LIST = 4
 SPH_OPT_NEIGHBOR_CAP = 5
+SPH_OPT_SKIN_PERMILLE = 6
 SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
 SPH_PHASE_COUNT = 5
 PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")
@@ -138,7 +139,8 @@ _PROTOS = {
     "sph_download": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "sph_step": (_I, [_P, _I, _P]),
     "sph_step_host": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
-    "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I)]),
+    "sph_read_rebuild_count": (_I, [_P, C.POINTER(C.c_uint), _P]),
     "sph_read_error_flags": (_I, [_P, C.POINTER(C.c_uint), _P]),
     "sph_steps_taken": (_I, [_P, C.POINTER(C.c_longlong)]),
     "sph_profile_read": (_I, [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), _I]),

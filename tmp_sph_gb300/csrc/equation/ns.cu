@@ -27,6 +27,11 @@
 // the same order, so the sums are the same as a walking pass.  A particle with more hits than
 // the list capacity is marked and walks the cells itself (same order again).
 //
+// With a Verlet skin the list is built with the cutoff kh(1 + skin) (kh2_list) on cells that
+// wide and kept while every particle stays within skin*kh/2 of its build position; both
+// passes still test r < kh on the current positions, and k_nbr_build keeps the build
+// positions (xb) that pass 2 measures each particle's displacement against.
+//
 // Kernel algebra (same quantities as the reference, simplified): with r = x_i - x_j,
 // q = |r|/h, t = 1 - q/2, the Wendland C2 gradient is grad W = c_fr t^3 r with
 // c_fr = -5 adh / h^2, which is the reference's per-component expression
@@ -89,27 +94,29 @@ __device__ __forceinline__ void ld_rec(const float4* __restrict__ R, int j, floa
         : "l"(p));
 }
 
-// Walk the cells of particle i over the dense positions X (x, y, z, ±1) and call
-// f(j, pj, dx, dy, dz, r2) for every j != i within the support radius.
-template <class F>
+// Walk the cells of particle i over the positions X[STRIDE * j] and call
+// f(j, pj, dx, dy, dz, r2) for every j != i with r2 < cut2.  X is the dense (x, y, z, ±1) array
+// (STRIDE 1) or a record array (STRIDE 2).
+template <int STRIDE, class F>
 __device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restrict__ cs,
                                            const unsigned* __restrict__ keys,
                                            const float4* __restrict__ X, int i, const float4& pi,
-                                           F&& f) {
+                                           float cut2, F&& f) {
     int cx, cy, cz;
     cell_of_key(k, keys[i], cx, cy, cz);
     for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-        const float4 pj = __ldg(X + j);
+        const float4 pj = __ldg(X + (size_t)STRIDE * (size_t)j);
         const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         const float r2 = dist2(dx, dy, dz);
-        if (r2 < k.kh2 && j != i) f(j, pj, dx, dy, dz, r2);
+        if (r2 < cut2 && j != i) f(j, pj, dx, dy, dz, r2);
     });
 }
 
-// Neighbours of i with their records R[2j], R[2j+1]: from the list (one 256-bit record load
-// per neighbour, list rows read as 16-byte vectors of four slots), or by walking the cells
-// over X when i overflowed the list.  f(j, a, b, dx, dy, dz, r2).
-template <bool LIST, class F>
+// Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one 256-bit
+// record load per listed pair, list rows read as 16-byte vectors of four slots; pairs in the
+// skin beyond the support radius are skipped), or by walking the cells over X[XSTRIDE * j]
+// when i overflowed the list.  f(j, a, b, dx, dy, dz, r2).
+template <bool LIST, int XSTRIDE, class F>
 __device__ __forceinline__ void visit_records(const KParams& k, const int* __restrict__ cs,
                                               const unsigned* __restrict__ keys,
                                               const NbrList& nl, const float4* __restrict__ X,
@@ -124,7 +131,8 @@ __device__ __forceinline__ void visit_records(const KParams& k, const int* __res
                 float4 a, b;
                 ld_rec(R, j, a, b);
                 const float dx = pi.x - a.x, dy = pi.y - a.y, dz = pi.z - a.z;
-                f(j, a, b, dx, dy, dz, dist2(dx, dy, dz));
+                const float r2 = dist2(dx, dy, dz);
+                if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
             };
 #pragma unroll 1
             for (int c = 0; c < cnt; c += 4) {
@@ -137,8 +145,8 @@ __device__ __forceinline__ void visit_records(const KParams& k, const int* __res
             return;
         }
     }
-    walk_pairs(k, cs, keys, X, i, pi, [&](int j, const float4&, float dx, float dy, float dz,
-                                          float r2) {
+    walk_pairs<XSTRIDE>(k, cs, keys, X, i, pi, k.kh2,
+                        [&](int j, const float4&, float dx, float dy, float dz, float r2) {
         float4 a, b;
         ld_rec(R, j, a, b);
         f(j, a, b, dx, dy, dz, r2);
@@ -153,16 +161,20 @@ __device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho 
 // slots, buffered in registers, so a warp store moves 512 B instead of 128 B.
 __global__ void __launch_bounds__(NS_THREADS)
 k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict__ keys,
-            const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err) {
+            const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err,
+            const unsigned* gate) {
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
     const float4 pi = X[i];
+    if (nl.xb) nl.xb[i] = pi;
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     int cnt = 0;
     int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     int4* __restrict__ row = reinterpret_cast<int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
     const int cap = nl.cap;
-    walk_pairs(k, cs, keys, X, i, pi, [&](int j, const float4& pj, float, float, float, float) {
+    walk_pairs<1>(k, cs, keys, X, i, pi, k.kh2_list,
+                  [&](int j, const float4& pj, float, float, float, float) {
         if (keep_all || fluid_rec(pj.w)) {
             const int slot = cnt & 3;
             b0 = slot == 0 ? j : b0;
@@ -193,7 +205,7 @@ k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     const float4 vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
     const bool fi = fluid_rec(vi.w);
     float dofv = 0.f, rs = 0.f, ws = 0.f;
-    visit_records<LIST>(k, cs, keys, nl, in.xyz, R, i, pi,
+    visit_records<LIST, 1>(k, cs, keys, nl, in.xyz, R, i, pi,
                         [&](int, const float4& aj, const float4& vj, float dx, float dy, float dz,
                             float r2) {
         if (!fluid_rec(vj.w)) return;
@@ -236,14 +248,18 @@ enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
 // artificial viscosity, gravity); then either the rates are stored (MODE_RATES) or the
 // midpoint predictor / corrector of src/sph/sph_run.cu:425-519 is applied and the updated
 // particle written to `out` with its next cell hash.
+//
+// `out` may alias `in`: the update touches only particle i's own rows, and neighbours (also
+// the positions of a cell walk) come from the pass-1 records.  Returns the squared distance
+// of particle i from its position when the neighbour list was built (0 without a list).
 template <int MODE, bool LIST>
-__global__ void __launch_bounds__(NS_THREADS)
-k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, NbrList nl, Pass1Out p1, float* __restrict__ rho_dt,
-        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
-        unsigned* __restrict__ out_hash, unsigned* err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+__device__ __forceinline__ float pass2_one(const KParams& k, int i, const ParticleSet& in,
+                                           const unsigned* __restrict__ keys,
+                                           const int* __restrict__ cs, const NbrList& nl,
+                                           const Pass1Out& p1, float* __restrict__ rho_dt,
+                                           float* __restrict__ vel_dt, int wall_rates,
+                                           const ParticleSet& out,
+                                           unsigned* __restrict__ out_hash, unsigned* err) {
     const float4* __restrict__ NR = p1.nrec;
     const float4 pi = NR[2 * (size_t)i];
     const float4 vi = NR[2 * (size_t)i + 1];
@@ -254,7 +270,7 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     if (fi || (MODE == MODE_RATES && wall_rates)) {
         const float damp_i = k.damper * dofvi;
         // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour
-        visit_records<LIST>(k, cs, keys, nl, in.xyz, NR, i, pi,
+        visit_records<LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
                             [&](int j, const float4& aj, const float4& vj, float dx, float dy,
                                 float dz, float r2) {
             const bool fj = fluid_rec(vj.w);
@@ -292,7 +308,7 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
         vel_dt[3 * i] = have ? ax : 0.f;
         vel_dt[3 * i + 1] = have ? ay : 0.f;
         vel_dt[3 * i + 2] = have ? az : 0.f;
-        return;
+        return 0.f;
     }
 
     float4 np = pi, nv;
@@ -347,6 +363,7 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     }
     out.rec[2 * (size_t)i] = make_float4(np.x, np.y, np.z, npres);
     out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+    if (out.xyz) out.xyz[i] = make_float4(np.x, np.y, np.z, fi ? 1.f : -1.f);
     out.type[i] = in.type[i];
     out.id[i] = in.id[i];
     if (MODE == MODE_PRED) {
@@ -356,6 +373,35 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     unsigned f = 0;
     out_hash[i] = (unsigned)cell_hash_clamped(k, np.x, np.y, np.z, &f);
     raise_flags(err, f);
+    if (!fi || !nl.xb) return 0.f;
+    const float4 xb = nl.xb[i];
+    return dist2(np.x - xb.x, np.y - xb.y, np.z - xb.z);
+}
+
+template <int MODE, bool LIST>
+__global__ void __launch_bounds__(NS_THREADS)
+k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
+        const int* __restrict__ cs, NbrList nl, Pass1Out p1, float* __restrict__ rho_dt,
+        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
+        unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < k.n)
+        d2 = pass2_one<MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                   out_hash, err);
+    if (MODE == MODE_RATES || disp == nullptr) return;
+    // block maximum of the squared displacement, one atomic per block (non-negative floats
+    // order like their bit patterns)
+    __shared__ unsigned s_max[NS_THREADS / 32];
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned m = s_max[0];
+#pragma unroll
+        for (int w = 1; w < NS_THREADS / 32; w++) m = max(m, s_max[w]);
+        if (m) atomicMax(disp, m);
+    }
 }
 
 inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
@@ -375,21 +421,22 @@ template <int MODE>
 void pass2_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
                   const NbrList* nl, const Pass1Out& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSet out, unsigned* out_hash, unsigned* err,
-                  cudaStream_t s) {
+                  unsigned* disp, cudaStream_t s) {
     const int b = blocks_for(k.n, NS_THREADS);
     if (nl)
         k_pass2<MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt, vel_dt,
-                                                      wall_rates, out, out_hash, err);
+                                                      wall_rates, out, out_hash, err, disp);
     else
         k_pass2<MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, p1, rho_dt,
-                                                       vel_dt, wall_rates, out, out_hash, err);
+                                                       vel_dt, wall_rates, out, out_hash, err,
+                                                       nullptr);
 }
 
 }  // namespace
 
-int nbr_capacity_for(const sph_params& p) {
-    // 1.5x the particles of a lattice inside the support sphere, rounded up to 16
-    const double r = (double)p.kh / (double)p.dx;
+int nbr_capacity_for(const sph_params& p, double skin) {
+    // 1.5x the particles of a lattice inside the list sphere, rounded up to 16
+    const double r = (double)p.kh * (1.0 + skin) / (double)p.dx;
     const double lattice = 4.18879020478639 * r * r * r;
     int cap = (int)(1.5 * lattice) + 16;
     cap = (cap + 15) & ~15;
@@ -398,10 +445,10 @@ int nbr_capacity_for(const sph_params& p) {
 
 cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* keys,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
-                             cudaStream_t s) {
+                             cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
     k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                                   walls_all, err);
+                                                                   walls_all, err, gate);
     return cudaGetLastError();
 }
 
@@ -421,19 +468,21 @@ cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in, const un
                                float* rho_dt, float* vel_dt, int wall_rates, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     pass2_launch<MODE_RATES>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, ParticleSet{},
-                             nullptr, nullptr, s);
+                             nullptr, nullptr, nullptr, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
                               const unsigned* keys, const int* cs, const NbrList* nl,
                               const Pass1Out& p1, ParticleSet out, unsigned* out_hash,
-                              unsigned* err, cudaStream_t s) {
+                              unsigned* err, unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (half == HALF_PREDICT)
-        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err, s);
+        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err,
+                                disp, s);
     else
-        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err, s);
+        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err,
+                                disp, s);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,7 @@ struct KParams {
     float gmin_x, gmin_y, gmin_z;
     float cell;          // cell edge (gridSize)
     float h, inv_h, kh, kh2;
+    float kh2_list;      // squared list cutoff (support radius + skin); kh2 without a skin
     float eta2;
     float adh;           // 21/(16 pi h^3)
     float c_fr;          // -5 adh / h^2: grad W = c_fr (1 - q/2)^3 r
@@ -103,6 +104,14 @@ __device__ __forceinline__ bool escaped(const KParams& k, float x, float y, floa
 }
 
 __device__ __forceinline__ bool is_fluid(float typef) { return typef == 1.0f; }
+
+// Kernels of the cell-list rebuild take a gate word: NULL runs unconditionally, otherwise the
+// kernel does nothing unless *gate is non-zero (decided on the device each half step, so one
+// captured CUDA graph serves steps that rebuild and steps that reuse the neighbour list).
+// Every thread of a block reads the same word, so a gated-off block returns as a whole.
+__device__ __forceinline__ bool gated_off(const unsigned* gate) {
+    return gate != nullptr && *gate == 0u;
+}
 
 // Fold a thread's flags into the device error word (flags are rare: one atomic per
 // flagged thread, no warp-wide collective so it is safe under divergence).

@@ -18,16 +18,18 @@ namespace sph {
 // keys_out / vals_out (which may alias keys_in / vals_in).  err (may be NULL) receives
 // SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.
 size_t sort_scratch_bytes(int n);
+// gate: see gated_off() — NULL sorts unconditionally.
 cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
                              int* vals_out, int n, int key_bits, void* scratch,
-                             size_t scratch_bytes, unsigned* err, cudaStream_t s);
+                             size_t scratch_bytes, unsigned* err, cudaStream_t s,
+                             const unsigned* gate = nullptr);
 int key_bits_for(int num_cells);
 
 // ---------------------------------------------------------------- cell list (lib/mesh.cu)
 // Dense cell starts: cell_start[c] = first sorted slot whose key >= c, for c in [0, C];
 // cell_start[C] = n.  Keys must be sorted and < C.
 cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
-                              int* cell_start, cudaStream_t s);
+                              int* cell_start, cudaStream_t s, const unsigned* gate = nullptr);
 
 // ---------------------------------------------------------------- resident state
 // One particle set.  rec holds two float4 per particle, rec[2i] = (x, y, z, p) and
@@ -57,12 +59,17 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // Per-half-step neighbour list: idx[i * cap + c] is the c-th neighbour of slot i (walk
 // order), count[i] how many; count[i] > cap means the list overflowed for i and the passes
 // walk the cells for it instead.  cap is a multiple of 16 (rows are 16-byte aligned).
+// The list holds every pair closer than the list cutoff (KParams::kh2_list, the support
+// radius plus a skin); xb (may be NULL) receives each slot's position when the list is built,
+// from which the integrator tracks how far particles have moved since.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
     int cap = 0;
+    float4* xb = nullptr;
 };
-int nbr_capacity_for(const sph_params& p);
+// List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
+int nbr_capacity_for(const sph_params& p, double skin = 0.0);
 
 // Neighbour passes (equation/ns.cu).  nl == NULL walks the cells in every pass.
 //  build : fills nl for the sorted set (walls keep only fluid neighbours unless walls_all).
@@ -73,7 +80,7 @@ int nbr_capacity_for(const sph_params& p);
 //          written into `out` (slot-aligned with `in`) with the next cell hash.
 cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
                              const int* cell_start, const NbrList& nl, int walls_all,
-                             unsigned* err, cudaStream_t s);
+                             unsigned* err, cudaStream_t s, const unsigned* gate = nullptr);
 cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
                          const int* cell_start, const NbrList* nl, const Pass1Out& out,
                          float* rhop_sum, float* w_sum, cudaStream_t s);
@@ -81,14 +88,19 @@ cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
                                const unsigned* sorted_keys, const int* cell_start,
                                const NbrList* nl, const Pass1Out& p1, float* rho_dt,
                                float* vel_dt, int wall_rates, cudaStream_t s);
+// `out` may be `in` (the update is per particle; neighbours are read from p1).  disp (may be
+// NULL) receives, by atomicMax on its float bits, the largest squared distance of a fluid
+// particle from its position when the list was built (nl->xb).
 cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
                               const unsigned* sorted_keys, const int* cell_start,
                               const NbrList* nl, const Pass1Out& p1, ParticleSet out,
-                              unsigned* out_hash, unsigned* err, cudaStream_t s);
+                              unsigned* out_hash, unsigned* err, unsigned* disp, cudaStream_t s);
 
 // Resident-state glue (lib/mesh.cu).
+// perm == NULL copies slot for slot.
 cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
-                          ParticleSet dst, int with_tmp, cudaStream_t s);
+                          ParticleSet dst, int with_tmp, cudaStream_t s,
+                          const unsigned* gate = nullptr);
 cudaError_t launch_upload_convert(const KParams& k, const float* pos, const float* vel,
                                   const float* rho, const float* p, const int* type,
                                   ParticleSet dst, unsigned* hash, unsigned* err,
@@ -130,8 +142,13 @@ struct sph_ctx {
     size_t sort_scratch_bytes = 0;
     unsigned* err = nullptr;         // device error word
 
-    // neighbour list of the current half step
+    // neighbour list, reused across half steps while every particle stays within skin/2 of
+    // where it was when the list was built
     sph::NbrList nl;
+    sph_params Pi{};                 // internal grid: cells of kh (1 + skin)
+    double skin = 0.1;               // list skin as a fraction of the support radius kh
+    unsigned* rb = nullptr;          // [0] rebuild gate, [1] max squared displacement (float
+                                     // bits), [2] forced rebuild, [3] rebuild count
 
     // graph replay of one full step
     int opt_use_graph = 1;

@@ -60,8 +60,9 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 __global__ void __launch_bounds__(RS_THREADS)
 k_rs_upsweep(const unsigned* __restrict__ keys, int n, int shift, unsigned xmask,
              int check_bits, unsigned* __restrict__ hist, int tiles,
-             unsigned* __restrict__ totals, unsigned* err) {
+             unsigned* __restrict__ totals, unsigned* err, const unsigned* gate) {
     __shared__ unsigned cnt[RS_RADIX];
+    if (gated_off(gate)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     cnt[tid] = 0;
     __syncthreads();
@@ -87,9 +88,11 @@ k_rs_upsweep(const unsigned* __restrict__ keys, int n, int shift, unsigned xmask
 // Exclusive scan of one digit's row of tile counts, offset by the counts of all smaller
 // digits: after this, hist[d * tiles + t] is the first output slot of digit d in tile t.
 __global__ void __launch_bounds__(RS_THREADS)
-k_rs_scan(unsigned* __restrict__ hist, int tiles, const unsigned* __restrict__ totals) {
+k_rs_scan(unsigned* __restrict__ hist, int tiles, const unsigned* __restrict__ totals,
+          const unsigned* gate) {
     __shared__ unsigned wsum[RS_WARPS];
     __shared__ unsigned s_carry;
+    if (gated_off(gate)) return;
     const int d = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // base = sum of totals of digits < d
     unsigned v = (tid < d) ? totals[tid] : 0u;
@@ -135,7 +138,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 k_rs_downsweep(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
                unsigned* __restrict__ keys_out, int* __restrict__ vals_out,
                const unsigned* __restrict__ hist, int n, int shift, unsigned xmask_in,
-               unsigned xmask_out, int tiles) {
+               unsigned xmask_out, int tiles, const unsigned* gate) {
     __shared__ unsigned s_cnt[RS_WARPS][RS_RADIX];
     __shared__ unsigned s_gbase[RS_RADIX];
     __shared__ unsigned s_tpre[RS_RADIX];
@@ -143,6 +146,7 @@ k_rs_downsweep(const unsigned* __restrict__ keys_in, const int* __restrict__ val
     __shared__ int s_vals[RS_TILE];
     __shared__ unsigned s_wsum[RS_WARPS];
 
+    if (gated_off(gate)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int w = 0; w < RS_WARPS; w++) s_cnt[w][tid] = 0;
@@ -217,14 +221,30 @@ k_rs_downsweep(const unsigned* __restrict__ keys_in, const int* __restrict__ val
     }
 }
 
-__global__ void k_iota(int* v, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = i;
+// Gated memset: the graph-capturable stand-in for cudaMemsetAsync inside a gated rebuild.
+__global__ void k_fill_u32(unsigned* __restrict__ p, unsigned value, long count,
+                           const unsigned* gate) {
+    if (gated_off(gate)) return;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (long)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+cudaError_t fill_u32(unsigned* p, unsigned value, long count, const unsigned* gate,
+                     cudaStream_t s) {
+    if (!gate)
+        return (value & 0xffu) * 0x01010101u == value
+                   ? cudaMemsetAsync(p, (int)(value & 0xffu), (size_t)count * sizeof(unsigned), s)
+                   : cudaErrorInvalidValue;
+    const int blocks = (int)std::min<long>((count + 255) / 256, 152L * 8);
+    k_fill_u32<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(p, value, count, gate);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- dense cell starts
 __global__ void k_cell_mark(const unsigned* __restrict__ keys, int n, int num_cells,
-                            int* __restrict__ cs) {
+                            int* __restrict__ cs, const unsigned* gate) {
+    if (gated_off(gate)) return;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned key = keys[k];
@@ -239,9 +259,11 @@ constexpr int FILL_CHUNK = FILL_THREADS * FILL_PER_THREAD;
 // Each block owns FILL_CHUNK cells; the value flowing in from the right of the chunk is the
 // first slot whose key is >= the chunk end (one binary search per block).
 __global__ void __launch_bounds__(FILL_THREADS)
-k_cell_fill(int* __restrict__ cs, int num_cells, const unsigned* __restrict__ keys, int n) {
+k_cell_fill(int* __restrict__ cs, int num_cells, const unsigned* __restrict__ keys, int n,
+            const unsigned* gate) {
     __shared__ int s_carry;
     __shared__ int s_wmin[FILL_THREADS / 32];
+    if (gated_off(gate)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long c0 = (long)blockIdx.x * FILL_CHUNK;
     if (tid == 0) {
@@ -360,10 +382,11 @@ __device__ __forceinline__ float signed_rho(int type, float rho) {
 }
 
 __global__ void k_gather(int n, const int* __restrict__ perm, ParticleSet src, ParticleSet dst,
-                         int with_tmp) {
+                         int with_tmp, const unsigned* gate) {
+    if (gated_off(gate)) return;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    int s = perm[k];
+    int s = perm ? perm[k] : k;
     if ((unsigned)s >= (unsigned)n) s = k;  // a consistent permutation never takes this
     const float4 a = src.rec[2 * (size_t)s], b = src.rec[2 * (size_t)s + 1];
     dst.rec[2 * (size_t)k] = a;
@@ -472,15 +495,19 @@ size_t sort_scratch_bytes(int n) {
 
 cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
                              int* vals_out, int n, int key_bits, void* scratch,
-                             size_t scratch_bytes, unsigned* err, cudaStream_t s) {
+                             size_t scratch_bytes, unsigned* err, cudaStream_t s,
+                             const unsigned* gate) {
     if (n <= 0) return cudaSuccess;
     if (key_bits < 1 || key_bits > 32 || !scratch || scratch_bytes < sort_scratch_bytes(n))
         return cudaErrorInvalidValue;
+    const int passes = (key_bits + 7) / 8;
+    // a gated sort must not need the ungated copies below
+    if (gate && passes % 2 == 1 && (keys_in == keys_out || (vals_in && vals_in == vals_out)))
+        return cudaErrorInvalidValue;
     SortScratch sc = carve(scratch, n);
     const int tiles = rs_tiles(n);
-    const int passes = (key_bits + 7) / 8;
     const unsigned xm = key_bits == 32 ? 0x80000000u : 0u;  // signed order for full keys
-    cudaError_t e = cudaMemsetAsync(sc.totals, 0, (size_t)RS_MAX_PASSES * RS_RADIX * sizeof(unsigned), s);
+    cudaError_t e = fill_u32(sc.totals, 0u, (long)RS_MAX_PASSES * RS_RADIX, gate, s);
     if (e != cudaSuccess) return e;
     const unsigned* kin = keys_in;
     const int* vin = vals_in;
@@ -509,10 +536,10 @@ cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsign
         const unsigned xout = (p == passes - 1) ? xm : 0u;
         unsigned* totals = sc.totals + (size_t)p * RS_RADIX;
         k_rs_upsweep<<<tiles, RS_THREADS, 0, s>>>(kin, n, shift, xin, p == 0 ? key_bits : 32,
-                                                   sc.hist, tiles, totals, err);
-        k_rs_scan<<<RS_RADIX, RS_THREADS, 0, s>>>(sc.hist, tiles, totals);
+                                                   sc.hist, tiles, totals, err, gate);
+        k_rs_scan<<<RS_RADIX, RS_THREADS, 0, s>>>(sc.hist, tiles, totals, gate);
         k_rs_downsweep<<<tiles, RS_THREADS, 0, s>>>(kin, vin, kdst, vdst, sc.hist, n, shift, xin,
-                                                     xout, tiles);
+                                                     xout, tiles, gate);
         kin = kdst;
         vin = vdst;
     }
@@ -520,19 +547,20 @@ cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsign
 }
 
 cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells, int* cs,
-                              cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(cs, 0x7f, (size_t)(num_cells + 1) * sizeof(int), s);
+                              cudaStream_t s, const unsigned* gate) {
+    cudaError_t e = fill_u32(reinterpret_cast<unsigned*>(cs), 0x7f7f7f7fu, (long)num_cells + 1,
+                             gate, s);
     if (e != cudaSuccess) return e;
-    if (n > 0) k_cell_mark<<<blocks_for(n, 256), 256, 0, s>>>(sorted_keys, n, num_cells, cs);
+    if (n > 0) k_cell_mark<<<blocks_for(n, 256), 256, 0, s>>>(sorted_keys, n, num_cells, cs, gate);
     k_cell_fill<<<blocks_for((long)num_cells + 1, FILL_CHUNK), FILL_THREADS, 0, s>>>(
-        cs, num_cells, sorted_keys, n);
+        cs, num_cells, sorted_keys, n, gate);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
-                          ParticleSet dst, int with_tmp, cudaStream_t s) {
+                          ParticleSet dst, int with_tmp, cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    k_gather<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, perm, src, dst, with_tmp);
+    k_gather<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, perm, src, dst, with_tmp, gate);
     return cudaGetLastError();
 }
 

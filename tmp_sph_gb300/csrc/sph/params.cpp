@@ -40,6 +40,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.inv_h = (float)(1.0 / (double)p.h);
     k.kh = p.kh;
     k.kh2 = p.kh * p.kh;
+    k.kh2_list = k.kh2;
     k.eta2 = p.eta * p.eta;
     k.adh = p.adh;
     k.c_fr = (float)(-5.0 * (double)p.adh / ((double)p.h * (double)p.h));

@@ -4,16 +4,26 @@
 // Reference counterpart: the step loop of src/sph/sph_run.cu:285-336 (hash, sort, reorder,
 // SPH_NS, PC_prediction, recover, then the same for PC_correction).  Here one half step is
 //
-//   radix sort (cell key, slot)  ->  gather x -> y in cell order + dense cell starts
-//   ->  neighbour-list build (y)  ->  pass 1 (y -> neighbour records p1)
-//   ->  pass 2 + integrator (p1 -> x, next cell keys)
+//   rebuild decision  ->  [radix sort (cell key, slot)  ->  gather y -> x -> y in cell order
+//   + dense cell starts  ->  neighbour-list build (y)]  ->  pass 1 (y -> records p1)
+//   ->  pass 2 + integrator (p1 -> y in place, next cell keys, largest displacement)
 //
 // so the state never returns to original order inside a step (the original particle id
 // travels with it and is used only by sph_download), there is no separate hash kernel
-// (pass 2 writes the next keys), and no host synchronisation: a full step is 2 x 15 kernel
-// launches plus 2 x 2 memsets, captured once as a CUDA graph and replayed.
+// (pass 2 writes the next keys), and no host synchronisation: a full step is a fixed list
+// of launches, captured once as a CUDA graph and replayed.
+//
+// Verlet skin.  The cells are kh(1 + skin) wide and the list holds every pair closer than
+// kh(1 + skin) at build time.  While no particle has moved more than skin*kh/2 since the
+// build, every pair now closer than kh is in the list, so the bracketed kernels are skipped:
+// k_decide (one thread, on the GPU) compares the largest displacement pass 2 recorded with
+// that bound and writes a gate word the gated kernels read before doing any work.  The
+// passes test r < kh themselves, so they evaluate the same pairs as a rebuild every half
+// step; only the order of the sums within a particle can differ.  skin = 0 rebuilds every
+// half step on the reference's cell size.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -61,8 +71,10 @@ void release(sph_ctx* c) {
     cudaFree(c->p1.nrec); cudaFree(c->p1.self);
     c->p1 = Pass1Out{};
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
-    cudaFree(c->nl.idx); cudaFree(c->nl.count);
+    cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb);
     c->nl = NbrList{};
+    cudaFree(c->rb);
+    c->rb = nullptr;
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -70,9 +82,8 @@ void release(sph_ctx* c) {
 int to_status(cudaError_t e) { return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA; }
 
 // Device staging for host transfers, carved from buffers that hold nothing between steps
-// (the predictor's saved state of the sorted set and the pass-1 neighbour records), so the
-// sorted view of the last step (y.rec/type/id, sorted keys, cell starts) survives an
-// upload/download.
+// (the scratch set's predictor arrays and the pass-1 neighbour records); the live state (y),
+// the sorted keys, cell starts and neighbour list are untouched by an upload/download.
 struct Staging {
     float* pos;   // 3n floats
     float* vel;   // 3n floats
@@ -83,8 +94,8 @@ struct Staging {
 
 Staging staging(sph_ctx* c, int n) {
     Staging s;
-    s.pos = reinterpret_cast<float*>(c->y.tpos);
-    s.vel = reinterpret_cast<float*>(c->y.tvel);
+    s.pos = reinterpret_cast<float*>(c->x.tpos);
+    s.vel = reinterpret_cast<float*>(c->x.tvel);
     float* a = reinterpret_cast<float*>(c->p1.nrec);  // 8n floats
     s.rho = a;
     s.p = a + n;
@@ -107,31 +118,80 @@ constexpr int EV_PER_HALF = PH_COUNT + 1;
 // The neighbour list to use this half step, or NULL to walk the cells in every pass.
 const NbrList* list_for(sph_ctx* c) { return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr; }
 
+// The resident solver's own grid: the caller's grid box with cells of kh (1 + skin), so a walk
+// of the 27 cells around a particle's cell at the last rebuild still finds every particle
+// within kh of it while no particle has moved more than skin/2.  skin = 0 keeps the caller's
+// grid exactly (cells of kh).
+sph_params internal_params(const sph_params& P, double skin) {
+    if (!(skin > 0.0)) return P;
+    sph_params Q = P;
+    Q.cell_size = (float)((double)P.kh * (1.0 + skin));
+    if (Q.cell_size < P.cell_size) Q.cell_size = P.cell_size;
+    for (int c = 0; c < 3; c++) {
+        float span = (Q.grid_max[c] - Q.grid_min[c]) / Q.cell_size;
+        Q.grid_dim[c] = (int)ceilf(span);
+        if (Q.grid_dim[c] < 1) Q.grid_dim[c] = 1;
+    }
+    Q.num_cells = Q.grid_dim[0] * Q.grid_dim[1] * Q.grid_dim[2];
+    return Q;
+}
+
+KParams resident_kparams(const sph_ctx* c) {
+    KParams k = make_kparams(c->Pi, c->n);
+    const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
+    k.kh2_list = (float)(cut * cut);
+    if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
+    return k;
+}
+
+// Rebuild decision, one thread: rebuild when forced, when the cells are walked every half
+// step (no list), or when some fluid particle has moved farther than skin/2 from where it was
+// at the last build (rb[1] holds the largest squared displacement as float bits).
+__global__ void k_decide(unsigned* rb, unsigned threshold_bits, int always) {
+    const bool rebuild = always || rb[2] != 0u || rb[1] > threshold_bits;
+    rb[0] = rebuild ? 1u : 0u;
+    if (rebuild) {
+        rb[1] = 0u;
+        rb[2] = 0u;
+        rb[3] += 1u;
+    }
+}
+
 // One half step (see the file comment).  `ev` (may be NULL) receives PH_COUNT + 1 timestamps.
 cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev) {
-    const KParams k = make_kparams(c->P, c->n);
-    const int bits = key_bits_for(c->P.num_cells);
+    const KParams k = resident_kparams(c);
+    const int bits = key_bits_for(c->Pi.num_cells);
     const NbrList* nl = list_for(c);
+    const unsigned* gate = c->rb;
+    const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
+    const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
+    unsigned thr_bits;
+    memcpy(&thr_bits, &thr, sizeof(thr_bits));
     cudaError_t e;
     if (ev) cudaEventRecord(ev[PH_SORT], s);
+    k_decide<<<1, 1, 0, s>>>(c->rb, thr_bits, nl ? 0 : 1);
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
-                         c->sort_scratch_bytes, c->err, s);
+                         c->sort_scratch_bytes, c->err, s, gate);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_GATHER], s);
-    if ((e = launch_gather(k, c->perm, c->x, c->y, half == HALF_CORRECT, s)) != cudaSuccess) return e;
-    if ((e = build_cell_starts(c->keys_sorted, c->n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
+    // permute the live set y into cell order through x, then copy it back
+    if ((e = launch_gather(k, c->perm, c->y, c->x, 1, s, gate)) != cudaSuccess) return e;
+    if ((e = launch_gather(k, nullptr, c->x, c->y, 1, s, gate)) != cudaSuccess) return e;
+    if ((e = build_cell_starts(c->keys_sorted, c->n, c->Pi.num_cells, c->cell_start, s, gate)) !=
+        cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_NBR], s);
-    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s)) !=
-                  cudaSuccess)
+    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s,
+                                    gate)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
     if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, nullptr, nullptr,
                           s)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_PASS2], s);
-    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->p1, c->x,
-                          c->hash_x, c->err, s);
+    // in place: pass 2 reads its neighbours from the pass-1 records
+    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->p1, c->y,
+                          c->hash_x, c->err, c->rb + 1, s);
     if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
 }
@@ -142,18 +202,27 @@ cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
     return half_step(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr);
 }
 
+// Next half step rebuilds the cell and neighbour lists whatever the displacement.
+cudaError_t force_rebuild(sph_ctx* c, cudaStream_t s) {
+    return cudaMemsetAsync(c->rb + 2, 1, sizeof(unsigned), s);
+}
+
 cudaError_t alloc_list(sph_ctx* c) {
     // the option is rounded up to a multiple of 16 so rows stay 16-byte aligned
-    const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15 : nbr_capacity_for(c->P);
+    const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
+                                       : nbr_capacity_for(c->P, c->skin);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
     cudaFree(c->nl.idx);
     cudaFree(c->nl.count);
+    cudaFree(c->nl.xb);
     c->nl = NbrList{};
     cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * (size_t)(c->capacity > 0 ? c->capacity : 1));
     if (e == cudaSuccess) e = dalloc(&c->nl.count, c->capacity);
+    if (e == cudaSuccess) e = dalloc(&c->nl.xb, c->capacity);
     if (e != cudaSuccess) {
         cudaFree(c->nl.idx);
         cudaFree(c->nl.count);
+        cudaFree(c->nl.xb);
         c->nl = NbrList{};
         return e;
     }
@@ -170,6 +239,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     sph_ctx* c = new (std::nothrow) sph_ctx();
     if (!c) return SPH_ERR_NOMEM;
     c->P = *p;
+    c->Pi = internal_params(*p, c->skin);
     c->capacity = capacity;
     cudaGetDevice(&c->device);
     cudaError_t e = cudaSuccess;
@@ -181,12 +251,14 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = dalloc(&c->perm, cap);
     if (e == cudaSuccess) e = dalloc(&c->p1.nrec, 2 * (size_t)cap);
     if (e == cudaSuccess) e = dalloc(&c->p1.self, cap);
-    if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)p->num_cells + 1);
-    c->cell_capacity = p->num_cells;
+    c->cell_capacity = std::max(p->num_cells, c->Pi.num_cells);
+    if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)c->cell_capacity + 1);
     c->sort_scratch_bytes = sort_scratch_bytes(cap);
     if (e == cudaSuccess) e = cudaMalloc(&c->sort_scratch, c->sort_scratch_bytes);
     if (e == cudaSuccess) e = dalloc(&c->err, 1);
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = dalloc(&c->rb, 4);
+    if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = alloc_list(c);
     for (auto& ev : c->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
@@ -207,27 +279,35 @@ extern "C" int sph_destroy(sph_ctx* c) {
     return SPH_OK;
 }
 
+// Grows the cell-start array to hold `cells` + 1 entries; the only allocation outside
+// sph_create besides the neighbour list (a grid with more cells).
+static cudaError_t ensure_cells(sph_ctx* c, int cells) {
+    if (cells <= c->cell_capacity) return cudaSuccess;
+    int* cs = nullptr;
+    cudaError_t e = dalloc(&cs, (size_t)cells + 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+    }
+    cudaFree(c->cell_start);
+    c->cell_start = cs;
+    c->cell_capacity = cells;
+    return cudaSuccess;
+}
+
 extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     if (!c || !params_ok(p)) return SPH_ERR_ARG;
-    if (p->num_cells > c->cell_capacity) {
-        // the one place besides sph_create that allocates: a grid with more cells
-        int* cs = nullptr;
-        if (dalloc(&cs, (size_t)p->num_cells + 1) != cudaSuccess) {
-            cudaGetLastError();
-            return SPH_ERR_NOMEM;
-        }
-        cudaFree(c->cell_start);
-        c->cell_start = cs;
-        c->cell_capacity = p->num_cells;
-    }
+    const sph_params pi = internal_params(*p, c->skin);
+    if (ensure_cells(c, std::max(p->num_cells, pi.num_cells)) != cudaSuccess) return SPH_ERR_NOMEM;
     c->P = *p;
+    c->Pi = pi;
     drop_graph(c);
     // and the neighbour list, when the support radius holds more lattice neighbours
     if (alloc_list(c) != cudaSuccess) {
         cudaGetLastError();
         return SPH_ERR_NOMEM;
     }
-    return SPH_OK;
+    return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_get_params(const sph_ctx* c, sph_params* out) {
@@ -242,18 +322,32 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
         case SPH_OPT_USE_GRAPH: c->opt_use_graph = value != 0; drop_graph(c); return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_PROFILE: c->opt_profile = value != 0; return SPH_OK;
-        case SPH_OPT_NEIGHBOR_LIST: c->opt_nbr_list = value != 0; drop_graph(c); return SPH_OK;
+        case SPH_OPT_NEIGHBOR_LIST:
+            c->opt_nbr_list = value != 0;
+            drop_graph(c);
+            break;
         case SPH_OPT_NEIGHBOR_CAP:
-            if (value < 0) return SPH_ERR_ARG;
-            c->opt_nbr_cap = value;
+        case SPH_OPT_SKIN_PERMILLE:
+            if (value < 0 || (option == SPH_OPT_SKIN_PERMILLE && value > 2000)) return SPH_ERR_ARG;
+            if (option == SPH_OPT_NEIGHBOR_CAP) {
+                c->opt_nbr_cap = value;
+            } else {
+                if (c->P.num_cells <= 0) return SPH_ERR_STATE;
+                const sph_params pi = internal_params(c->P, value / 1000.0);
+                if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
+                c->skin = value / 1000.0;
+                c->Pi = pi;
+            }
             drop_graph(c);
             if (alloc_list(c) != cudaSuccess) {
                 cudaGetLastError();
                 return SPH_ERR_NOMEM;
             }
-            return SPH_OK;
+            break;
         default: return SPH_ERR_ARG;
     }
+    // the cell and neighbour lists no longer match: rebuild them next half step
+    return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
 extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const float* rho,
@@ -287,8 +381,13 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
             return SPH_ERR_CUDA;
         dpos = spos; dvel = svel; drho = srho; dp = sp; dtype = stype;
     }
-    KParams k = make_kparams(c->P, n);
-    return to_status(launch_upload_convert(k, dpos, dvel, drho, dp, dtype, c->x, c->hash_x, c->err, s));
+    // the state goes straight into the live set, hashed on the solver's grid; the first half
+    // step sorts it
+    const KParams k = resident_kparams(c);
+    if (cudaMemsetAsync(c->rb, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
+        force_rebuild(c, s) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    return to_status(launch_upload_convert(k, dpos, dvel, drho, dp, dtype, c->y, c->hash_x, c->err, s));
 }
 
 extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, float* p, int* type,
@@ -300,14 +399,14 @@ extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, floa
     cudaStream_t s = (cudaStream_t)stream;
     KParams k = make_kparams(c->P, n);
     if (!to_host)
-        return to_status(launch_download_convert(k, c->x, pos, vel, rho, p, type, s));
+        return to_status(launch_download_convert(k, c->y, pos, vel, rho, p, type, s));
     Staging st = staging(c, n);
     float* spos = pos ? st.pos : nullptr;
     float* svel = vel ? st.vel : nullptr;
     float* srho = rho ? st.rho : nullptr;
     float* sp = p ? st.p : nullptr;
     int* stype = type ? st.type : nullptr;
-    cudaError_t e = launch_download_convert(k, c->x, spos, svel, srho, sp, stype, s);
+    cudaError_t e = launch_download_convert(k, c->y, spos, svel, srho, sp, stype, s);
     if (e != cudaSuccess) return SPH_ERR_CUDA;
     if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (vel && cudaMemcpyAsync(vel, svel, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
@@ -392,8 +491,9 @@ extern "C" int sph_step_host(sph_ctx* c, float* pos, float* vel, float* rho, flo
 }
 
 extern "C" int sph_ctx_sorted_view(sph_ctx* c, const int** cell_start, const int** sorted_id,
-                                   const int** sorted_hash) {
+                                   const int** sorted_hash, int* num_cells) {
     if (!c) return SPH_ERR_ARG;
+    if (num_cells) *num_cells = c->Pi.num_cells;
     if (cell_start) *cell_start = c->cell_start;
     if (sorted_id) *sorted_id = c->y.id;
     if (sorted_hash) *sorted_hash = reinterpret_cast<const int*>(c->keys_sorted);
@@ -445,22 +545,35 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     cudaStream_t s = (cudaStream_t)stream;
     KParams k = make_kparams(c->P, n);
     cudaError_t e;
-    if ((e = launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->y, c->keys_sorted,
+    if ((e = launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->x, c->keys_sorted,
                                c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     const NbrList* nl = list_for(c);
-    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl,
+    if (nl && (e = launch_nbr_build(k, c->x, c->keys_sorted, c->cell_start, *nl,
                                     c->opt_wall_rates, c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
+    if ((e = launch_pass1(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
                           s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass2_rates(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt,
+    if ((e = launch_pass2_rates(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt,
                                 vel_dt, c->opt_wall_rates, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     if ((e = launch_ns_writeback(k, s_type, c->p1.self, s_rho, s_p, dofv, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
+    // the resident state (y) is untouched, but the cell and neighbour lists now describe these
+    // arrays: a later sph_step rebuilds them first
+    return force_rebuild(c, s) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_read_rebuild_count(sph_ctx* c, unsigned* count, void* stream) {
+    if (!c || !count) return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, c->rb + 3, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    *count = h;
     return SPH_OK;
 }

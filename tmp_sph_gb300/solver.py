@@ -107,10 +107,18 @@ class Solver:
         call("sph_profile_read", self.handle, ms, ln, 1 if reset else 0)
         return {name: {"ms": ms[i], "launches": ln[i]} for i, name in enumerate(api.PHASE_NAMES)}
 
-    def sorted_view(self) -> tuple[int, int, int]:
-        cs, sid, sh = C.c_void_p(), C.c_void_p(), C.c_void_p()
-        call("sph_ctx_sorted_view", self.handle, C.byref(cs), C.byref(sid), C.byref(sh))
-        return cs.value, sid.value, sh.value
+    def sorted_view(self) -> tuple[int, int, int, int]:
+        """(cell_start, sorted_id, sorted_hash) device addresses and the solver's cell count."""
+        cs, sid, sh, nc = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_int(0)
+        call("sph_ctx_sorted_view", self.handle, C.byref(cs), C.byref(sid), C.byref(sh),
+             C.byref(nc))
+        return cs.value, sid.value, sh.value, nc.value
+
+    def rebuild_count(self, stream=None) -> int:
+        """Cell-list / neighbour-list rebuilds since the last upload."""
+        v = C.c_uint(0)
+        call("sph_read_rebuild_count", self.handle, C.byref(v), _stream(stream))
+        return v.value
 
     def ns(self, s_pos, s_vel, s_rho, s_p, s_type, rho_dt, vel_dt, cell_start, cell_end, n,
            hash_, dofv, rhop_sum=None, w_sum=None, stream=None) -> None:

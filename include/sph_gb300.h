@@ -182,6 +182,16 @@ int sph_sort_scratch_bytes(int n, size_t* bytes);
 int sph_sort_particles(int* hash, int* index, int n, int key_bits,
                        void* scratch, size_t scratch_bytes, void* stream);
 
+/* sph_sort_particles without a scratch argument and without allocating: no counterpart in
+ * the reference.  For callers bound to the three-argument sortParticles form that may not
+ * allocate device memory during a run.  Scratch is a fixed array of this library (one per
+ * device, about 9.5 MB); n > SPH_SORT_NOALLOC_MAX_N returns SPH_ERR_SCRATCH.  The first call
+ * on a device looks up that array's address (make it before any stream capture); nothing in
+ * the array needs to start at zero.  Calls on one device whose executions overlap race on the
+ * shared array: order them on one stream or with events. */
+#define SPH_SORT_NOALLOC_MAX_N (1 << 20)
+int sph_sort_particles_noalloc(int* hash, int* index, int n, int key_bits, void* stream);
+
 /* reorder (src/header/mesh.cuh:29, src/lib/mesh.cu:89-159): cell_start[c] = first sorted
  * slot of cell c or -1 if empty, cell_end[c] = one past its last slot (untouched for an
  * empty cell), and gathers pos, vel (AoS), rho, p, type, zone into sorted order.

@@ -125,6 +125,7 @@ _PROTOS = {
     "sph_calc_hash": (_I, [_PP, _P, _P, _P, _I, _P]),
     "sph_sort_scratch_bytes": (_I, [_I, C.POINTER(C.c_size_t)]),
     "sph_sort_particles": (_I, [_P, _P, _I, _I, _P, C.c_size_t, _P]),
+    "sph_sort_particles_noalloc": (_I, [_P, _P, _I, _I, _P]),
     "sph_reorder": (_I, [_PP] + [_P] * 16 + [_I, _P]),
     "sph_recover": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sph_pc_prediction": (_I, [_PP] + [_P] * 10 + [_I, _P, _P]),

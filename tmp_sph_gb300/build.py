@@ -24,6 +24,7 @@ LIB = os.path.join(PKG, "libsph_gb300.so")
 
 SOURCES = [
     "lib/mesh.cu",
+    "lib/sort_noalloc.cu",
     "equation/ns.cu",
     "sph/integrator.cu",
     "sph/solver.cu",

@@ -312,6 +312,7 @@ def main():
     sol.step(prof_steps, stream=stream)
     prof = sol.profile(reset=True)
     sol.set_option(api.SPH_OPT_PROFILE, 0)
+    flags |= sol.error_flags(stream=stream)
     hbm_peak, peak_kind = peaks()
     phases = {}
     for name, v in prof.items():

@@ -48,14 +48,22 @@ def test_steps_match_oracle(sphlib, oracle, cuda, report, physics):
     from tmp_sph_gb300 import cases
     st, p = cases.build("small", physics=physics, dx=0.02, jitter=0.01)
     P = oracle.params_like(p)
-    for nsteps, tol in ((1, 2e-5), (20, 2e-4)):  # measured 2e-6 / 2e-5
+    # After one step the displacement (~3.5e-7 m) is only ~50 ulp of the position, so a
+    # velocity that differs in its last bits flips the rounding of pos + dt v for a few
+    # particles: 1-ulp flips with probability ~1e-4 per coordinate give disp errors of ~1e-4.
+    # The positions themselves are checked to within 1 ulp.
+    for nsteps, tol, tol_disp in ((1, 2e-5, 5e-4), (20, 2e-4, 2e-4)):  # measured 2e-6 / 2e-5
         out, flags = run_gpu(st, p, nsteps)
         ref = oracle.run(P, st, nsteps)
         assert flags == 0
         e = field_errors(out, ref, st)
         for k, v in e.items():
-            report(f"solver {physics} {nsteps} steps {k}", v, tol)
-        assert all(v < tol for v in e.values()), (nsteps, e)
+            report(f"solver {physics} {nsteps} steps {k}", v, tol_disp if k == "disp" else tol)
+        assert e["disp"] < tol_disp and all(v < tol for k, v in e.items() if k != "disp"), \
+            (nsteps, e)
+        if nsteps == 1:
+            ulp = np.spacing(np.abs(ref["pos"]).astype(np.float32))
+            assert (np.abs(out["pos"] - ref["pos"]) <= ulp).all()
         wl = st["type"] != 1
         assert np.array_equal(out["pos"][wl], st["pos"][wl])
         assert np.array_equal(out["type"], st["type"])
@@ -137,6 +145,35 @@ def test_skin_reuse_matches_oracle(sphlib, oracle, cuda, report, skin):
     assert flags == 0
     assert all(v < 2e-4 for v in e.values()), e
     assert 1 <= rebuilds < 40
+
+
+def test_grid_change_mid_run_matches_oracle(sphlib, oracle, cuda, report):
+    """Changing the skin (and so the cell grid) or re-setting the parameters between steps
+    recomputes the cell keys of the resident particles before the next rebuild: the run still
+    matches the oracle."""
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    n = len(st["rho"])
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 100)
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(3, stream=s)
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
+        sol.step(3, stream=s)
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 300)
+        sol.step(2, stream=s)
+        sol.set_params(p)
+        sol.step(2, stream=s)
+        out = sol.download(stream=s)
+        flags = sol.error_flags(stream=s)
+    ref = oracle.run(oracle.params_like(p), st, 10)
+    e = field_errors(out, ref, st)
+    for k, v in e.items():
+        report(f"grid change mid run 10 steps {k}", v, 2e-4)
+    assert flags == 0
+    assert all(v < 2e-4 for v in e.values()), e
 
 
 def test_skin_reuse_fast_flow(sphlib, oracle, cuda, report):

@@ -101,6 +101,9 @@ cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet
 cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
                           ParticleSet dst, int with_tmp, cudaStream_t s,
                           const unsigned* gate = nullptr);
+// Recompute the cell keys of `set` on the grid of `k` (k.n particles).
+cudaError_t launch_rehash(const KParams& k, const ParticleSet& set, unsigned* hash, unsigned* err,
+                          cudaStream_t s);
 cudaError_t launch_upload_convert(const KParams& k, const float* pos, const float* vel,
                                   const float* rho, const float* p, const int* type,
                                   ParticleSet dst, unsigned* hash, unsigned* err,
@@ -128,6 +131,7 @@ struct sph_ctx {
     int n = 0;
     int device = 0;
     bool loaded = false;
+    bool rehash = false;  // the grid changed since the keys in hash_x were computed
     long long steps = 0;
 
     sph::ParticleSet x;   // integrator output, slot-aligned with the previous sorted order

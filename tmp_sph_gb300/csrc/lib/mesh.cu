@@ -420,6 +420,17 @@ __global__ void k_upload_convert(KParams kp, const float* __restrict__ pos,
     raise_flags(err, f);
 }
 
+// Cell keys of a resident set on the current grid (after the grid changed under it).
+__global__ void k_rehash(KParams kp, const float4* __restrict__ xyz, unsigned* __restrict__ hash,
+                         unsigned* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    const float4 q = xyz[i];
+    unsigned f = 0;
+    hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+    raise_flags(err, f);
+}
+
 __global__ void k_download_convert(int n, ParticleSet src, float* __restrict__ pos,
                                    float* __restrict__ vel, float* __restrict__ rho,
                                    float* __restrict__ p, int* __restrict__ type) {
@@ -570,6 +581,13 @@ cudaError_t launch_upload_convert(const KParams& k, const float* pos, const floa
                                   cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     k_upload_convert<<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, dst, hash, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rehash(const KParams& k, const ParticleSet& set, unsigned* hash, unsigned* err,
+                          cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    k_rehash<<<blocks_for(k.n, 256), 256, 0, s>>>(k, set.xyz, hash, err);
     return cudaGetLastError();
 }
 

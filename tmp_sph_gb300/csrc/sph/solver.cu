@@ -301,6 +301,7 @@ extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     if (ensure_cells(c, std::max(p->num_cells, pi.num_cells)) != cudaSuccess) return SPH_ERR_NOMEM;
     c->P = *p;
     c->Pi = pi;
+    c->rehash = c->loaded;
     drop_graph(c);
     // and the neighbour list, when the support radius holds more lattice neighbours
     if (alloc_list(c) != cudaSuccess) {
@@ -337,6 +338,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
                 if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
                 c->skin = value / 1000.0;
                 c->Pi = pi;
+                c->rehash = c->loaded;
             }
             drop_graph(c);
             if (alloc_list(c) != cudaSuccess) {
@@ -359,6 +361,7 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
     c->n = n;
     c->steps = 0;
     c->loaded = true;
+    c->rehash = false;  // the upload computes the keys on the current grid
     if (n == 0) return SPH_OK;
     const float* dpos = pos;
     const float* dvel = vel;
@@ -425,6 +428,13 @@ extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
         return SPH_OK;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    if (c->rehash) {
+        // the grid changed (sph_set_params, skin option): the keys pass 2 wrote for the
+        // current positions index the old grid
+        if (launch_rehash(resident_kparams(c), c->y, c->hash_x, c->err, s) != cudaSuccess)
+            return SPH_ERR_CUDA;
+        c->rehash = false;
+    }
     if (c->opt_profile) {
         for (int i = 0; i < nsteps; i++) {
             cudaError_t e = full_step(c, s, c->ev);

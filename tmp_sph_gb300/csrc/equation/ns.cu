@@ -22,9 +22,11 @@
 // support radius, and the lanes of a warp (particles of two or three adjacent cells) almost
 // always have at least one hit per candidate, so a pass that tests and evaluates in one loop
 // pays the full pair body for every candidate.  k_nbr_build therefore walks the candidates
-// once per half step and stores the hits of particle i, in walk order, in row i of a
-// particle-major table (idx[i * cap + c]); both passes then iterate only true neighbours, in
-// the same order, so the sums are the same as a walking pass.  A particle with more hits than
+// once per list build and stores the hits of particle i, in walk order, in column i of its
+// warp's slot block (nbr_col); both passes then iterate only true neighbours, in the same
+// order, so the sums are the same as a walking pass.  The passes are limited by L1 data-stage
+// wavefronts (each lane gathers a different record): interleaving the slots makes a warp's
+// list read one line per step instead of one line per lane.  A particle with more hits than
 // the list capacity is marked and walks the cells itself (same order again).
 //
 // With a Verlet skin the list is built with the cutoff kh(1 + skin) (kh2_list) on cells that
@@ -112,10 +114,17 @@ __device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restri
     });
 }
 
+// Column of particle i in the warp-interleaved list: entry c of i is col[32 c].  The 32
+// particles of a warp share one block of cap x 32 slots, so a warp reading entry c of all its
+// lanes touches one 128-byte line.
+__device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
+    return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + (size_t)(i & 31);
+}
+
 // Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one 256-bit
-// record load per listed pair, list rows read as 16-byte vectors of four slots; pairs in the
-// skin beyond the support radius are skipped), or by walking the cells over X[XSTRIDE * j]
-// when i overflowed the list.  f(j, a, b, dx, dy, dz, r2).
+// record load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond
+// the support radius are skipped), or by walking the cells over X[XSTRIDE * j] when i
+// overflowed the list.  f(j, a, b, dx, dy, dz, r2).
 template <bool LIST, int XSTRIDE, class F>
 __device__ __forceinline__ void visit_records(const KParams& k, const int* __restrict__ cs,
                                               const unsigned* __restrict__ keys,
@@ -125,22 +134,17 @@ __device__ __forceinline__ void visit_records(const KParams& k, const int* __res
     if (LIST) {
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
-            const int4* __restrict__ row =
-                reinterpret_cast<const int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
-            auto one = [&](int j) {
+            const int* __restrict__ col = nl.idx + nbr_col(nl, i);
+            int j = cnt > 0 ? __ldg(col) : 0;
+#pragma unroll 1
+            for (int c = 0; c < cnt; c++) {
+                const int jn = c + 1 < cnt ? __ldg(col + ((size_t)(c + 1) << 5)) : 0;
                 float4 a, b;
                 ld_rec(R, j, a, b);
                 const float dx = pi.x - a.x, dy = pi.y - a.y, dz = pi.z - a.z;
                 const float r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
-            };
-#pragma unroll 1
-            for (int c = 0; c < cnt; c += 4) {
-                const int4 q = __ldg(row + (c >> 2));
-                one(q.x);
-                if (c + 1 < cnt) one(q.y);
-                if (c + 2 < cnt) one(q.z);
-                if (c + 3 < cnt) one(q.w);
+                j = jn;
             }
             return;
         }
@@ -157,8 +161,8 @@ __device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho 
 
 // Neighbour-list build: every boundary particle keeps its fluid neighbours (all that pass 1
 // needs), every fluid particle all of them; with walls_all, boundary particles keep all.
-// Rows are particle-major (row i = idx + i * cap) and written as 16-byte vectors of four
-// slots, buffered in registers, so a warp store moves 512 B instead of 128 B.
+// Slots are warp-interleaved (nbr_col): the passes read them coalesced, the build writes them
+// scattered within its warp's block, which L2 merges before they reach HBM.
 __global__ void __launch_bounds__(NS_THREADS)
 k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict__ keys,
             const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err,
@@ -170,22 +174,15 @@ k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict_
     if (nl.xb) nl.xb[i] = pi;
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     int cnt = 0;
-    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-    int4* __restrict__ row = reinterpret_cast<int4*>(nl.idx + (size_t)i * (size_t)nl.cap);
+    int* __restrict__ col = nl.idx + nbr_col(nl, i);
     const int cap = nl.cap;
     walk_pairs<1>(k, cs, keys, X, i, pi, k.kh2_list,
                   [&](int j, const float4& pj, float, float, float, float) {
         if (keep_all || fluid_rec(pj.w)) {
-            const int slot = cnt & 3;
-            b0 = slot == 0 ? j : b0;
-            b1 = slot == 1 ? j : b1;
-            b2 = slot == 2 ? j : b2;
-            b3 = slot == 3 ? j : b3;
+            if (cnt < cap) col[(size_t)cnt << 5] = j;
             cnt++;
-            if (slot == 3 && cnt <= cap) row[(cnt >> 2) - 1] = make_int4(b0, b1, b2, b3);
         }
     });
-    if ((cnt & 3) && cnt < cap) row[cnt >> 2] = make_int4(b0, b1, b2, b3);
     nl.count[i] = cnt;
     raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }

@@ -62,6 +62,9 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // The list holds every pair closer than the list cutoff (KParams::kh2_list, the support
 // radius plus a skin); xb (may be NULL) receives each slot's position when the list is built,
 // from which the integrator tracks how far particles have moved since.
+// Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + c * 32 + i % 32] (each warp
+// of 32 consecutive particles owns a block of cap x 32 slots), count[i] entries, and xb[i]
+// the position i had when the list was built.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;

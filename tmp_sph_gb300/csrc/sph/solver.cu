@@ -208,7 +208,7 @@ cudaError_t force_rebuild(sph_ctx* c, cudaStream_t s) {
 }
 
 cudaError_t alloc_list(sph_ctx* c) {
-    // the option is rounded up to a multiple of 16 so rows stay 16-byte aligned
+    // the option is rounded up to a multiple of 16, like the derived capacity
     const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
                                        : nbr_capacity_for(c->P, c->skin);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
@@ -216,7 +216,9 @@ cudaError_t alloc_list(sph_ctx* c) {
     cudaFree(c->nl.count);
     cudaFree(c->nl.xb);
     c->nl = NbrList{};
-    cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * (size_t)(c->capacity > 0 ? c->capacity : 1));
+    // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
+    const size_t rows = ((size_t)(c->capacity > 0 ? c->capacity : 1) + 31) & ~(size_t)31;
+    cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * rows);
     if (e == cudaSuccess) e = dalloc(&c->nl.count, c->capacity);
     if (e == cudaSuccess) e = dalloc(&c->nl.xb, c->capacity);
     if (e != cudaSuccess) {

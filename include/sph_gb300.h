@@ -23,8 +23,9 @@
  *     order and advances whole predictor-corrector steps with fused kernels; optionally
  *     replays each step as a CUDA graph.  This is the fast path; its physics is the same.
  *
- * No function here allocates device memory except sph_create (everything a context needs) and
- * sph_set_params (only when the new grid has more cells than the context was built for).
+ * No function here allocates device memory except sph_create (everything a context needs),
+ * and sph_set_params / sph_ctx_set_option when a new grid or list needs more room than the
+ * context holds.
  * All functions are host functions; none is thread-safe on the same sph_ctx.
  */
 #ifndef SPH_GB300_H
@@ -239,6 +240,11 @@ typedef struct sph_ctx sph_ctx;
                                     some particle has moved more than skin/2 since the last
                                     build (decided on the GPU each half step); 0 rebuilds every
                                     half step as the reference does */
+#define SPH_OPT_CONDITIONAL_GRAPH 7  /* 1 (default): the replayed step graph holds the rebuild
+                                    kernels under conditional nodes, so a half step that keeps
+                                    its lists launches none of them; 0: they are launched and
+                                    return at once (also the fallback when the driver refuses
+                                    conditional nodes) */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
  * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;

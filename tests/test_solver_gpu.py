@@ -63,7 +63,11 @@ def test_steps_match_oracle(sphlib, oracle, cuda, report, physics):
             (nsteps, e)
         if nsteps == 1:
             ulp = np.spacing(np.abs(ref["pos"]).astype(np.float32))
-            assert (np.abs(out["pos"] - ref["pos"]) <= ulp).all()
+            dist = np.abs(out["pos"] - ref["pos"]) / ulp
+            w = np.unravel_index(np.argmax(dist), dist.shape)
+            report(f"solver {physics} 1 step max position difference in ulp", dist.max(), 2.0)
+            assert dist.max() <= 2.0, (w, out["pos"][w[0]], ref["pos"][w[0]], st["pos"][w[0]],
+                                       out["vel"][w[0]], ref["vel"][w[0]], st["type"][w[0]])
         wl = st["type"] != 1
         assert np.array_equal(out["pos"][wl], st["pos"][wl])
         assert np.array_equal(out["type"], st["type"])
@@ -71,12 +75,18 @@ def test_steps_match_oracle(sphlib, oracle, cuda, report, physics):
 
 
 def test_graph_replay_is_bitwise_identical(sphlib, cuda):
-    from tmp_sph_gb300 import cases
+    """Graph replay (rebuild kernels under conditional nodes, or gated) and plain launches give
+    the same bits, with list rebuilds forced by fast flow as well as skipped."""
+    from tmp_sph_gb300 import api, cases
+    from gpu_util import perturbed
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    a, _ = run_gpu(st, p, 7, graph=True)
-    b, _ = run_gpu(st, p, 7, graph=False)
-    for k in ("pos", "vel", "rho", "p", "type"):
-        assert np.array_equal(a[k], b[k]), k
+    for s in (st, perturbed(st, vamp=2.0, ramp=0.0)):
+        a, _ = run_gpu(s, p, 7, graph=True)
+        b, _ = run_gpu(s, p, 7, graph=False)
+        c, _ = run_opts(s, p, 7, {api.SPH_OPT_CONDITIONAL_GRAPH: 0})
+        for k in ("pos", "vel", "rho", "p", "type"):
+            assert np.array_equal(a[k], b[k]), k
+            assert np.array_equal(a[k], c[k]), k
 
 
 def run_opts(st, p, nsteps, opts):

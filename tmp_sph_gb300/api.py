@@ -39,6 +39,7 @@ SPH_OPT_PROFILE = 3
 SPH_OPT_NEIGHBOR_LIST = 4
 SPH_OPT_NEIGHBOR_CAP = 5
 SPH_OPT_SKIN_PERMILLE = 6
+SPH_OPT_CONDITIONAL_GRAPH = 7
 SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
 SPH_PHASE_COUNT = 5
 PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")

@@ -65,11 +65,15 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + c * 32 + i % 32] (each warp
 // of 32 consecutive particles owns a block of cap x 32 slots), count[i] entries, and xb[i]
 // the position i had when the list was built.
+// mask: one bit per slot, whether it is inside the support radius at the current positions
+// (written by pass 1, read by pass 2), interleaved the same way in words of 32 slots.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
     int cap = 0;
     float4* xb = nullptr;
+    unsigned* mask = nullptr;
+    int mask_words = 0;
 };
 // List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
 int nbr_capacity_for(const sph_params& p, double skin = 0.0);
@@ -163,9 +167,12 @@ struct sph_ctx {
     int opt_profile = 0;
     int opt_nbr_list = 1;
     int opt_nbr_cap = 0;  // 0: nbr_capacity_for(P)
+    int opt_cond_graph = 1;  // graph replay skips the rebuild kernels through conditional nodes
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;
+    bool graph_conditional = false;  // rebuild kernels under conditional nodes
+    cudaStream_t side_stream = nullptr;  // captures the conditional bodies
     // profiling events (PH_COUNT + 1 per half step) / accumulated milliseconds per phase
     cudaEvent_t ev[2 * (sph::PH_COUNT + 1)] = {};
     double phase_ms[sph::PH_COUNT] = {};

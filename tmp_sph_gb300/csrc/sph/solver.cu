@@ -65,13 +65,15 @@ void drop_graph(sph_ctx* c) {
 
 void release(sph_ctx* c) {
     drop_graph(c);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
+    c->side_stream = nullptr;
     free_set(c->x);
     free_set(c->y);
     cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm);
     cudaFree(c->p1.nrec); cudaFree(c->p1.self);
     c->p1 = Pass1Out{};
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
-    cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb);
+    cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb); cudaFree(c->nl.mask);
     c->nl = NbrList{};
     cudaFree(c->rb);
     c->rb = nullptr;
@@ -147,7 +149,10 @@ KParams resident_kparams(const sph_ctx* c) {
 // Rebuild decision, one thread: rebuild when forced, when the cells are walked every half
 // step (no list), or when some fluid particle has moved farther than skin/2 from where it was
 // at the last build (rb[1] holds the largest squared displacement as float bits).
-__global__ void k_decide(unsigned* rb, unsigned threshold_bits, int always) {
+// In a graph built with conditional nodes it also sets the condition of the node that holds
+// the rebuild kernels, so a half step without a rebuild launches none of them.
+__global__ void k_decide(unsigned* rb, unsigned threshold_bits, int always,
+                         cudaGraphConditionalHandle cond, int set_cond) {
     const bool rebuild = always || rb[2] != 0u || rb[1] > threshold_bits;
     rb[0] = rebuild ? 1u : 0u;
     if (rebuild) {
@@ -155,21 +160,22 @@ __global__ void k_decide(unsigned* rb, unsigned threshold_bits, int always) {
         rb[2] = 0u;
         rb[3] += 1u;
     }
+    if (set_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
 }
 
-// One half step (see the file comment).  `ev` (may be NULL) receives PH_COUNT + 1 timestamps.
-cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev) {
-    const KParams k = resident_kparams(c);
+// Conditional-node capture of a half step: the rebuild kernels go into the body of an IF node
+// (captured on `side`), whose condition k_decide sets.
+struct CondCapture {
+    cudaStream_t side;
+    cudaGraphConditionalHandle handle;
+};
+
+// Sort, gather, cell starts and list build, each kernel gated on rb[0].  `ev` as half_step.
+cudaError_t rebuild_lists(sph_ctx* c, const KParams& k, cudaStream_t s, cudaEvent_t* ev) {
     const int bits = key_bits_for(c->Pi.num_cells);
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
-    const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
-    const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
-    unsigned thr_bits;
-    memcpy(&thr_bits, &thr, sizeof(thr_bits));
     cudaError_t e;
-    if (ev) cudaEventRecord(ev[PH_SORT], s);
-    k_decide<<<1, 1, 0, s>>>(c->rb, thr_bits, nl ? 0 : 1);
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
                          c->sort_scratch_bytes, c->err, s, gate);
     if (e != cudaSuccess) return e;
@@ -184,6 +190,55 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s,
                                     gate)) != cudaSuccess)
         return e;
+    return cudaSuccess;
+}
+
+// Adds an IF node (condition cc.handle) after the current capture dependencies of `s` and
+// captures the rebuild kernels into its body on cc.side.
+cudaError_t capture_conditional_rebuild(sph_ctx* c, const KParams& k, cudaStream_t s,
+                                        const CondCapture& cc) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    if (st != cudaStreamCaptureStatusActive) return cudaErrorStreamCaptureInvalidated;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cc.handle;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp)) != cudaSuccess) return e;
+    if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                                 cudaStreamSetCaptureDependencies)) != cudaSuccess)
+        return e;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(cc.side, body, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return e;
+    e = rebuild_lists(c, k, cc.side, nullptr);
+    cudaGraph_t out = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cc.side, &out);
+    return e != cudaSuccess ? e : e2;
+}
+
+// One half step (see the file comment).  `ev` (may be NULL) receives PH_COUNT + 1 timestamps;
+// `cc` (may be NULL) puts the rebuild kernels under a conditional node of the capture.
+cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev,
+                      const CondCapture* cc = nullptr) {
+    const KParams k = resident_kparams(c);
+    const NbrList* nl = list_for(c);
+    const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
+    const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
+    unsigned thr_bits;
+    memcpy(&thr_bits, &thr, sizeof(thr_bits));
+    cudaError_t e;
+    if (ev) cudaEventRecord(ev[PH_SORT], s);
+    k_decide<<<1, 1, 0, s>>>(c->rb, thr_bits, nl ? 0 : 1, cc ? cc->handle : 0, cc ? 1 : 0);
+    e = cc ? capture_conditional_rebuild(c, k, s, *cc) : rebuild_lists(c, k, s, ev);
+    if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
     if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, nullptr, nullptr,
                           s)) != cudaSuccess)
@@ -196,10 +251,39 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     return e;
 }
 
-cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev) {
-    cudaError_t e = half_step(c, HALF_PREDICT, s, ev);
+cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev,
+                      const CondCapture* cc = nullptr) {
+    cudaError_t e = half_step(c, HALF_PREDICT, s, ev, cc);
     if (e != cudaSuccess) return e;
-    return half_step(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr);
+    return half_step(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr, cc ? cc + 1 : nullptr);
+}
+
+// The step graph with the rebuild kernels under two conditional nodes (one per half step).
+cudaError_t build_conditional_graph(sph_ctx* c, cudaStream_t s, cudaGraph_t* out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    CondCapture cc[2];
+    for (int h = 0; h < 2 && e == cudaSuccess; h++) {
+        cc[h].side = c->side_stream;
+        e = cudaGraphConditionalHandleCreate(&cc[h].handle, g, 1u, cudaGraphCondAssignDefault);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = full_step(c, s, nullptr, cc);
+        cudaGraph_t g2 = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(s, &g2);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        return e;
+    }
+    *out = g;
+    return cudaSuccess;
 }
 
 // Next half step rebuilds the cell and neighbour lists whatever the displacement.
@@ -207,28 +291,33 @@ cudaError_t force_rebuild(sph_ctx* c, cudaStream_t s) {
     return cudaMemsetAsync(c->rb + 2, 1, sizeof(unsigned), s);
 }
 
+void free_list(NbrList& nl) {
+    cudaFree(nl.idx);
+    cudaFree(nl.count);
+    cudaFree(nl.xb);
+    cudaFree(nl.mask);
+    nl = NbrList{};
+}
+
 cudaError_t alloc_list(sph_ctx* c) {
     // the option is rounded up to a multiple of 16, like the derived capacity
     const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
                                        : nbr_capacity_for(c->P, c->skin);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
-    cudaFree(c->nl.idx);
-    cudaFree(c->nl.count);
-    cudaFree(c->nl.xb);
-    c->nl = NbrList{};
+    free_list(c->nl);
     // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
     const size_t rows = ((size_t)(c->capacity > 0 ? c->capacity : 1) + 31) & ~(size_t)31;
+    const int words = (cap + 31) / 32;
     cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * rows);
     if (e == cudaSuccess) e = dalloc(&c->nl.count, c->capacity);
     if (e == cudaSuccess) e = dalloc(&c->nl.xb, c->capacity);
+    if (e == cudaSuccess) e = dalloc(&c->nl.mask, (size_t)words * rows);
     if (e != cudaSuccess) {
-        cudaFree(c->nl.idx);
-        cudaFree(c->nl.count);
-        cudaFree(c->nl.xb);
-        c->nl = NbrList{};
+        free_list(c->nl);
         return e;
     }
     c->nl.cap = cap;
+    c->nl.mask_words = words;
     return cudaSuccess;
 }
 
@@ -261,6 +350,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = dalloc(&c->rb, 4);
     if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = alloc_list(c);
     for (auto& ev : c->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
@@ -323,6 +413,10 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
     if (!c) return SPH_ERR_ARG;
     switch (option) {
         case SPH_OPT_USE_GRAPH: c->opt_use_graph = value != 0; drop_graph(c); return SPH_OK;
+        case SPH_OPT_CONDITIONAL_GRAPH:
+            c->opt_cond_graph = value != 0;
+            drop_graph(c);
+            return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_PROFILE: c->opt_profile = value != 0; return SPH_OK;
         case SPH_OPT_NEIGHBOR_LIST:
@@ -466,20 +560,33 @@ extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
     if (!c->graph || c->graph_stream != s || c->graph_n != c->n) {
         drop_graph(c);
         cudaGraph_t g = nullptr;
-        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-            return SPH_ERR_CUDA;
-        cudaError_t e = full_step(c, s, nullptr);
-        cudaError_t e2 = cudaStreamEndCapture(s, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            cudaGetLastError();
-            return SPH_ERR_CUDA;
+        // rebuild kernels under conditional nodes when the driver takes them, else gated
+        if (c->opt_cond_graph && c->side_stream && build_conditional_graph(c, s, &g) == cudaSuccess) {
+            if (cudaGraphInstantiate(&c->graph, g, 0) != cudaSuccess) {
+                c->graph = nullptr;
+                cudaGetLastError();
+            }
+            cudaGraphDestroy(g);
+            g = nullptr;
         }
-        e = cudaGraphInstantiate(&c->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            c->graph = nullptr;
-            return SPH_ERR_CUDA;
+        c->graph_conditional = c->graph != nullptr;
+        if (!c->graph) {
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return SPH_ERR_CUDA;
+            cudaError_t e = full_step(c, s, nullptr);
+            cudaError_t e2 = cudaStreamEndCapture(s, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return SPH_ERR_CUDA;
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&c->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                c->graph = nullptr;
+                cudaGetLastError();
+                return SPH_ERR_CUDA;
+            }
         }
         c->graph_stream = s;
         c->graph_n = c->n;

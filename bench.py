@@ -155,17 +155,20 @@ def build_case(name: str):
     return cases.build(name, physics="config")
 
 
-def launches_per_step(p) -> int:
-    from tmp_sph_gb300 import api  # noqa: F401
+def count_launches(num_cells: int, half_steps: int, rebuilds: int, mode: str) -> int:
+    """Kernels launched over `half_steps` half steps with `rebuilds` list rebuilds."""
     bits = 1
-    while bits < 31 and (1 << bits) < p.num_cells:
+    while bits < 31 and (1 << bits) < num_cells:
         bits += 1
     passes = (bits + 7) // 8
-    # per half step, all launched whether or not the lists are rebuilt (gated kernels return
-    # at once when they are not): rebuild decision, sort-totals clear, 3 kernels per radix
-    # pass, gather + copy back, cell-start clear, mark and fill, neighbour-list build,
-    # pass 1, pass 2
-    return 2 * (3 * passes + 10)
+    # every half step: rebuild decision, pass 1, pass 2; a rebuild adds the sort-totals
+    # clear, 3 kernels per radix pass, gather + copy back, cell-start clear, mark and fill,
+    # and the neighbour-list build.  In gated mode the rebuild kernels are launched every
+    # half step (and return at once when the lists are kept).
+    rebuild_kernels = 3 * passes + 7
+    if mode == "gated":
+        return half_steps * (3 + rebuild_kernels)
+    return 3 * half_steps + rebuilds * rebuild_kernels
 
 
 def cpu_baseline(st, p, budget_s: float = 20.0) -> dict:
@@ -229,7 +232,8 @@ def config_block(args, p, n):
             "cells": p.num_cells, "eos": "tait", "dt_s": p.dt,
             "parallelism": f"replicas x{dist_env()[0]}",
             "l2": "state larger than L2 (no flush needed)",
-            "neighbour_list_skin_over_kh": args.skin / 1000.0}
+            "neighbour_list_skin_over_kh": args.skin / 1000.0,
+            "graph_mode": args.graph_mode}
 
 
 def main():
@@ -242,6 +246,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
+                    help="rebuild kernels of the step graph under conditional nodes, or launched "
+                         "every half step and returning at once when the lists are kept")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -263,6 +270,7 @@ def main():
     stream = torch.cuda.Stream()
     sol = S.Solver(p, n)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+    sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
 
     def barrier():
@@ -274,6 +282,7 @@ def main():
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     rebuilds0 = sol.rebuild_count(stream=stream)
+    sol_cells = sol.sorted_view()[3]
     with ClockSampler(gpu_uuid(local)) as clk:
         barrier()
         torch.cuda.synchronize()
@@ -373,7 +382,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
-        "gpu_launches": launches_per_step(p) * args.steps,
+        "gpu_launches": count_launches(sol_cells, 2 * args.steps, rebuilds, args.graph_mode),
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
                           "skin_permille": args.skin},
         "rebuild_every_half_step": no_reuse,

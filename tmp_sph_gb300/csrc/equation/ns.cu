@@ -121,21 +121,12 @@ __device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
     return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + (size_t)(i & 31);
 }
 
-// Hit mask of the list: bit c % 32 of word mask[mask_col + 32 (c / 32)] says whether slot c of
-// particle i lies inside the support radius at the current positions.  Pass 1 writes it, pass 2
-// (same positions) reads it and skips the record gather of the slots in the skin.
-__device__ __forceinline__ size_t mask_col(const NbrList& nl, int i) {
-    return (size_t)(i >> 5) * ((size_t)nl.mask_words << 5) + (size_t)(i & 31);
-}
-
-enum { MASK_NONE = 0, MASK_WRITE = 1, MASK_READ = 2 };
-
 // Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one 256-bit
 // record load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond
 // the support radius are skipped), or by walking the cells over X[XSTRIDE * j] when i
-// overflowed the list.  f(j, a, b, dx, dy, dz, r2).  MASK_WRITE records which slots were hits,
-// MASK_READ gathers only those.
-template <bool LIST, int XSTRIDE, int MASK = MASK_NONE, class F>
+// overflowed the list.  f(j, a, b, dx, dy, dz, r2).  (Skipping the gathers of slots in the skin
+// with a pass-1 hit mask cost pass 2 more in instructions than it saved in sectors.)
+template <bool LIST, int XSTRIDE, class F>
 __device__ __forceinline__ void visit_records(const KParams& k, const int* __restrict__ cs,
                                               const unsigned* __restrict__ keys,
                                               const NbrList& nl, const float4* __restrict__ X,
@@ -145,32 +136,15 @@ __device__ __forceinline__ void visit_records(const KParams& k, const int* __res
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             const int* __restrict__ col = nl.idx + nbr_col(nl, i);
-            unsigned* __restrict__ mcol = MASK != MASK_NONE ? nl.mask + mask_col(nl, i) : nullptr;
             int j = cnt > 0 ? __ldg(col) : 0;
-            unsigned bits = 0u;
 #pragma unroll 1
             for (int c = 0; c < cnt; c++) {
                 const int jn = c + 1 < cnt ? __ldg(col + ((size_t)(c + 1) << 5)) : 0;
-                if (MASK == MASK_READ) {
-                    if ((c & 31) == 0) bits = __ldg(mcol + ((size_t)(c >> 5) << 5));
-                    if (!((bits >> (c & 31)) & 1u)) {
-                        j = jn;
-                        continue;
-                    }
-                }
                 float4 a, b;
                 ld_rec(R, j, a, b);
                 const float dx = pi.x - a.x, dy = pi.y - a.y, dz = pi.z - a.z;
                 const float r2 = dist2(dx, dy, dz);
-                const bool hit = r2 < k.kh2;
-                if (MASK == MASK_WRITE) {
-                    bits |= (unsigned)hit << (c & 31);
-                    if ((c & 31) == 31 || c + 1 == cnt) {
-                        mcol[(size_t)(c >> 5) << 5] = bits;
-                        bits = 0u;
-                    }
-                }
-                if (hit) f(j, a, b, dx, dy, dz, r2);
+                if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
                 j = jn;
             }
             return;
@@ -229,7 +203,7 @@ k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
     const float4 vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
     const bool fi = fluid_rec(vi.w);
     float dofv = 0.f, rs = 0.f, ws = 0.f;
-    visit_records<LIST, 1, MASK_WRITE>(k, cs, keys, nl, in.xyz, R, i, pi,
+    visit_records<LIST, 1>(k, cs, keys, nl, in.xyz, R, i, pi,
                         [&](int, const float4& aj, const float4& vj, float dx, float dy, float dz,
                             float r2) {
         if (!fluid_rec(vj.w)) return;
@@ -294,7 +268,7 @@ __device__ __forceinline__ float pass2_one(const KParams& k, int i, const Partic
     if (fi || (MODE == MODE_RATES && wall_rates)) {
         const float damp_i = k.damper * dofvi;
         // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour
-        visit_records<LIST, 2, MASK_READ>(k, cs, keys, nl, NR, NR, i, pi,
+        visit_records<LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
                             [&](int j, const float4& aj, const float4& vj, float dx, float dy,
                                 float dz, float r2) {
             const bool fj = fluid_rec(vj.w);

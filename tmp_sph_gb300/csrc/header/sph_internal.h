@@ -65,15 +65,11 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + c * 32 + i % 32] (each warp
 // of 32 consecutive particles owns a block of cap x 32 slots), count[i] entries, and xb[i]
 // the position i had when the list was built.
-// mask: one bit per slot, whether it is inside the support radius at the current positions
-// (written by pass 1, read by pass 2), interleaved the same way in words of 32 slots.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
     int cap = 0;
     float4* xb = nullptr;
-    unsigned* mask = nullptr;
-    int mask_words = 0;
 };
 // List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
 int nbr_capacity_for(const sph_params& p, double skin = 0.0);

@@ -73,7 +73,7 @@ void release(sph_ctx* c) {
     cudaFree(c->p1.nrec); cudaFree(c->p1.self);
     c->p1 = Pass1Out{};
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
-    cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb); cudaFree(c->nl.mask);
+    cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb);
     c->nl = NbrList{};
     cudaFree(c->rb);
     c->rb = nullptr;
@@ -295,7 +295,6 @@ void free_list(NbrList& nl) {
     cudaFree(nl.idx);
     cudaFree(nl.count);
     cudaFree(nl.xb);
-    cudaFree(nl.mask);
     nl = NbrList{};
 }
 
@@ -307,17 +306,14 @@ cudaError_t alloc_list(sph_ctx* c) {
     free_list(c->nl);
     // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
     const size_t rows = ((size_t)(c->capacity > 0 ? c->capacity : 1) + 31) & ~(size_t)31;
-    const int words = (cap + 31) / 32;
     cudaError_t e = dalloc(&c->nl.idx, (size_t)cap * rows);
     if (e == cudaSuccess) e = dalloc(&c->nl.count, c->capacity);
     if (e == cudaSuccess) e = dalloc(&c->nl.xb, c->capacity);
-    if (e == cudaSuccess) e = dalloc(&c->nl.mask, (size_t)words * rows);
     if (e != cudaSuccess) {
         free_list(c->nl);
         return e;
     }
     c->nl.cap = cap;
-    c->nl.mask_words = words;
     return cudaSuccess;
 }
 

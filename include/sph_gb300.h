@@ -245,6 +245,15 @@ typedef struct sph_ctx sph_ctx;
                                     its lists launches none of them; 0: they are launched and
                                     return at once (also the fallback when the driver refuses
                                     conditional nodes) */
+#define SPH_OPT_PRECISION     8  /* SPH_PREC_* below; set before sph_upload (the state is
+                                    reallocated; the uploaded state is dropped) */
+
+/* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
+#define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */
+#define SPH_PREC_FP64  1  /* FP64 state and arithmetic: the accuracy reference for the others */
+#define SPH_PREC_MIXED 2  /* FP32 neighbour sums on relative positions rebuilt from cell-local
+                             offsets, compensated density and force sums; FP64 positions and
+                             density perturbation (rho - rho0) for the time integration */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
  * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;
@@ -277,6 +286,11 @@ int sph_upload(sph_ctx* ctx, const float* pos, const float* vel, const float* rh
 /* Write the current state back in original order; any pointer may be NULL. */
 int sph_download(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
                  int to_host, void* stream);
+/* The same in double (no reference counterpart): FP64 positions and density of the FP64 and
+ * mixed-precision solvers without rounding to float, FP32 values widened otherwise.  For
+ * accuracy studies against an FP64 run. */
+int sph_download_f64(sph_ctx* ctx, double* pos, double* vel, double* rho, double* p,
+                     int to_host, void* stream);
 /* Advance nsteps full predictor-corrector steps (two cell-list builds, four neighbour passes
  * per step), asynchronously on `stream`. */
 int sph_step(sph_ctx* ctx, int nsteps, void* stream);

@@ -40,6 +40,9 @@ SPH_OPT_NEIGHBOR_LIST = 4
 SPH_OPT_NEIGHBOR_CAP = 5
 SPH_OPT_SKIN_PERMILLE = 6
 SPH_OPT_CONDITIONAL_GRAPH = 7
+SPH_OPT_PRECISION = 8
+SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED = 0, 1, 2
+PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED}
 SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
 SPH_PHASE_COUNT = 5
 PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")
@@ -139,6 +142,7 @@ _PROTOS = {
     "sph_ns": (_I, [_P] + [_P] * 9 + [_I] + [_P] * 4 + [_P]),
     "sph_upload": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_download": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
+    "sph_download_f64": (_I, [_P, _P, _P, _P, _P, _I, _P]),
     "sph_step": (_I, [_P, _I, _P]),
     "sph_step_host": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I)]),

@@ -4,14 +4,15 @@
 // computeBoundary_Delta_acoustic_D (pass 1, src/equation/ns.cu:30-131) and
 // computeGovering_equationD (pass 2, src/equation/ns.cu:134-249).
 //
-// Layout.  Particles are in cell-sorted order; each is one 32-byte record of two float4,
+// Layout.  Particles are in cell-sorted order; each is one record of two vec4,
 // rec[2i] = (x, y, z, p) and rec[2i+1] = (vx, vy, vz, ±rho) with the sign of rho marking a
 // fluid (+) or boundary (-) particle, so everything a neighbour contributes to pass 1 is one
-// aligned 32-byte sector.  Pass 1 writes the record pass 2 gathers, nrec[2i] = (x, y, z, q),
-// nrec[2i+1] = (vx, vy, vz, ±rho'), where q = p' - rho0 cs h dofv: the acoustic-damper term of a
-// fluid-fluid pair, rho0 cs h (dofv_i + dofv_j), splits into an i part and a j part, and the j
-// part is folded into the neighbour's pressure (boundary particles have dofv = 0, so q = p').
-// It also writes self[i] = (p', rho', dofv, 0) for the particle's own side.
+// aligned 32-byte sector in FP32.  Pass 1 writes the record pass 2 gathers, nrec[2i] =
+// (x, y, z, q), nrec[2i+1] = (vx, vy, vz, ±rho'), where q = p' - rho0 cs h dofv: the
+// acoustic-damper term of a fluid-fluid pair, rho0 cs h (dofv_i + dofv_j), splits into an i part
+// and a j part, and the j part is folded into the neighbour's pressure (boundary particles
+// have dofv = 0, so q = p').  It also writes self[i] = (p', rho', dofv, 0) for the particle's
+// own side.
 //
 // Cells are walked as nine x-strips: the three cells (x-1 .. x+1) of one (y, z) row are
 // consecutive in the sorted order, so each strip is one contiguous slot range
@@ -34,6 +35,14 @@
 // passes still test r < kh on the current positions, and k_nbr_build keeps the build
 // positions (xb) that pass 2 measures each particle's displacement against.
 //
+// Precision.  Every kernel is instantiated for the three policies of sph_internal.h: FP32
+// (records of float4), FP64 (records of two 32-byte double vectors) and mixed.  The mixed
+// policy stores positions as FP32 offsets from the origin of the particle's cell at the last
+// list build; a pair's relative position is (o_i - o_j) - (c_j - c_i) cell, exact to a few
+// ulp of the cell size instead of a few ulp of the domain size, with c_j - c_i stored in the
+// list slot (or known to the cell walk).  Its sums use compensated (Neumaier) accumulation,
+// and its integrator advances FP64 positions and the FP64 density perturbation rho - rho0.
+//
 // Kernel algebra (same quantities as the reference, simplified): with r = x_i - x_j,
 // q = |r|/h, t = 1 - q/2, the Wendland C2 gradient is grad W = c_fr t^3 r with
 // c_fr = -5 adh / h^2, which is the reference's per-component expression
@@ -47,24 +56,53 @@ namespace sph {
 namespace {
 
 constexpr int NS_THREADS = 128;
-
-__device__ __forceinline__ void cell_of_key(const KParams& k, unsigned key, int& cx, int& cy,
-                                            int& cz) {
-    unsigned t = key / (unsigned)k.gx;
-    cx = (int)(key - t * (unsigned)k.gx);
-    cz = (int)(t / (unsigned)k.gy);
-    cy = (int)(t - (unsigned)cz * (unsigned)k.gy);
-}
+// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^27).
+constexpr int CODE_SHIFT = 27;
+constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
 
 // Squared distance with an explicit rounding sequence, so the in-range test gives the same
 // answer in the list build, in the walking passes and in the list passes.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
+__device__ __forceinline__ double dist2(double dx, double dy, double dz) {
+    return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+}
+__device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float dabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double dabs(double x) { return fabs(x); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
-// Visit every candidate slot j of the 27 cells around (cx, cy, cz), strip by strip.
-template <class F>
-__device__ __forceinline__ void for_each_candidate(const KParams& k, const int* __restrict__ cs,
+// A neighbour sum: plain, or compensated (Neumaier) when COMP.  The compensated form uses
+// explicitly rounded adds so no contraction folds the error terms away.
+template <class T, bool COMP>
+struct Sum {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T v) {
+        if constexpr (COMP) {
+            const T t = add_rn(s, v);
+            c = add_rn(c, dabs(s) >= dabs(v) ? add_rn(sub_rn(s, t), v) : add_rn(sub_rn(v, t), s));
+            s = t;
+        } else {
+            s += v;
+        }
+    }
+    __device__ __forceinline__ T get() const {
+        if constexpr (COMP) return add_rn(s, c);
+        return s;
+    }
+};
+
+// Visit every candidate slot j of the 27 cells around (cx, cy, cz): f(j, code).  Without CODES
+// each x-strip is one range and code is 0; with CODES the strip's three cells are visited one
+// by one and code = (dz+1)*9 + (dy+1)*3 + (dx+1) is j's cell relative to (cx, cy, cz).  Both
+// visit the same slots in the same order.
+template <bool CODES, class KP, class F>
+__device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
                                                    int cx, int cy, int cz, F&& f) {
     const int xl = cx > 0 ? cx - 1 : 0;
     const int xh = cx < k.gx - 1 ? cx + 1 : k.gx - 1;
@@ -77,17 +115,26 @@ __device__ __forceinline__ void for_each_candidate(const KParams& k, const int* 
             const int y = cy + dy;
             if ((unsigned)y >= (unsigned)k.gy) continue;
             const int row = (z * k.gy + y) * k.gx;
-            const int j0 = max(__ldg(cs + row + xl), 0);
-            const int j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
+            if constexpr (CODES) {
+#pragma unroll 1
+                for (int xc = xl; xc <= xh; xc++) {
+                    const unsigned code = (unsigned)((dz + 1) * 9 + (dy + 1) * 3 + (xc - cx + 1));
+                    const int j0 = max(__ldg(cs + row + xc), 0);
+                    const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
+                    for (int j = j0; j < j1; j++) f(j, code);
+                }
+            } else {
+                const int j0 = max(__ldg(cs + row + xl), 0);
+                const int j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
 #pragma unroll 4
-            for (int j = j0; j < j1; j++) f(j);
+                for (int j = j0; j < j1; j++) f(j, 0u);
+            }
         }
     }
 }
 
-// One 32-byte record (two float4) in a single 256-bit read-only load: a neighbour gather
-// touches one L1 sector with one request.  R is 32-byte aligned (cudaMalloc'd, two float4 per
-// particle).
+// One record (two vec4) in single 256-bit read-only loads: a neighbour gather touches one L1
+// sector per 32 bytes with one request.  R is 32-byte aligned (cudaMalloc'd).
 __device__ __forceinline__ void ld_rec(const float4* __restrict__ R, int j, float4& a,
                                        float4& b) {
     const float4* p = R + 2 * (size_t)j;
@@ -95,22 +142,70 @@ __device__ __forceinline__ void ld_rec(const float4* __restrict__ R, int j, floa
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
         : "l"(p));
 }
+__device__ __forceinline__ void ld_rec(const dvec4* __restrict__ R, int j, dvec4& a, dvec4& b) {
+    const dvec4* p = R + 2 * (size_t)j;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(a.x), "=d"(a.y), "=d"(a.z), "=d"(a.w)
+        : "l"(p));
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(b.x), "=d"(b.y), "=d"(b.z), "=d"(b.w)
+        : "l"(p + 1));
+}
+__device__ __forceinline__ float4 ld_pos(const float4* __restrict__ X, size_t j) {
+    return __ldg(X + j);
+}
+__device__ __forceinline__ dvec4 ld_pos(const dvec4* __restrict__ X, size_t j) {
+    const dvec4* p = X + j;
+    dvec4 a;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(a.x), "=d"(a.y), "=d"(a.z), "=d"(a.w)
+        : "l"(p));
+    return a;
+}
+
+// Relative position r = x_i - x_j of a pair: from absolute positions, or (mixed precision)
+// from cell-local offsets and j's cell relative to i's.
+template <class P, class V>
+__device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const V& pi,
+                                        const V& pj, unsigned code, typename P::T& dx,
+                                        typename P::T& dy, typename P::T& dz) {
+    using T = typename P::T;
+    if constexpr (P::kMixed) {
+        const int rz = (int)(code / 9u) - 1;
+        const int rem = (int)(code % 9u);
+        const int ry = rem / 3 - 1;
+        const int rx = rem % 3 - 1;
+        dx = (pi.x - pj.x) - (T)rx * k.cell;
+        dy = (pi.y - pj.y) - (T)ry * k.cell;
+        dz = (pi.z - pj.z) - (T)rz * k.cell;
+    } else {
+        (void)k;
+        (void)code;
+        dx = pi.x - pj.x;
+        dy = pi.y - pj.y;
+        dz = pi.z - pj.z;
+    }
+}
 
 // Walk the cells of particle i over the positions X[STRIDE * j] and call
-// f(j, pj, dx, dy, dz, r2) for every j != i with r2 < cut2.  X is the dense (x, y, z, ±1) array
-// (STRIDE 1) or a record array (STRIDE 2).
-template <int STRIDE, class F>
-__device__ __forceinline__ void walk_pairs(const KParams& k, const int* __restrict__ cs,
+// f(j, code, pj, dx, dy, dz, r2) for every j != i with r2 < cut2.  X is the dense
+// (x, y, z, ±1) array (STRIDE 1) or a record array (STRIDE 2).
+template <class P, int STRIDE, class F>
+__device__ __forceinline__ void walk_pairs(const KParamsT<typename P::T>& k,
+                                           const int* __restrict__ cs,
                                            const unsigned* __restrict__ keys,
-                                           const float4* __restrict__ X, int i, const float4& pi,
-                                           float cut2, F&& f) {
+                                           const vec4_t<typename P::T>* __restrict__ X, int i,
+                                           const vec4_t<typename P::T>& pi, typename P::T cut2,
+                                           F&& f) {
+    using T = typename P::T;
     int cx, cy, cz;
-    cell_of_key(k, keys[i], cx, cy, cz);
-    for_each_candidate(k, cs, cx, cy, cz, [&](int j) {
-        const float4 pj = __ldg(X + (size_t)STRIDE * (size_t)j);
-        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-        const float r2 = dist2(dx, dy, dz);
-        if (r2 < cut2 && j != i) f(j, pj, dx, dy, dz, r2);
+    cell_of_key(k.gx, k.gy, keys[i], cx, cy, cz);
+    for_each_candidate<P::kMixed>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
+        const vec4_t<T> pj = ld_pos(X, (size_t)STRIDE * (size_t)j);
+        T dx, dy, dz;
+        rel_pos<P>(k, pi, pj, code, dx, dy, dz);
+        const T r2 = dist2(dx, dy, dz);
+        if (r2 < cut2 && j != i) f(j, code, pj, dx, dy, dz, r2);
     });
 }
 
@@ -121,66 +216,81 @@ __device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
     return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + (size_t)(i & 31);
 }
 
-// Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one 256-bit
-// record load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond
-// the support radius are skipped), or by walking the cells over X[XSTRIDE * j] when i
-// overflowed the list.  f(j, a, b, dx, dy, dz, r2).  (Skipping the gathers of slots in the skin
-// with a pass-1 hit mask cost pass 2 more in instructions than it saved in sectors.)
-template <bool LIST, int XSTRIDE, class F>
-__device__ __forceinline__ void visit_records(const KParams& k, const int* __restrict__ cs,
+// Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one record
+// load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond the
+// support radius are skipped), or by walking the cells over X[XSTRIDE * j] when i overflowed
+// the list.  f(j, a, b, dx, dy, dz, r2).  (Skipping the gathers of slots in the skin with a
+// pass-1 hit mask cost pass 2 more in instructions than it saved in sectors.)
+template <class P, bool LIST, int XSTRIDE, class F>
+__device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
+                                              const int* __restrict__ cs,
                                               const unsigned* __restrict__ keys,
-                                              const NbrList& nl, const float4* __restrict__ X,
-                                              const float4* __restrict__ R, int i,
-                                              const float4& pi, F&& f) {
+                                              const NbrList& nl,
+                                              const vec4_t<typename P::T>* __restrict__ X,
+                                              const vec4_t<typename P::T>* __restrict__ R, int i,
+                                              const vec4_t<typename P::T>& pi, F&& f) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
     if (LIST) {
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             const int* __restrict__ col = nl.idx + nbr_col(nl, i);
-            int j = cnt > 0 ? __ldg(col) : 0;
+            int e = cnt > 0 ? __ldg(col) : 0;
 #pragma unroll 1
             for (int c = 0; c < cnt; c++) {
-                const int jn = c + 1 < cnt ? __ldg(col + ((size_t)(c + 1) << 5)) : 0;
-                float4 a, b;
+                const int en = c + 1 < cnt ? __ldg(col + ((size_t)(c + 1) << 5)) : 0;
+                const int j = P::kMixed ? (int)((unsigned)e & IDX_MASK) : e;
+                V a, b;
                 ld_rec(R, j, a, b);
-                const float dx = pi.x - a.x, dy = pi.y - a.y, dz = pi.z - a.z;
-                const float r2 = dist2(dx, dy, dz);
+                T dx, dy, dz;
+                rel_pos<P>(k, pi, a, (unsigned)e >> CODE_SHIFT, dx, dy, dz);
+                const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
-                j = jn;
+                e = en;
             }
             return;
         }
     }
-    walk_pairs<XSTRIDE>(k, cs, keys, X, i, pi, k.kh2,
-                        [&](int j, const float4&, float dx, float dy, float dz, float r2) {
-        float4 a, b;
+    walk_pairs<P, XSTRIDE>(k, cs, keys, X, i, pi, k.kh2,
+                           [&](int j, unsigned, const V&, T dx, T dy, T dz, T r2) {
+        V a, b;
         ld_rec(R, j, a, b);
         f(j, a, b, dx, dy, dz, r2);
     });
 }
 
-__device__ __forceinline__ bool fluid_rec(float signed_rho) { return signed_rho > 0.f; }
+template <class T>
+__device__ __forceinline__ bool fluid_rec(T signed_rho) { return signed_rho > T(0); }
+
+// Position the list build records for the displacement test (offsets in mixed precision).
+__device__ __forceinline__ float4 as_float4(const float4& v) { return v; }
+__device__ __forceinline__ float4 as_float4(const dvec4& v) {
+    return make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+}
 
 // Neighbour-list build: every boundary particle keeps its fluid neighbours (all that pass 1
 // needs), every fluid particle all of them; with walls_all, boundary particles keep all.
 // Slots are warp-interleaved (nbr_col): the passes read them coalesced, the build writes them
 // scattered within its warp's block, which L2 merges before they reach HBM.
+template <class P>
 __global__ void __launch_bounds__(NS_THREADS)
-k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict__ keys,
-            const int* __restrict__ cs, NbrList nl, int walls_all, unsigned* err,
-            const unsigned* gate) {
+k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
+            const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+            int walls_all, unsigned* err, const unsigned* gate) {
+    using T = typename P::T;
     if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4 pi = X[i];
-    if (nl.xb) nl.xb[i] = pi;
+    const vec4_t<T> pi = X[i];
+    if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     int cnt = 0;
     int* __restrict__ col = nl.idx + nbr_col(nl, i);
     const int cap = nl.cap;
-    walk_pairs<1>(k, cs, keys, X, i, pi, k.kh2_list,
-                  [&](int j, const float4& pj, float, float, float, float) {
+    walk_pairs<P, 1>(k, cs, keys, X, i, pi, k.kh2_list,
+                     [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
         if (keep_all || fluid_rec(pj.w)) {
-            if (cnt < cap) col[(size_t)cnt << 5] = j;
+            if (cnt < cap) col[(size_t)cnt << 5] = P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j;
             cnt++;
         }
     });
@@ -191,52 +301,54 @@ k_nbr_build(KParams k, const float4* __restrict__ X, const unsigned* __restrict_
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
 // particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
 // neighbour record and the particle's own (p', rho', dofv).
-template <bool WRITE_SUMS, bool LIST>
+template <class P, bool WRITE_SUMS, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
-k_pass1(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, NbrList nl, Pass1Out out, float* __restrict__ rhop_sum,
-        float* __restrict__ w_sum) {
+k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+        const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+        Pass1OutT<typename P::T> out, float* __restrict__ rhop_sum, float* __restrict__ w_sum) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= k.n) return;
-    const float4* __restrict__ R = in.rec;
-    const float4 pi = R[2 * (size_t)i];      // x, y, z, p
-    const float4 vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
+    const V* __restrict__ R = in.rec;
+    const V pi = R[2 * (size_t)i];      // x, y, z, p
+    const V vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
     const bool fi = fluid_rec(vi.w);
-    float dofv = 0.f, rs = 0.f, ws = 0.f;
-    visit_records<LIST, 1>(k, cs, keys, nl, in.xyz, R, i, pi,
-                        [&](int, const float4& aj, const float4& vj, float dx, float dy, float dz,
-                            float r2) {
+    Sum<T, P::kMixed> dofv, rs, ws;
+    visit_records<P, LIST, 1>(k, cs, keys, nl, in.xyz, R, i, pi,
+                              [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
         if (!fluid_rec(vj.w)) return;
-        const float rr = sqrtf(r2);
-        const float q = rr * k.inv_h;
-        const float t = 1.f - 0.5f * q;
-        const float t2 = t * t;
+        const T rr = dsqrt(r2);
+        const T q = rr * k.inv_h;
+        const T t = T(1) - T(0.5) * q;
+        const T t2 = t * t;
         if (!fi) {
-            const float w = k.adh * t2 * t2 * (2.f * q + 1.f);
-            rs += (aj.w + vj.w * k.g * dz) * w;
-            ws += w;
+            const T w = k.adh * t2 * t2 * (T(2) * q + T(1));
+            rs.add((aj.w + vj.w * k.g * dz) * w);
+            ws.add(w);
         } else {
-            const float fr = k.c_fr * t2 * t;
-            const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            dofv -= fr * vdotr * (k.mass / vj.w);
+            const T fr = k.c_fr * t2 * t;
+            const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            dofv.add(-(fr * vdotr * (k.mass / vj.w)));
         }
     });
-    float p, rho;
+    T p, rho;
+    const T dv = dofv.get(), rsum = rs.get(), wsum = ws.get();
     if (fi) {
         p = pi.w;
         rho = vi.w;
     } else {
-        p = fabsf(ws) > 1.0e-8f ? rs / ws : 0.f;
-        if (p < 0.f) p = 0.f;
+        p = dabs(wsum) > T(1.0e-8) ? rsum / wsum : T(0);
+        if (p < T(0)) p = T(0);
         rho = eos_density(k, p);
     }
-    const float qv = fi ? p - k.damper * dofv : p;
-    out.nrec[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, qv);
-    out.nrec[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, fi ? rho : -rho);
-    out.self[i] = make_float4(p, rho, dofv, 0.f);
-    if (WRITE_SUMS) {
-        rhop_sum[i] = rs;
-        w_sum[i] = ws;
+    const T qv = fi ? p - k.damper * dv : p;
+    out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
+    out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
+    out.self[i] = make4<T>(p, rho, dv, T(0));
+    if constexpr (WRITE_SUMS) {
+        rhop_sum[i] = (float)rsum;
+        w_sum[i] = (float)wsum;
     }
 }
 
@@ -250,143 +362,216 @@ enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
 // `out` may alias `in`: the update touches only particle i's own rows, and neighbours (also
 // the positions of a cell walk) come from the pass-1 records.  Returns the squared distance
 // of particle i from its position when the neighbour list was built (0 without a list).
-template <int MODE, bool LIST>
-__device__ __forceinline__ float pass2_one(const KParams& k, int i, const ParticleSet& in,
+template <class P, int MODE, bool LIST>
+__device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int i,
+                                           const ParticleSetT<typename P::T>& in,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ cs, const NbrList& nl,
-                                           const Pass1Out& p1, float* __restrict__ rho_dt,
-                                           float* __restrict__ vel_dt, int wall_rates,
-                                           const ParticleSet& out,
+                                           const Pass1OutT<typename P::T>& p1,
+                                           float* __restrict__ rho_dt, float* __restrict__ vel_dt,
+                                           int wall_rates, const ParticleSetT<typename P::T>& out,
                                            unsigned* __restrict__ out_hash, unsigned* err) {
-    const float4* __restrict__ NR = p1.nrec;
-    const float4 pi = NR[2 * (size_t)i];
-    const float4 vi = NR[2 * (size_t)i + 1];
-    const float4 si = p1.self[i];  // p_i, rho_i, dofv_i
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const V* __restrict__ NR = p1.nrec;
+    const V pi = NR[2 * (size_t)i];
+    const V vi = NR[2 * (size_t)i + 1];
+    const V si = p1.self[i];  // p_i, rho_i, dofv_i
     const bool fi = fluid_rec(vi.w);
-    const float rhoi = si.y, presi = si.x, dofvi = si.z;
-    float drho = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+    const T rhoi = si.y, presi = si.x, dofvi = si.z;
+    T drho = T(0), ax = T(0), ay = T(0), az = T(0);
     if (fi || (MODE == MODE_RATES && wall_rates)) {
-        const float damp_i = k.damper * dofvi;
+        const T damp_i = k.damper * dofvi;
+        Sum<T, P::kMixed> sd, sx, sy, sz;
         // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour
-        visit_records<LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
-                            [&](int j, const float4& aj, const float4& vj, float dx, float dy,
-                                float dz, float r2) {
+        visit_records<P, LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
+                                  [&](int j, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
             const bool fj = fluid_rec(vj.w);
-            const float rhoj = fabsf(vj.w);
-            const float rr = sqrtf(r2);
-            const float q = rr * k.inv_h;
-            const float t = 1.f - 0.5f * q;
-            const float fr = k.c_fr * t * t * t;
-            const float vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            const float m_rhoj = k.mass / rhoj;
-            const float inv_r2e = 1.f / (r2 + k.eta2);
-            drho += m_rhoj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e);
-            float S;
+            const T rhoj = dabs(vj.w);
+            const T rr = dsqrt(r2);
+            const T q = rr * k.inv_h;
+            const T t = T(1) - T(0.5) * q;
+            const T fr = k.c_fr * t * t * t;
+            const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            const T m_rhoj = k.mass / rhoj;
+            const T inv_r2e = T(1) / (r2 + k.eta2);
+            sd.add(m_rhoj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
+            T S;
             if (fi) {
                 S = -presi - aj.w;
                 if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
             } else {
                 S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
             }
-            const float c = fr * S * m_rhoj;
-            ax += c * dx;
-            ay += c * dy;
-            az += c * dz;
+            const T c = fr * S * m_rhoj;
+            sx.add(c * dx);
+            sy.add(c * dy);
+            sz.add(c * dz);
         });
-        const float inv_rhoi = 1.f / rhoi;
-        ax *= inv_rhoi;
-        ay *= inv_rhoi;
-        az *= inv_rhoi;
+        drho = sd.get();
+        const T inv_rhoi = T(1) / rhoi;
+        ax = sx.get() * inv_rhoi;
+        ay = sy.get() * inv_rhoi;
+        az = sz.get() * inv_rhoi;
     }
     az += k.g;
 
-    if (MODE == MODE_RATES) {
+    if constexpr (MODE == MODE_RATES) {
         const bool have = fi || wall_rates;
-        rho_dt[i] = have ? drho : 0.f;
-        vel_dt[3 * i] = have ? ax : 0.f;
-        vel_dt[3 * i + 1] = have ? ay : 0.f;
-        vel_dt[3 * i + 2] = have ? az : 0.f;
+        rho_dt[i] = have ? (float)drho : 0.f;
+        vel_dt[3 * i] = have ? (float)ax : 0.f;
+        vel_dt[3 * i + 1] = have ? (float)ay : 0.f;
+        vel_dt[3 * i + 2] = have ? (float)az : 0.f;
         return 0.f;
-    }
-
-    float4 np = pi, nv;
-    float npres, nrho;
-    float4 tp, tv;
-    if (fi) {
-        if (escaped(k, pi.x, pi.y, pi.z)) {
-            np = make_float4(k.park_x, k.park_y, k.park_z, 0.f);
-            nv = make_float4(0.f, 0.f, 0.f, 0.f);
-            npres = 0.f;
-            nrho = k.rho0;
-            tp = make_float4(np.x, np.y, np.z, k.rho0);
-            tv = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else if (MODE == MODE_PRED) {
-            tp = make_float4(pi.x, pi.y, pi.z, rhoi);
-            tv = make_float4(vi.x, vi.y, vi.z, 0.f);
-            float rho = rhoi + drho * k.half_dt;
-            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-            np.x = pi.x + vi.x * k.half_dt;
-            np.y = pi.y + vi.y * k.half_dt;
-            np.z = pi.z + vi.z * k.half_dt;
-            nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt, 0.f);
-            nrho = rho;
-            npres = eos_pressure(k, rho);
+    } else if constexpr (P::kMixed) {
+        // FP64 position and density perturbation; FP32 velocity
+        const dvec4 xm = in.xm[i];
+        dvec4 nxm = xm, txm = xm;
+        float4 nv, tv;
+        float npres, nrho;
+        const double hdt = (double)k.half_dt;
+        if (fi) {
+            if (escaped(k, xm.x, xm.y, xm.z)) {
+                nxm = dvec4{(double)k.park_x, (double)k.park_y, (double)k.park_z, 0.0};
+                nv = make_float4(0.f, 0.f, 0.f, 0.f);
+                txm = nxm;
+                tv = nv;
+            } else if (MODE == MODE_PRED) {
+                tv = make_float4(vi.x, vi.y, vi.z, 0.f);
+                double d = xm.w + (double)drho * hdt;
+                if (k.clamp_density && d < 0.0) d = 0.0;
+                nxm.x = xm.x + (double)vi.x * hdt;
+                nxm.y = xm.y + (double)vi.y * hdt;
+                nxm.z = xm.z + (double)vi.z * hdt;
+                nxm.w = d;
+                nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
+                                 0.f);
+            } else {
+                txm = in.txm[i];
+                tv = in.tvel[i];
+                double ds = txm.w + (double)drho * hdt;
+                if (k.clamp_density && ds < 0.0) ds = 0.0;
+                double d = 2.0 * ds - txm.w;
+                if (k.clamp_density && d < 0.0) d = 0.0;
+                nxm.x = 2.0 * (txm.x + (double)vi.x * hdt) - txm.x;
+                nxm.y = 2.0 * (txm.y + (double)vi.y * hdt) - txm.y;
+                nxm.z = 2.0 * (txm.z + (double)vi.z * hdt) - txm.z;
+                nxm.w = d;
+                const float uxs = tv.x + ax * k.half_dt;
+                const float uys = tv.y + ay * k.half_dt;
+                const float uzs = tv.z + az * k.half_dt;
+                nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, 0.f);
+            }
+            nrho = k.rho0 + (float)nxm.w;
+            npres = eos_pressure_d(k, (float)nxm.w);
         } else {
-            tp = in.tpos[i];
-            tv = in.tvel[i];
-            float rho = tp.w + drho * k.half_dt;
-            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-            const float xs = tp.x + vi.x * k.half_dt;
-            const float ys = tp.y + vi.y * k.half_dt;
-            const float zs = tp.z + vi.z * k.half_dt;
-            const float uxs = tv.x + ax * k.half_dt;
-            const float uys = tv.y + ay * k.half_dt;
-            const float uzs = tv.z + az * k.half_dt;
-            rho = 2.f * rho - tp.w;
-            if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-            np.x = 2.f * xs - tp.x;
-            np.y = 2.f * ys - tp.y;
-            np.z = 2.f * zs - tp.z;
-            nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, 0.f);
-            nrho = rho;
-            npres = eos_pressure(k, rho);
+            // boundary particles do not move; they keep the extrapolated pressure and density
+            nv = make_float4(vi.x, vi.y, vi.z, 0.f);
+            npres = presi;
+            nrho = rhoi;
+            tv = nv;
         }
+        double ox, oy, oz;
+        cell_origin(k, keys[i], ox, oy, oz);
+        const float px = (float)(nxm.x - ox), py = (float)(nxm.y - oy), pz = (float)(nxm.z - oz);
+        out.rec[2 * (size_t)i] = make_float4(px, py, pz, npres);
+        out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+        if (out.xyz) out.xyz[i] = make_float4(px, py, pz, fi ? 1.f : -1.f);
+        out.type[i] = in.type[i];
+        out.id[i] = in.id[i];
+        out.xm[i] = nxm;
+        if (MODE == MODE_PRED) {
+            out.txm[i] = txm;
+            out.tvel[i] = tv;
+        }
+        unsigned f = 0;
+        out_hash[i] = (unsigned)cell_hash_clamped(k, nxm.x, nxm.y, nxm.z, &f);
+        raise_flags(err, f);
+        if (!fi || !nl.xb) return 0.f;
+        const float4 xb = nl.xb[i];
+        return dist2(px - xb.x, py - xb.y, pz - xb.z);
     } else {
-        // boundary particles do not move; they keep the extrapolated pressure and density
-        nv = make_float4(vi.x, vi.y, vi.z, 0.f);
-        npres = presi;
-        nrho = rhoi;
-        tp = make_float4(pi.x, pi.y, pi.z, rhoi);
-        tv = make_float4(vi.x, vi.y, vi.z, 0.f);
+        V np = pi, nv;
+        T npres, nrho;
+        V tp, tv;
+        if (fi) {
+            if (escaped(k, pi.x, pi.y, pi.z)) {
+                np = make4<T>(k.park_x, k.park_y, k.park_z, T(0));
+                nv = make4<T>(T(0), T(0), T(0), T(0));
+                npres = T(0);
+                nrho = k.rho0;
+                tp = make4<T>(np.x, np.y, np.z, k.rho0);
+                tv = make4<T>(T(0), T(0), T(0), T(0));
+            } else if (MODE == MODE_PRED) {
+                tp = make4<T>(pi.x, pi.y, pi.z, rhoi);
+                tv = make4<T>(vi.x, vi.y, vi.z, T(0));
+                T rho = rhoi + drho * k.half_dt;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                np.x = pi.x + vi.x * k.half_dt;
+                np.y = pi.y + vi.y * k.half_dt;
+                np.z = pi.z + vi.z * k.half_dt;
+                nv = make4<T>(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
+                              T(0));
+                nrho = rho;
+                npres = eos_pressure(k, rho);
+            } else {
+                tp = in.tpos[i];
+                tv = in.tvel[i];
+                T rho = tp.w + drho * k.half_dt;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                const T xs = tp.x + vi.x * k.half_dt;
+                const T ys = tp.y + vi.y * k.half_dt;
+                const T zs = tp.z + vi.z * k.half_dt;
+                const T uxs = tv.x + ax * k.half_dt;
+                const T uys = tv.y + ay * k.half_dt;
+                const T uzs = tv.z + az * k.half_dt;
+                rho = T(2) * rho - tp.w;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                np.x = T(2) * xs - tp.x;
+                np.y = T(2) * ys - tp.y;
+                np.z = T(2) * zs - tp.z;
+                nv = make4<T>(T(2) * uxs - tv.x, T(2) * uys - tv.y, T(2) * uzs - tv.z, T(0));
+                nrho = rho;
+                npres = eos_pressure(k, rho);
+            }
+        } else {
+            // boundary particles do not move; they keep the extrapolated pressure and density
+            nv = make4<T>(vi.x, vi.y, vi.z, T(0));
+            npres = presi;
+            nrho = rhoi;
+            tp = make4<T>(pi.x, pi.y, pi.z, rhoi);
+            tv = make4<T>(vi.x, vi.y, vi.z, T(0));
+        }
+        out.rec[2 * (size_t)i] = make4<T>(np.x, np.y, np.z, npres);
+        out.rec[2 * (size_t)i + 1] = make4<T>(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+        if (out.xyz) out.xyz[i] = make4<T>(np.x, np.y, np.z, fi ? T(1) : T(-1));
+        out.type[i] = in.type[i];
+        out.id[i] = in.id[i];
+        if (MODE == MODE_PRED) {
+            out.tpos[i] = tp;
+            out.tvel[i] = tv;
+        }
+        unsigned f = 0;
+        out_hash[i] = (unsigned)cell_hash_clamped(k, np.x, np.y, np.z, &f);
+        raise_flags(err, f);
+        if (!fi || !nl.xb) return 0.f;
+        const float4 xb = nl.xb[i];
+        return (float)dist2(np.x - (T)xb.x, np.y - (T)xb.y, np.z - (T)xb.z);
     }
-    out.rec[2 * (size_t)i] = make_float4(np.x, np.y, np.z, npres);
-    out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
-    if (out.xyz) out.xyz[i] = make_float4(np.x, np.y, np.z, fi ? 1.f : -1.f);
-    out.type[i] = in.type[i];
-    out.id[i] = in.id[i];
-    if (MODE == MODE_PRED) {
-        out.tpos[i] = tp;
-        out.tvel[i] = tv;
-    }
-    unsigned f = 0;
-    out_hash[i] = (unsigned)cell_hash_clamped(k, np.x, np.y, np.z, &f);
-    raise_flags(err, f);
-    if (!fi || !nl.xb) return 0.f;
-    const float4 xb = nl.xb[i];
-    return dist2(np.x - xb.x, np.y - xb.y, np.z - xb.z);
 }
 
-template <int MODE, bool LIST>
+template <class P, int MODE, bool LIST>
 __global__ void __launch_bounds__(NS_THREADS)
-k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
-        const int* __restrict__ cs, NbrList nl, Pass1Out p1, float* __restrict__ rho_dt,
-        float* __restrict__ vel_dt, int wall_rates, ParticleSet out,
-        unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
+k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+        const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+        Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
+        int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
+        unsigned* err, unsigned* disp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
     if (i < k.n)
-        d2 = pass2_one<MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                   out_hash, err);
+        d2 = pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
+                                      out, out_hash, err);
     if (MODE == MODE_RATES || disp == nullptr) return;
     // block maximum of the squared displacement, one atomic per block (non-negative floats
     // order like their bit patterns)
@@ -404,30 +589,36 @@ k_pass2(KParams k, ParticleSet in, const unsigned* __restrict__ keys,
 
 inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
 
-template <bool LIST>
-void pass1_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
-                  const NbrList& nl, const Pass1Out& o, float* rhop_sum, float* w_sum,
+template <class P, bool LIST>
+void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                  const unsigned* keys, const int* cs, const NbrList& nl,
+                  const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
     const int b = blocks_for(k.n, NS_THREADS);
-    if (rhop_sum && w_sum)
-        k_pass1<true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, rhop_sum, w_sum);
-    else
-        k_pass1<false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, nullptr, nullptr);
+    if constexpr (P::kId == SPH_PREC_FP32) {
+        if (rhop_sum && w_sum) {
+            k_pass1<P, true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, rhop_sum,
+                                                            w_sum);
+            return;
+        }
+    }
+    k_pass1<P, false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, nullptr, nullptr);
 }
 
-template <int MODE>
-void pass2_launch(const KParams& k, const ParticleSet& in, const unsigned* keys, const int* cs,
-                  const NbrList* nl, const Pass1Out& p1, float* rho_dt, float* vel_dt,
-                  int wall_rates, ParticleSet out, unsigned* out_hash, unsigned* err,
-                  unsigned* disp, cudaStream_t s) {
+template <class P, int MODE>
+void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                  const unsigned* keys, const int* cs, const NbrList* nl,
+                  const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
+                  int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
+                  unsigned* err, unsigned* disp, cudaStream_t s) {
     const int b = blocks_for(k.n, NS_THREADS);
     if (nl)
-        k_pass2<MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt, vel_dt,
-                                                      wall_rates, out, out_hash, err, disp);
+        k_pass2<P, MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt, vel_dt,
+                                                         wall_rates, out, out_hash, err, disp);
     else
-        k_pass2<MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, p1, rho_dt,
-                                                       vel_dt, wall_rates, out, out_hash, err,
-                                                       nullptr);
+        k_pass2<P, MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, p1, rho_dt,
+                                                          vel_dt, wall_rates, out, out_hash, err,
+                                                          nullptr);
 }
 
 }  // namespace
@@ -441,23 +632,27 @@ int nbr_capacity_for(const sph_params& p, double skin) {
     return cap < 32 ? 32 : cap;
 }
 
-cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* keys,
+template <class P>
+cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
+                             const ParticleSetT<typename P::T>& in, const unsigned* keys,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    k_nbr_build<<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                                   walls_all, err, gate);
+    k_nbr_build<P><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                      walls_all, err, gate);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* keys,
-                         const int* cs, const NbrList* nl, const Pass1Out& out, float* rhop_sum,
-                         float* w_sum, cudaStream_t s) {
+template <class P>
+cudaError_t launch_pass1(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                         const unsigned* keys, const int* cs, const NbrList* nl,
+                         const Pass1OutT<typename P::T>& out, float* rhop_sum, float* w_sum,
+                         cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (nl)
-        pass1_launch<true>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
+        pass1_launch<P, true>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
     else
-        pass1_launch<false>(k, in, keys, cs, NbrList{}, out, rhop_sum, w_sum, s);
+        pass1_launch<P, false>(k, in, keys, cs, NbrList{}, out, rhop_sum, w_sum, s);
     return cudaGetLastError();
 }
 
@@ -465,23 +660,42 @@ cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in, const un
                                const int* cs, const NbrList* nl, const Pass1Out& p1,
                                float* rho_dt, float* vel_dt, int wall_rates, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    pass2_launch<MODE_RATES>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, ParticleSet{},
-                             nullptr, nullptr, nullptr, s);
+    pass2_launch<PrecF32, MODE_RATES>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
+                                      ParticleSet{}, nullptr, nullptr, nullptr, s);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
-                              const unsigned* keys, const int* cs, const NbrList* nl,
-                              const Pass1Out& p1, ParticleSet out, unsigned* out_hash,
-                              unsigned* err, unsigned* disp, cudaStream_t s) {
+template <class P>
+cudaError_t launch_pass2_step(const KParamsT<typename P::T>& k, HalfStep half,
+                              const ParticleSetT<typename P::T>& in, const unsigned* keys,
+                              const int* cs, const NbrList* nl,
+                              const Pass1OutT<typename P::T>& p1,
+                              ParticleSetT<typename P::T> out, unsigned* out_hash, unsigned* err,
+                              unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     if (half == HALF_PREDICT)
-        pass2_launch<MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err,
-                                disp, s);
+        pass2_launch<P, MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash,
+                                   err, disp, s);
     else
-        pass2_launch<MODE_CORR>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash, err,
-                                disp, s);
+        pass2_launch<P, MODE_CORR>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash,
+                                   err, disp, s);
     return cudaGetLastError();
 }
+
+#define SPH_NS_INSTANTIATE(P)                                                                  \
+    template cudaError_t launch_nbr_build<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&, \
+                                             const unsigned*, const int*, const NbrList&, int, \
+                                             unsigned*, cudaStream_t, const unsigned*);        \
+    template cudaError_t launch_pass1<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&,     \
+                                         const unsigned*, const int*, const NbrList*,          \
+                                         const Pass1OutT<P::T>&, float*, float*, cudaStream_t);\
+    template cudaError_t launch_pass2_step<P>(                                                 \
+        const KParamsT<P::T>&, HalfStep, const ParticleSetT<P::T>&, const unsigned*,           \
+        const int*, const NbrList*, const Pass1OutT<P::T>&, ParticleSetT<P::T>, unsigned*,    \
+        unsigned*, unsigned*, cudaStream_t);
+SPH_NS_INSTANTIATE(PrecF32)
+SPH_NS_INSTANTIATE(PrecF64)
+SPH_NS_INSTANTIATE(PrecMix)
+#undef SPH_NS_INSTANTIATE
 
 }  // namespace sph

@@ -10,34 +10,59 @@
 
 namespace sph {
 
+// 32-byte-aligned vector of four doubles (the FP64 counterpart of float4).
+struct __align__(32) dvec4 {
+    double x, y, z, w;
+};
+
+template <class T> struct Vec4Of;
+template <> struct Vec4Of<float> { using type = float4; };
+template <> struct Vec4Of<double> { using type = dvec4; };
+template <class T> using vec4_t = typename Vec4Of<T>::type;
+
+template <class T>
+__host__ __device__ __forceinline__ vec4_t<T> make4(T x, T y, T z, T w) {
+    vec4_t<T> v;
+    v.x = x;
+    v.y = y;
+    v.z = z;
+    v.w = w;
+    return v;
+}
+
 // Constants every kernel reads, passed by value (they land in the kernel-parameter constant
 // bank, which serves warp-uniform reads as fast as __constant__ memory and lets several
 // contexts with different parameters run side by side).  Derived on the host from
-// sph_params by make_kparams().
-struct KParams {
+// sph_params by make_kparams<T>(): T = float for the FP32 and mixed-precision solvers (the
+// float derivation the reference's kernels see), T = double for the FP64 solver (the same
+// parameters, derived in double).
+template <class T>
+struct KParamsT {
     int n;
     int gx, gy, gz;      // grid dimensions
     int num_cells;
-    float gmin_x, gmin_y, gmin_z;
-    float cell;          // cell edge (gridSize)
-    float h, inv_h, kh, kh2;
-    float kh2_list;      // squared list cutoff (support radius + skin); kh2 without a skin
-    float eta2;
-    float adh;           // 21/(16 pi h^3)
-    float c_fr;          // -5 adh / h^2: grad W = c_fr (1 - q/2)^3 r
-    float mass, rho0, cs, g, half_dt;
-    float delta_h_cs;    // delta h cs
-    float damper;        // rho0 cs h
-    float visc;          // alpha h cs rho0
+    T gmin_x, gmin_y, gmin_z;
+    T cell;              // cell edge (gridSize)
+    T h, inv_h, kh, kh2;
+    T kh2_list;          // squared list cutoff (support radius + skin); kh2 without a skin
+    T eta2;
+    T adh;               // 21/(16 pi h^3)
+    T c_fr;              // -5 adh / h^2: grad W = c_fr (1 - q/2)^3 r
+    T mass, rho0, cs, g, half_dt;
+    T delta_h_cs;        // delta h cs
+    T damper;            // rho0 cs h
+    T visc;              // alpha h cs rho0
     int eos;
-    float tait_gamma, tait_b, inv_tait_b, inv_gamma;
-    float inv_cs2;
+    T tait_gamma, tait_b, inv_tait_b, inv_gamma;
+    T inv_cs2;
     int clamp_density;
-    float esc_min_x, esc_min_y, esc_min_z, esc_max_x, esc_max_y, esc_max_z;
-    float park_x, park_y, park_z;
+    T esc_min_x, esc_min_y, esc_min_z, esc_max_x, esc_max_y, esc_max_z;
+    T park_x, park_y, park_z;
 };
+using KParams = KParamsT<float>;
 
 KParams make_kparams(const sph_params& p, int n);
+template <class T> KParamsT<T> make_kparams_t(const sph_params& p, int n);
 
 // ---------------------------------------------------------------- cell math
 // floorf((p - min) / gridSize) with explicitly IEEE-rounded subtract and divide, so the
@@ -45,6 +70,10 @@ KParams make_kparams(const sph_params& p, int n);
 // contraction flags the file is built with.
 __device__ __forceinline__ int cell_coord(float p, float gmin, float cell) {
     return (int)floorf(__fdiv_rn(__fsub_rn(p, gmin), cell));
+}
+// The FP64 solver's cell of a double position.
+__device__ __forceinline__ int cell_coord(double p, double gmin, double cell) {
+    return (int)floor(__ddiv_rn(__dsub_rn(p, gmin), cell));
 }
 
 // Reference hash without clamping (src/lib/mesh.cu:20-23).
@@ -57,19 +86,42 @@ __device__ __forceinline__ int cell_hash_raw(const KParams& k, float x, float y,
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Cell coordinates of a cell key (z-major: key = (z gy + y) gx + x).
+__device__ __forceinline__ void cell_of_key(int gx, int gy, unsigned key, int& cx, int& cy,
+                                            int& cz) {
+    unsigned t = key / (unsigned)gx;
+    cx = (int)(key - t * (unsigned)gx);
+    cz = (int)(t / (unsigned)gy);
+    cy = (int)(t - (unsigned)cz * (unsigned)gy);
+}
+
+// Origin of a cell of the (float) grid, in double: the frame of the mixed-precision offsets.
+template <class KT>
+__device__ __forceinline__ void cell_origin(const KParamsT<KT>& k, unsigned key, double& ox,
+                                            double& oy, double& oz) {
+    int cx, cy, cz;
+    cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+    ox = (double)k.gmin_x + (double)cx * (double)k.cell;
+    oy = (double)k.gmin_y + (double)cy * (double)k.cell;
+    oz = (double)k.gmin_z + (double)cz * (double)k.cell;
+}
+
 // Hash used by the resident solver: identical to the reference for in-grid positions; an
 // out-of-grid or non-finite position is clamped into the grid and reported through `flag`.
-__device__ __forceinline__ int cell_hash_clamped(const KParams& k, float x, float y, float z,
+// KT is the constant block's real type, PT the position's (a mixed-precision solver hashes its
+// double positions on the float grid, in double).
+template <class KT, class PT>
+__device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT y, PT z,
                                                  unsigned* flag) {
     if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
         *flag |= SPH_FLAG_NONFINITE | SPH_FLAG_OUT_OF_GRID;
-        x = isfinite(x) ? x : k.gmin_x;
-        y = isfinite(y) ? y : k.gmin_y;
-        z = isfinite(z) ? z : k.gmin_z;
+        x = isfinite(x) ? x : (PT)k.gmin_x;
+        y = isfinite(y) ? y : (PT)k.gmin_y;
+        z = isfinite(z) ? z : (PT)k.gmin_z;
     }
-    int cx = cell_coord(x, k.gmin_x, k.cell);
-    int cy = cell_coord(y, k.gmin_y, k.cell);
-    int cz = cell_coord(z, k.gmin_z, k.cell);
+    int cx = cell_coord(x, (PT)k.gmin_x, (PT)k.cell);
+    int cy = cell_coord(y, (PT)k.gmin_y, (PT)k.cell);
+    int cz = cell_coord(z, (PT)k.gmin_z, (PT)k.cell);
     if ((unsigned)cx >= (unsigned)k.gx || (unsigned)cy >= (unsigned)k.gy ||
         (unsigned)cz >= (unsigned)k.gz) {
         *flag |= SPH_FLAG_OUT_OF_GRID;
@@ -81,26 +133,38 @@ __device__ __forceinline__ int cell_hash_clamped(const KParams& k, float x, floa
 }
 
 // ---------------------------------------------------------------- equation of state
-// Linear (the reference's only form, src/sph/sph_run.cu:467) or Tait.  The Tait form is
-// evaluated as B expm1(gamma log1p((rho - rho0)/rho0)): accurate relative to p itself for the
-// small density perturbations of weakly-compressible flow, where B((rho/rho0)^gamma - 1)
-// would lose most of its float digits to cancellation.
-__device__ __forceinline__ float eos_pressure(const KParams& k, float rho) {
-    if (k.eos == SPH_EOS_TAIT)
-        return k.tait_b * expm1f(k.tait_gamma * log1pf((rho - k.rho0) / k.rho0));
-    return k.cs * k.cs * (rho - k.rho0);
+__device__ __forceinline__ float dexpm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double dexpm1(double x) { return expm1(x); }
+__device__ __forceinline__ float dlog1p(float x) { return log1pf(x); }
+__device__ __forceinline__ double dlog1p(double x) { return log1p(x); }
+
+// Pressure of the density perturbation drho = rho - rho0: linear (the reference's only form,
+// src/sph/sph_run.cu:467) or Tait, evaluated as B expm1(gamma log1p(drho/rho0)) — accurate
+// relative to p itself for the small perturbations of weakly-compressible flow, where
+// B((rho/rho0)^gamma - 1) would lose most of its float digits to cancellation.
+template <class T>
+__device__ __forceinline__ T eos_pressure_d(const KParamsT<T>& k, T drho) {
+    if (k.eos == SPH_EOS_TAIT) return k.tait_b * dexpm1(k.tait_gamma * dlog1p(drho / k.rho0));
+    return k.cs * k.cs * drho;
+}
+
+template <class T>
+__device__ __forceinline__ T eos_pressure(const KParamsT<T>& k, T rho) {
+    return eos_pressure_d(k, rho - k.rho0);
 }
 
 // Inverse used for wall particles (src/equation/ns.cu:128 for the linear form).
-__device__ __forceinline__ float eos_density(const KParams& k, float p) {
+template <class T>
+__device__ __forceinline__ T eos_density(const KParamsT<T>& k, T p) {
     if (k.eos == SPH_EOS_TAIT)
-        return k.rho0 + k.rho0 * expm1f(k.inv_gamma * log1pf(p * k.inv_tait_b));
+        return k.rho0 + k.rho0 * dexpm1(k.inv_gamma * dlog1p(p * k.inv_tait_b));
     return p / k.cs / k.cs + k.rho0;
 }
 
-__device__ __forceinline__ bool escaped(const KParams& k, float x, float y, float z) {
-    return x > k.esc_max_x || x < k.esc_min_x || y > k.esc_max_y || y < k.esc_min_y ||
-           z > k.esc_max_z || z < k.esc_min_z;
+template <class KT, class PT>
+__device__ __forceinline__ bool escaped(const KParamsT<KT>& k, PT x, PT y, PT z) {
+    return x > (PT)k.esc_max_x || x < (PT)k.esc_min_x || y > (PT)k.esc_max_y ||
+           y < (PT)k.esc_min_y || z > (PT)k.esc_max_z || z < (PT)k.esc_min_z;
 }
 
 __device__ __forceinline__ bool is_fluid(float typef) { return typef == 1.0f; }

@@ -31,40 +31,72 @@ int key_bits_for(int num_cells);
 cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
                               int* cell_start, cudaStream_t s, const unsigned* gate = nullptr);
 
+// ---------------------------------------------------------------- precision policies
+// The resident solver in three precisions sharing one code path:
+//  PrecF32 — FP32 state and arithmetic (the reference's precision; the drop-in path).
+//  PrecF64 — FP64 state and arithmetic: the accuracy reference every result is measured
+//            against ("an FP64 run of the same solver").
+//  PrecMix — FP32 neighbour sums on relative positions rebuilt from cell-local offsets, with
+//            compensated (Neumaier) accumulation of the density and force sums; FP64 master
+//            positions and density perturbation rho - rho0 for the integration.
+struct PrecF32 {
+    using T = float;
+    static constexpr bool kMixed = false;
+    static constexpr int kId = SPH_PREC_FP32;
+};
+struct PrecF64 {
+    using T = double;
+    static constexpr bool kMixed = false;
+    static constexpr int kId = SPH_PREC_FP64;
+};
+struct PrecMix {
+    using T = float;
+    static constexpr bool kMixed = true;
+    static constexpr int kId = SPH_PREC_MIXED;
+};
+
 // ---------------------------------------------------------------- resident state
-// One particle set.  rec holds two float4 per particle, rec[2i] = (x, y, z, p) and
+// One particle set.  rec holds two vec4 per particle, rec[2i] = (x, y, z, p) and
 // rec[2i+1] = (vx, vy, vz, ±rho) with rho negated for boundary (non-fluid) particles: one
-// aligned 32-byte record, the unit a neighbour gather reads.  type keeps the particle kind as
-// given (0 wall, 1 fluid, 2 rigid, ...), id the original particle index; tpos/tvel hold the
-// predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
-struct ParticleSet {
-    float4* rec = nullptr;
-    float4* xyz = nullptr;  // sorted set only: dense (x, y, z, ±1) for candidate walks
+// aligned record (32 bytes in FP32), the unit a neighbour gather reads.  type keeps the
+// particle kind as given (0 wall, 1 fluid, 2 rigid, ...), id the original particle index;
+// tpos/tvel hold the predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
+// Mixed precision: x, y, z in rec and xyz are offsets from the origin of the particle's cell
+// at the last list build (its sorted key); xm holds the FP64 position and rho - rho0, txm the
+// predictor's save of it (tpos is unused).
+template <class T>
+struct ParticleSetT {
+    vec4_t<T>* rec = nullptr;
+    vec4_t<T>* xyz = nullptr;  // sorted set only: dense (x, y, z, ±1) for candidate walks
     int* type = nullptr;
     int* id = nullptr;
-    float4* tpos = nullptr;
-    float4* tvel = nullptr;
+    vec4_t<T>* tpos = nullptr;
+    vec4_t<T>* tvel = nullptr;
+    dvec4* xm = nullptr;
+    dvec4* txm = nullptr;
 };
+using ParticleSet = ParticleSetT<float>;
 
 // Pass-1 output.  nrec[2i] = (x, y, z, q) with q = p' - rho0 cs h dofv for fluid particles and
 // q = p' for boundary particles, nrec[2i+1] = (vx, vy, vz, ±rho'): the record pass 2 gathers per
 // neighbour.  self[i] = (p', rho', dofv, 0): the particle's own side.
-struct Pass1Out {
-    float4* nrec = nullptr;
-    float4* self = nullptr;
+template <class T>
+struct Pass1OutT {
+    vec4_t<T>* nrec = nullptr;
+    vec4_t<T>* self = nullptr;
 };
+using Pass1Out = Pass1OutT<float>;
 
 enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 
-// Per-half-step neighbour list: idx[i * cap + c] is the c-th neighbour of slot i (walk
-// order), count[i] how many; count[i] > cap means the list overflowed for i and the passes
-// walk the cells for it instead.  cap is a multiple of 16 (rows are 16-byte aligned).
-// The list holds every pair closer than the list cutoff (KParams::kh2_list, the support
-// radius plus a skin); xb (may be NULL) receives each slot's position when the list is built,
-// from which the integrator tracks how far particles have moved since.
 // Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + c * 32 + i % 32] (each warp
 // of 32 consecutive particles owns a block of cap x 32 slots), count[i] entries, and xb[i]
-// the position i had when the list was built.
+// the position i had when the list was built (cell-local offset in mixed precision).  The list
+// holds every pair closer than the list cutoff (KParams::kh2_list, the support radius plus a
+// skin), in candidate-walk order; count[i] > cap means the list overflowed for i and the
+// passes walk the cells for it instead.  Mixed precision stores with each slot, in bits 27-31,
+// the neighbour's cell relative to i's ((dz+1)*9 + (dy+1)*3 + (dx+1)), from which the passes
+// rebuild relative positions out of the cell-local offsets.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
@@ -74,19 +106,25 @@ struct NbrList {
 // List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
 int nbr_capacity_for(const sph_params& p, double skin = 0.0);
 
-// Neighbour passes (equation/ns.cu).  nl == NULL walks the cells in every pass.
+// Neighbour passes (equation/ns.cu), one instantiation per precision policy P.
+// nl == NULL walks the cells in every pass.
 //  build : fills nl for the sorted set (walls keep only fluid neighbours unless walls_all).
 //  pass 1: fills a Pass1Out — boundary particles get the extrapolated p and rho, fluid
 //          particles their own p, rho and the velocity divergence.  rhop_sum / w_sum are
-//          written when non-NULL.
-//  pass 2: either rates only (rho_dt, AoS vel_dt) or rates + the predictor/corrector update
-//          written into `out` (slot-aligned with `in`) with the next cell hash.
-cudaError_t launch_nbr_build(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
+//          written when non-NULL (FP32 only).
+//  pass 2: either rates only (rho_dt, AoS vel_dt; FP32 only) or rates + the
+//          predictor/corrector update written into `out` (slot-aligned with `in`) with the
+//          next cell hash.
+template <class P>
+cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
+                             const ParticleSetT<typename P::T>& in, const unsigned* sorted_keys,
                              const int* cell_start, const NbrList& nl, int walls_all,
                              unsigned* err, cudaStream_t s, const unsigned* gate = nullptr);
-cudaError_t launch_pass1(const KParams& k, const ParticleSet& in, const unsigned* sorted_keys,
-                         const int* cell_start, const NbrList* nl, const Pass1Out& out,
-                         float* rhop_sum, float* w_sum, cudaStream_t s);
+template <class P>
+cudaError_t launch_pass1(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                         const unsigned* sorted_keys, const int* cell_start, const NbrList* nl,
+                         const Pass1OutT<typename P::T>& out, float* rhop_sum, float* w_sum,
+                         cudaStream_t s);
 cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
                                const unsigned* sorted_keys, const int* cell_start,
                                const NbrList* nl, const Pass1Out& p1, float* rho_dt,
@@ -94,26 +132,39 @@ cudaError_t launch_pass2_rates(const KParams& k, const ParticleSet& in,
 // `out` may be `in` (the update is per particle; neighbours are read from p1).  disp (may be
 // NULL) receives, by atomicMax on its float bits, the largest squared distance of a fluid
 // particle from its position when the list was built (nl->xb).
-cudaError_t launch_pass2_step(const KParams& k, HalfStep half, const ParticleSet& in,
-                              const unsigned* sorted_keys, const int* cell_start,
-                              const NbrList* nl, const Pass1Out& p1, ParticleSet out,
-                              unsigned* out_hash, unsigned* err, unsigned* disp, cudaStream_t s);
+template <class P>
+cudaError_t launch_pass2_step(const KParamsT<typename P::T>& k, HalfStep half,
+                              const ParticleSetT<typename P::T>& in, const unsigned* sorted_keys,
+                              const int* cell_start, const NbrList* nl,
+                              const Pass1OutT<typename P::T>& p1,
+                              ParticleSetT<typename P::T> out, unsigned* out_hash, unsigned* err,
+                              unsigned* disp, cudaStream_t s);
 
-// Resident-state glue (lib/mesh.cu).
-// perm == NULL copies slot for slot.
-cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
-                          ParticleSet dst, int with_tmp, cudaStream_t s,
+// Resident-state glue (lib/mesh.cu), one instantiation per precision policy P.
+// perm == NULL copies slot for slot.  Mixed precision: a permuting gather recomputes the
+// cell-local offsets from the FP64 positions for the cells in `keys` (the new sorted keys).
+template <class P>
+cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,
+                          const ParticleSetT<typename P::T>& src, ParticleSetT<typename P::T> dst,
+                          int with_tmp, const unsigned* keys, cudaStream_t s,
                           const unsigned* gate = nullptr);
 // Recompute the cell keys of `set` on the grid of `k` (k.n particles).
-cudaError_t launch_rehash(const KParams& k, const ParticleSet& set, unsigned* hash, unsigned* err,
-                          cudaStream_t s);
-cudaError_t launch_upload_convert(const KParams& k, const float* pos, const float* vel,
-                                  const float* rho, const float* p, const int* type,
-                                  ParticleSet dst, unsigned* hash, unsigned* err,
-                                  cudaStream_t s);
-cudaError_t launch_download_convert(const KParams& k, const ParticleSet& src, float* pos,
-                                    float* vel, float* rho, float* p, int* type,
-                                    cudaStream_t s);
+template <class P>
+cudaError_t launch_rehash(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& set,
+                          unsigned* hash, unsigned* err, cudaStream_t s);
+template <class P>
+cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float* pos,
+                                  const float* vel, const float* rho, const float* p,
+                                  const int* type, ParticleSetT<typename P::T> dst,
+                                  unsigned* hash, unsigned* err, cudaStream_t s);
+template <class P>
+cudaError_t launch_download_convert(const KParamsT<typename P::T>& k,
+                                    const ParticleSetT<typename P::T>& src, float* pos,
+                                    float* vel, float* rho, float* p, int* type, cudaStream_t s);
+template <class P>
+cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
+                                const ParticleSetT<typename P::T>& src, double* pos, double* vel,
+                                double* rho, double* p, cudaStream_t s);
 // Drop-in sph_ns glue: AoS sorted arrays -> SoA set (and back for the outputs).
 cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,
                               const float* s_rho, const float* s_p, const int* s_type,
@@ -137,12 +188,16 @@ struct sph_ctx {
     bool rehash = false;  // the grid changed since the keys in hash_x were computed
     long long steps = 0;
 
-    sph::ParticleSet x;   // integrator output, slot-aligned with the previous sorted order
-    sph::ParticleSet y;   // cell-sorted order the neighbour passes read
+    int prec = SPH_PREC_FP32;   // SPH_OPT_PRECISION
+    // FP32 and mixed precision use x, y, p1; FP64 uses xd, yd, p1d (the other is unallocated)
+    sph::ParticleSet x;   // scratch: permutation target on a rebuild, download staging
+    sph::ParticleSet y;   // live state in the cell-sorted order the neighbour passes read
     unsigned* hash_x = nullptr;      // next cell of every slot of x
     unsigned* keys_sorted = nullptr; // sorted cell keys of y
     int* perm = nullptr;             // y slot k came from x slot perm[k]
     sph::Pass1Out p1;                // pass-1 output
+    sph::ParticleSetT<double> xd, yd;
+    sph::Pass1OutT<double> p1d;
     int* cell_start = nullptr;       // [num_cells + 1]
     int cell_capacity = 0;
     void* sort_scratch = nullptr;

@@ -376,74 +376,160 @@ __global__ void k_recover(float* __restrict__ pos, float* __restrict__ vel,
 }
 
 // ---------------------------------------------------------------- resident-state kernels
-// Signed density of a record: negative marks a boundary (non-fluid) particle.
-__device__ __forceinline__ float signed_rho(int type, float rho) {
+template <class T>
+__device__ __forceinline__ T signed_rho_t(int type, T rho) {
     return type == SPH_TYPE_FLUID ? rho : -rho;
 }
 
-__global__ void k_gather(int n, const int* __restrict__ perm, ParticleSet src, ParticleSet dst,
-                         int with_tmp, const unsigned* gate) {
+// Cell-local offsets of an FP64 position in the cell `key` (mixed precision).
+template <class KT>
+__device__ __forceinline__ float4 offsets_in_cell(const KParamsT<KT>& k, unsigned key,
+                                                  const dvec4& xm, float w) {
+    double ox, oy, oz;
+    cell_origin(k, key, ox, oy, oz);
+    return make_float4((float)(xm.x - ox), (float)(xm.y - oy), (float)(xm.z - oz), w);
+}
+
+// Permute (perm) or copy (perm == NULL) a particle set.  Mixed precision: a permuting gather
+// re-expresses positions as offsets in the new cells keys[k].
+template <class P>
+__global__ void k_gather(KParamsT<typename P::T> kp, const int* __restrict__ perm,
+                         ParticleSetT<typename P::T> src, ParticleSetT<typename P::T> dst,
+                         int with_tmp, const unsigned* __restrict__ keys, const unsigned* gate) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
     if (gated_off(gate)) return;
+    const int n = kp.n;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int s = perm ? perm[k] : k;
     if ((unsigned)s >= (unsigned)n) s = k;  // a consistent permutation never takes this
-    const float4 a = src.rec[2 * (size_t)s], b = src.rec[2 * (size_t)s + 1];
+    V a = src.rec[2 * (size_t)s];
+    const V b = src.rec[2 * (size_t)s + 1];
+    if constexpr (P::kMixed) {
+        const dvec4 xm = src.xm[s];
+        dst.xm[k] = xm;
+        if (with_tmp) dst.txm[k] = src.txm[s];
+        if (perm) a = offsets_in_cell(kp, keys[k], xm, a.w);
+    } else {
+        (void)keys;
+        if (with_tmp) dst.tpos[k] = src.tpos[s];
+    }
     dst.rec[2 * (size_t)k] = a;
     dst.rec[2 * (size_t)k + 1] = b;
-    dst.xyz[k] = make_float4(a.x, a.y, a.z, b.w > 0.f ? 1.f : -1.f);
+    dst.xyz[k] = make4<T>(a.x, a.y, a.z, b.w > T(0) ? T(1) : T(-1));
     dst.type[k] = src.type[s];
     dst.id[k] = src.id[s];
-    if (with_tmp) {
-        dst.tpos[k] = src.tpos[s];
-        dst.tvel[k] = src.tvel[s];
-    }
+    if (with_tmp) dst.tvel[k] = src.tvel[s];
 }
 
-__global__ void k_upload_convert(KParams kp, const float* __restrict__ pos,
+template <class P>
+__global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __restrict__ pos,
                                  const float* __restrict__ vel, const float* __restrict__ rho,
                                  const float* __restrict__ p, const int* __restrict__ type,
-                                 ParticleSet dst, unsigned* __restrict__ hash, unsigned* err) {
+                                 ParticleSetT<typename P::T> dst, unsigned* __restrict__ hash,
+                                 unsigned* err) {
+    using T = typename P::T;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
     const float vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
     const int t = type[i];
-    dst.rec[2 * (size_t)i] = make_float4(x, y, z, p[i]);
-    dst.rec[2 * (size_t)i + 1] = make_float4(vx, vy, vz, signed_rho(t, rho[i]));
+    unsigned f = 0;
     dst.type[i] = t;
     dst.id[i] = i;
-    dst.tpos[i] = make_float4(x, y, z, rho[i]);
-    dst.tvel[i] = make_float4(vx, vy, vz, 0.0f);
-    unsigned f = 0;
-    hash[i] = (unsigned)cell_hash_clamped(kp, x, y, z, &f);
+    dst.tvel[i] = make4<T>(vx, vy, vz, T(0));
+    dst.rec[2 * (size_t)i + 1] = make4<T>(vx, vy, vz, signed_rho_t<T>(t, (T)rho[i]));
+    if constexpr (P::kMixed) {
+        const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[i] - (double)kp.rho0};
+        const unsigned h = (unsigned)cell_hash_clamped(kp, xm.x, xm.y, xm.z, &f);
+        dst.xm[i] = xm;
+        dst.txm[i] = xm;
+        dst.rec[2 * (size_t)i] = offsets_in_cell(kp, h, xm, p[i]);
+        hash[i] = h;
+    } else {
+        dst.rec[2 * (size_t)i] = make4<T>(x, y, z, (T)p[i]);
+        dst.tpos[i] = make4<T>(x, y, z, (T)rho[i]);
+        hash[i] = (unsigned)cell_hash_clamped(kp, (T)x, (T)y, (T)z, &f);
+    }
     raise_flags(err, f);
 }
 
 // Cell keys of a resident set on the current grid (after the grid changed under it).
-__global__ void k_rehash(KParams kp, const float4* __restrict__ xyz, unsigned* __restrict__ hash,
-                         unsigned* err) {
+template <class P>
+__global__ void k_rehash(KParamsT<typename P::T> kp, ParticleSetT<typename P::T> set,
+                         unsigned* __restrict__ hash, unsigned* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
-    const float4 q = xyz[i];
     unsigned f = 0;
-    hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+    if constexpr (P::kMixed) {
+        const dvec4 q = set.xm[i];
+        hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+    } else {
+        const auto q = set.xyz[i];
+        hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+    }
     raise_flags(err, f);
 }
 
-__global__ void k_download_convert(int n, ParticleSet src, float* __restrict__ pos,
+template <class P>
+__global__ void k_download_convert(int n, ParticleSetT<typename P::T> src, float* __restrict__ pos,
                                    float* __restrict__ vel, float* __restrict__ rho,
                                    float* __restrict__ p, int* __restrict__ type) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int r = src.id[k];
     if ((unsigned)r >= (unsigned)n) return;
-    const float4 a = src.rec[2 * (size_t)k], v = src.rec[2 * (size_t)k + 1];
-    if (pos) { pos[3 * r] = a.x; pos[3 * r + 1] = a.y; pos[3 * r + 2] = a.z; }
-    if (vel) { vel[3 * r] = v.x; vel[3 * r + 1] = v.y; vel[3 * r + 2] = v.z; }
-    if (rho) rho[r] = fabsf(v.w);
-    if (p) p[r] = a.w;
+    const auto a = src.rec[2 * (size_t)k];
+    const auto v = src.rec[2 * (size_t)k + 1];
+    if (pos) {
+        if constexpr (P::kMixed) {
+            const dvec4 xm = src.xm[k];
+            pos[3 * r] = (float)xm.x;
+            pos[3 * r + 1] = (float)xm.y;
+            pos[3 * r + 2] = (float)xm.z;
+        } else {
+            pos[3 * r] = (float)a.x;
+            pos[3 * r + 1] = (float)a.y;
+            pos[3 * r + 2] = (float)a.z;
+        }
+    }
+    if (vel) { vel[3 * r] = (float)v.x; vel[3 * r + 1] = (float)v.y; vel[3 * r + 2] = (float)v.z; }
+    if (rho) rho[r] = (float)fabs((double)v.w);
+    if (p) p[r] = (float)a.w;
     if (type) type[r] = src.type[k];
+}
+
+// The state in original order and full precision of the solver (FP64 positions of the FP64
+// and mixed solvers, FP32 values widened otherwise).
+template <class P>
+__global__ void k_download_f64(int n, double rho0, ParticleSetT<typename P::T> src,
+                               double* __restrict__ pos, double* __restrict__ vel,
+                               double* __restrict__ rho, double* __restrict__ p) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int r = src.id[k];
+    if ((unsigned)r >= (unsigned)n) return;
+    const auto a = src.rec[2 * (size_t)k];
+    const auto v = src.rec[2 * (size_t)k + 1];
+    double x = (double)a.x, y = (double)a.y, z = (double)a.z;
+    double rr = fabs((double)v.w);
+    if constexpr (P::kMixed) {
+        const dvec4 xm = src.xm[k];
+        x = xm.x;
+        y = xm.y;
+        z = xm.z;
+        if (src.type[k] == SPH_TYPE_FLUID) rr = rho0 + xm.w;
+    }
+    if (pos) { pos[3 * r] = x; pos[3 * r + 1] = y; pos[3 * r + 2] = z; }
+    if (vel) { vel[3 * r] = v.x; vel[3 * r + 1] = v.y; vel[3 * r + 2] = v.z; }
+    if (rho) rho[r] = rr;
+    if (p) p[r] = (double)a.w;
+}
+
+// Signed density of a record: negative marks a boundary (non-fluid) particle.
+__device__ __forceinline__ float signed_rho(int type, float rho) {
+    return signed_rho_t<float>(type, rho);
 }
 
 // A sorted hash outside [0, num_cells) (a particle outside the grid) is clamped to the
@@ -568,36 +654,75 @@ cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather(const KParams& k, const int* perm, const ParticleSet& src,
-                          ParticleSet dst, int with_tmp, cudaStream_t s, const unsigned* gate) {
+template <class P>
+cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,
+                          const ParticleSetT<typename P::T>& src, ParticleSetT<typename P::T> dst,
+                          int with_tmp, const unsigned* keys, cudaStream_t s,
+                          const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    k_gather<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, perm, src, dst, with_tmp, gate);
+    if (P::kMixed && perm && !keys) return cudaErrorInvalidValue;
+    k_gather<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, perm, src, dst, with_tmp, keys, gate);
     return cudaGetLastError();
 }
 
-cudaError_t launch_upload_convert(const KParams& k, const float* pos, const float* vel,
-                                  const float* rho, const float* p, const int* type,
-                                  ParticleSet dst, unsigned* hash, unsigned* err,
-                                  cudaStream_t s) {
+template <class P>
+cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float* pos,
+                                  const float* vel, const float* rho, const float* p,
+                                  const int* type, ParticleSetT<typename P::T> dst,
+                                  unsigned* hash, unsigned* err, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_upload_convert<<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, dst, hash, err);
+    k_upload_convert<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, dst, hash,
+                                                             err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_rehash(const KParams& k, const ParticleSet& set, unsigned* hash, unsigned* err,
-                          cudaStream_t s) {
+template <class P>
+cudaError_t launch_rehash(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& set,
+                          unsigned* hash, unsigned* err, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_rehash<<<blocks_for(k.n, 256), 256, 0, s>>>(k, set.xyz, hash, err);
+    k_rehash<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, set, hash, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_download_convert(const KParams& k, const ParticleSet& src, float* pos,
-                                    float* vel, float* rho, float* p, int* type,
-                                    cudaStream_t s) {
+template <class P>
+cudaError_t launch_download_convert(const KParamsT<typename P::T>& k,
+                                    const ParticleSetT<typename P::T>& src, float* pos,
+                                    float* vel, float* rho, float* p, int* type, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_download_convert<<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, src, pos, vel, rho, p, type);
+    k_download_convert<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, src, pos, vel, rho, p, type);
     return cudaGetLastError();
 }
+
+template <class P>
+cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
+                                const ParticleSetT<typename P::T>& src, double* pos, double* vel,
+                                double* rho, double* p, cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    k_download_f64<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k.n, (double)k.rho0, src, pos, vel,
+                                                           rho, p);
+    return cudaGetLastError();
+}
+
+#define SPH_MESH_INSTANTIATE(P)                                                                 \
+    template cudaError_t launch_download_f64<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&,\
+                                                double*, double*, double*, double*,             \
+                                                cudaStream_t);                                  \
+    template cudaError_t launch_gather<P>(const KParamsT<P::T>&, const int*,                    \
+                                          const ParticleSetT<P::T>&, ParticleSetT<P::T>, int,   \
+                                          const unsigned*, cudaStream_t, const unsigned*);      \
+    template cudaError_t launch_upload_convert<P>(const KParamsT<P::T>&, const float*,          \
+                                                  const float*, const float*, const float*,     \
+                                                  const int*, ParticleSetT<P::T>, unsigned*,    \
+                                                  unsigned*, cudaStream_t);                     \
+    template cudaError_t launch_rehash<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&,     \
+                                          unsigned*, unsigned*, cudaStream_t);                  \
+    template cudaError_t launch_download_convert<P>(const KParamsT<P::T>&,                      \
+                                                    const ParticleSetT<P::T>&, float*, float*,  \
+                                                    float*, float*, int*, cudaStream_t);
+SPH_MESH_INSTANTIATE(PrecF32)
+SPH_MESH_INSTANTIATE(PrecF64)
+SPH_MESH_INSTANTIATE(PrecMix)
+#undef SPH_MESH_INSTANTIATE
 
 cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,
                               const float* s_rho, const float* s_p, const int* s_type,

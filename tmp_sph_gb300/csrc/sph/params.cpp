@@ -71,6 +71,61 @@ KParams make_kparams(const sph_params& p, int n) {
     return k;
 }
 
+template <>
+KParams make_kparams_t<float>(const sph_params& p, int n) {
+    return make_kparams(p, n);
+}
+
+// The same constants in double, from the same float parameters (the FP64 solver runs the
+// parameters the FP32 solver runs, without rounding anything derived from them to float).
+template <>
+KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
+    KParamsT<double> k{};
+    k.n = n;
+    k.gx = p.grid_dim[0];
+    k.gy = p.grid_dim[1];
+    k.gz = p.grid_dim[2];
+    k.num_cells = p.num_cells;
+    k.gmin_x = p.grid_min[0];
+    k.gmin_y = p.grid_min[1];
+    k.gmin_z = p.grid_min[2];
+    k.cell = p.cell_size;
+    const double h = p.h, kh = p.kh, cs = p.cs, rho0 = p.rho0;
+    k.h = h;
+    k.inv_h = 1.0 / h;
+    k.kh = kh;
+    k.kh2 = kh * kh;
+    k.kh2_list = k.kh2;
+    k.eta2 = (double)p.eta * (double)p.eta;
+    k.adh = p.adh;
+    k.c_fr = -5.0 * (double)p.adh / (h * h);
+    k.mass = p.mass;
+    k.rho0 = rho0;
+    k.cs = cs;
+    k.g = p.gravity;
+    k.half_dt = (double)p.dt / 2.0;
+    k.delta_h_cs = (double)p.delta * h * cs;
+    k.damper = rho0 * cs * h;
+    k.visc = (double)p.alpha * h * cs * rho0;
+    k.eos = p.eos;
+    k.tait_gamma = p.tait_gamma;
+    k.tait_b = p.tait_b;
+    k.inv_tait_b = p.tait_b != 0.f ? 1.0 / (double)p.tait_b : 0.0;
+    k.inv_gamma = p.tait_gamma != 0.f ? 1.0 / (double)p.tait_gamma : 0.0;
+    k.inv_cs2 = 1.0 / (cs * cs);
+    k.clamp_density = p.clamp_density;
+    k.esc_min_x = p.escape_min[0];
+    k.esc_min_y = p.escape_min[1];
+    k.esc_min_z = p.escape_min[2];
+    k.esc_max_x = p.escape_max[0];
+    k.esc_max_y = p.escape_max[1];
+    k.esc_max_z = p.escape_max[2];
+    k.park_x = p.escape_park[0];
+    k.park_y = p.escape_park[1];
+    k.park_z = p.escape_park[2];
+    return k;
+}
+
 }  // namespace sph
 
 extern "C" int sph_params_derive(const sph_config* c, sph_params* P) {

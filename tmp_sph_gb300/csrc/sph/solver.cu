@@ -39,13 +39,15 @@ cudaError_t dalloc(T** p, size_t count) {
     return cudaMalloc(reinterpret_cast<void**>(p), (count > 0 ? count : 1) * sizeof(T));
 }
 
-void free_set(ParticleSet& s) {
+template <class T>
+void free_set(ParticleSetT<T>& s) {
     cudaFree(s.rec); cudaFree(s.xyz); cudaFree(s.type); cudaFree(s.id);
-    cudaFree(s.tpos); cudaFree(s.tvel);
-    s = ParticleSet{};
+    cudaFree(s.tpos); cudaFree(s.tvel); cudaFree(s.xm); cudaFree(s.txm);
+    s = ParticleSetT<T>{};
 }
 
-cudaError_t alloc_set(ParticleSet& s, int cap) {
+template <class T>
+cudaError_t alloc_set(ParticleSetT<T>& s, int cap, bool mixed) {
     cudaError_t e;
     if ((e = dalloc(&s.rec, 2 * (size_t)cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.xyz, cap)) != cudaSuccess) return e;
@@ -53,7 +55,71 @@ cudaError_t alloc_set(ParticleSet& s, int cap) {
     if ((e = dalloc(&s.id, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tpos, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tvel, cap)) != cudaSuccess) return e;
+    if (mixed) {
+        if ((e = dalloc(&s.xm, cap)) != cudaSuccess) return e;
+        if ((e = dalloc(&s.txm, cap)) != cudaSuccess) return e;
+    }
     return cudaSuccess;
+}
+
+template <class T>
+void free_p1(Pass1OutT<T>& p) {
+    cudaFree(p.nrec);
+    cudaFree(p.self);
+    p = Pass1OutT<T>{};
+}
+
+template <class T>
+cudaError_t alloc_p1(Pass1OutT<T>& p, int cap) {
+    cudaError_t e = dalloc(&p.nrec, 2 * (size_t)cap);
+    if (e == cudaSuccess) e = dalloc(&p.self, cap);
+    return e;
+}
+
+// The particle state of the context's precision: x, y, p1 (FP32, mixed) or xd, yd, p1d (FP64).
+void free_state(sph_ctx* c) {
+    free_set(c->x);
+    free_set(c->y);
+    free_p1(c->p1);
+    free_set(c->xd);
+    free_set(c->yd);
+    free_p1(c->p1d);
+}
+
+cudaError_t alloc_state(sph_ctx* c) {
+    const int cap = c->capacity;
+    cudaError_t e;
+    if (c->prec == SPH_PREC_FP64) {
+        if ((e = alloc_set(c->xd, cap, false)) != cudaSuccess) return e;
+        if ((e = alloc_set(c->yd, cap, false)) != cudaSuccess) return e;
+        return alloc_p1(c->p1d, cap);
+    }
+    const bool mixed = c->prec == SPH_PREC_MIXED;
+    if ((e = alloc_set(c->x, cap, mixed)) != cudaSuccess) return e;
+    if ((e = alloc_set(c->y, cap, mixed)) != cudaSuccess) return e;
+    return alloc_p1(c->p1, cap);
+}
+
+// The state arrays one precision policy works on.
+template <class P> struct State {
+    static ParticleSet& x(sph_ctx* c) { return c->x; }
+    static ParticleSet& y(sph_ctx* c) { return c->y; }
+    static Pass1Out& p1(sph_ctx* c) { return c->p1; }
+};
+template <> struct State<PrecF64> {
+    static ParticleSetT<double>& x(sph_ctx* c) { return c->xd; }
+    static ParticleSetT<double>& y(sph_ctx* c) { return c->yd; }
+    static Pass1OutT<double>& p1(sph_ctx* c) { return c->p1d; }
+};
+
+// Calls f(P{}) for the context's precision policy.
+template <class F>
+auto with_prec(const sph_ctx* c, F&& f) {
+    switch (c->prec) {
+        case SPH_PREC_FP64: return f(PrecF64{});
+        case SPH_PREC_MIXED: return f(PrecMix{});
+        default: return f(PrecF32{});
+    }
 }
 
 void drop_graph(sph_ctx* c) {
@@ -67,11 +133,8 @@ void release(sph_ctx* c) {
     drop_graph(c);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
     c->side_stream = nullptr;
-    free_set(c->x);
-    free_set(c->y);
+    free_state(c);
     cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm);
-    cudaFree(c->p1.nrec); cudaFree(c->p1.self);
-    c->p1 = Pass1Out{};
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
     cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb);
     c->nl = NbrList{};
@@ -96,9 +159,11 @@ struct Staging {
 
 Staging staging(sph_ctx* c, int n) {
     Staging s;
-    s.pos = reinterpret_cast<float*>(c->x.tpos);
-    s.vel = reinterpret_cast<float*>(c->x.tvel);
-    float* a = reinterpret_cast<float*>(c->p1.nrec);  // 8n floats
+    const bool d = c->prec == SPH_PREC_FP64;
+    s.pos = d ? reinterpret_cast<float*>(c->xd.tpos) : reinterpret_cast<float*>(c->x.tpos);
+    s.vel = d ? reinterpret_cast<float*>(c->xd.tvel) : reinterpret_cast<float*>(c->x.tvel);
+    // 8n floats (FP32 records) or 16n (FP64)
+    float* a = d ? reinterpret_cast<float*>(c->p1d.nrec) : reinterpret_cast<float*>(c->p1.nrec);
     s.rho = a;
     s.p = a + n;
     s.type = reinterpret_cast<int*>(a + 2 * (size_t)n);
@@ -138,10 +203,11 @@ sph_params internal_params(const sph_params& P, double skin) {
     return Q;
 }
 
-KParams resident_kparams(const sph_ctx* c) {
-    KParams k = make_kparams(c->Pi, c->n);
+template <class T>
+KParamsT<T> resident_kparams(const sph_ctx* c) {
+    KParamsT<T> k = make_kparams_t<T>(c->Pi, c->n);
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
-    k.kh2_list = (float)(cut * cut);
+    k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
     return k;
 }
@@ -171,7 +237,9 @@ struct CondCapture {
 };
 
 // Sort, gather, cell starts and list build, each kernel gated on rb[0].  `ev` as half_step.
-cudaError_t rebuild_lists(sph_ctx* c, const KParams& k, cudaStream_t s, cudaEvent_t* ev) {
+template <class P>
+cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStream_t s,
+                          cudaEvent_t* ev) {
     const int bits = key_bits_for(c->Pi.num_cells);
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
@@ -181,22 +249,26 @@ cudaError_t rebuild_lists(sph_ctx* c, const KParams& k, cudaStream_t s, cudaEven
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_GATHER], s);
     // permute the live set y into cell order through x, then copy it back
-    if ((e = launch_gather(k, c->perm, c->y, c->x, 1, s, gate)) != cudaSuccess) return e;
-    if ((e = launch_gather(k, nullptr, c->x, c->y, 1, s, gate)) != cudaSuccess) return e;
+    auto& x = State<P>::x(c);
+    auto& y = State<P>::y(c);
+    if ((e = launch_gather<P>(k, c->perm, y, x, 1, c->keys_sorted, s, gate)) != cudaSuccess)
+        return e;
+    if ((e = launch_gather<P>(k, nullptr, x, y, 1, nullptr, s, gate)) != cudaSuccess) return e;
     if ((e = build_cell_starts(c->keys_sorted, c->n, c->Pi.num_cells, c->cell_start, s, gate)) !=
         cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_NBR], s);
-    if (nl && (e = launch_nbr_build(k, c->y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s,
-                                    gate)) != cudaSuccess)
+    if (nl && (e = launch_nbr_build<P>(k, y, c->keys_sorted, c->cell_start, *nl, 0, c->err, s,
+                                       gate)) != cudaSuccess)
         return e;
     return cudaSuccess;
 }
 
 // Adds an IF node (condition cc.handle) after the current capture dependencies of `s` and
 // captures the rebuild kernels into its body on cc.side.
-cudaError_t capture_conditional_rebuild(sph_ctx* c, const KParams& k, cudaStream_t s,
-                                        const CondCapture& cc) {
+template <class P>
+cudaError_t capture_conditional_rebuild(sph_ctx* c, const KParamsT<typename P::T>& k,
+                                        cudaStream_t s, const CondCapture& cc) {
     cudaStreamCaptureStatus st;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -218,7 +290,7 @@ cudaError_t capture_conditional_rebuild(sph_ctx* c, const KParams& k, cudaStream
     if ((e = cudaStreamBeginCaptureToGraph(cc.side, body, nullptr, nullptr, 0,
                                            cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return e;
-    e = rebuild_lists(c, k, cc.side, nullptr);
+    e = rebuild_lists<P>(c, k, cc.side, nullptr);
     cudaGraph_t out = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(cc.side, &out);
     return e != cudaSuccess ? e : e2;
@@ -226,9 +298,12 @@ cudaError_t capture_conditional_rebuild(sph_ctx* c, const KParams& k, cudaStream
 
 // One half step (see the file comment).  `ev` (may be NULL) receives PH_COUNT + 1 timestamps;
 // `cc` (may be NULL) puts the rebuild kernels under a conditional node of the capture.
+template <class P>
 cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev,
                       const CondCapture* cc = nullptr) {
-    const KParams k = resident_kparams(c);
+    const KParamsT<typename P::T> k = resident_kparams<typename P::T>(c);
+    auto& y = State<P>::y(c);
+    auto& p1 = State<P>::p1(c);
     const NbrList* nl = list_for(c);
     const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
     const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
@@ -237,25 +312,29 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     cudaError_t e;
     if (ev) cudaEventRecord(ev[PH_SORT], s);
     k_decide<<<1, 1, 0, s>>>(c->rb, thr_bits, nl ? 0 : 1, cc ? cc->handle : 0, cc ? 1 : 0);
-    e = cc ? capture_conditional_rebuild(c, k, s, *cc) : rebuild_lists(c, k, s, ev);
+    e = cc ? capture_conditional_rebuild<P>(c, k, s, *cc) : rebuild_lists<P>(c, k, s, ev);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
-    if ((e = launch_pass1(k, c->y, c->keys_sorted, c->cell_start, nl, c->p1, nullptr, nullptr,
-                          s)) != cudaSuccess)
+    if ((e = launch_pass1<P>(k, y, c->keys_sorted, c->cell_start, nl, p1, nullptr, nullptr,
+                             s)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_PASS2], s);
     // in place: pass 2 reads its neighbours from the pass-1 records
-    e = launch_pass2_step(k, half, c->y, c->keys_sorted, c->cell_start, nl, c->p1, c->y,
-                          c->hash_x, c->err, c->rb + 1, s);
+    e = launch_pass2_step<P>(k, half, y, c->keys_sorted, c->cell_start, nl, p1, y, c->hash_x,
+                             c->err, c->rb + 1, s);
     if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
 }
 
 cudaError_t full_step(sph_ctx* c, cudaStream_t s, cudaEvent_t* ev,
                       const CondCapture* cc = nullptr) {
-    cudaError_t e = half_step(c, HALF_PREDICT, s, ev, cc);
-    if (e != cudaSuccess) return e;
-    return half_step(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr, cc ? cc + 1 : nullptr);
+    return with_prec(c, [&](auto tag) {
+        using P = decltype(tag);
+        cudaError_t e = half_step<P>(c, HALF_PREDICT, s, ev, cc);
+        if (e != cudaSuccess) return e;
+        return half_step<P>(c, HALF_CORRECT, s, ev ? ev + EV_PER_HALF : nullptr,
+                            cc ? cc + 1 : nullptr);
+    });
 }
 
 // The step graph with the rebuild kernels under two conditional nodes (one per half step).
@@ -331,13 +410,10 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     cudaGetDevice(&c->device);
     cudaError_t e = cudaSuccess;
     const int cap = capacity;
-    if (e == cudaSuccess) e = alloc_set(c->x, cap);
-    if (e == cudaSuccess) e = alloc_set(c->y, cap);
+    if (e == cudaSuccess) e = alloc_state(c);
     if (e == cudaSuccess) e = dalloc(&c->hash_x, cap);
     if (e == cudaSuccess) e = dalloc(&c->keys_sorted, cap);
     if (e == cudaSuccess) e = dalloc(&c->perm, cap);
-    if (e == cudaSuccess) e = dalloc(&c->p1.nrec, 2 * (size_t)cap);
-    if (e == cudaSuccess) e = dalloc(&c->p1.self, cap);
     c->cell_capacity = std::max(p->num_cells, c->Pi.num_cells);
     if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)c->cell_capacity + 1);
     c->sort_scratch_bytes = sort_scratch_bytes(cap);
@@ -414,6 +490,25 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             drop_graph(c);
             return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
+        case SPH_OPT_PRECISION: {
+            if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && value != SPH_PREC_MIXED)
+                return SPH_ERR_ARG;
+            if (value == c->prec) return SPH_OK;
+            drop_graph(c);
+            free_state(c);
+            c->prec = value;
+            c->loaded = false;
+            c->n = 0;
+            if (alloc_state(c) != cudaSuccess) {
+                cudaGetLastError();
+                free_state(c);
+                c->prec = SPH_PREC_FP32;
+                alloc_state(c);
+                cudaGetLastError();
+                return SPH_ERR_NOMEM;
+            }
+            return SPH_OK;
+        }
         case SPH_OPT_PROFILE: c->opt_profile = value != 0; return SPH_OK;
         case SPH_OPT_NEIGHBOR_LIST:
             c->opt_nbr_list = value != 0;
@@ -448,6 +543,8 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
                           const float* p, const int* type, int n, int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
+    // mixed-precision list slots keep the neighbour index in 27 bits
+    if (c->prec == SPH_PREC_MIXED && n >= (1 << 27)) return SPH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     if (n != c->n) drop_graph(c);
     c->n = n;
@@ -478,11 +575,14 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
     }
     // the state goes straight into the live set, hashed on the solver's grid; the first half
     // step sorts it
-    const KParams k = resident_kparams(c);
     if (cudaMemsetAsync(c->rb, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
         force_rebuild(c, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    return to_status(launch_upload_convert(k, dpos, dvel, drho, dp, dtype, c->y, c->hash_x, c->err, s));
+    return to_status(with_prec(c, [&](auto tag) {
+        using P = decltype(tag);
+        return launch_upload_convert<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho, dp,
+                                        dtype, State<P>::y(c), c->hash_x, c->err, s);
+    }));
 }
 
 extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, float* p, int* type,
@@ -492,22 +592,60 @@ extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, floa
     const int n = c->n;
     if (n == 0) return SPH_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    KParams k = make_kparams(c->P, n);
-    if (!to_host)
-        return to_status(launch_download_convert(k, c->y, pos, vel, rho, p, type, s));
+    auto convert = [&](float* dpos, float* dvel, float* drho, float* dp, int* dtype) {
+        return with_prec(c, [&](auto tag) {
+            using P = decltype(tag);
+            return launch_download_convert<P>(resident_kparams<typename P::T>(c), State<P>::y(c),
+                                              dpos, dvel, drho, dp, dtype, s);
+        });
+    };
+    if (!to_host) return to_status(convert(pos, vel, rho, p, type));
     Staging st = staging(c, n);
     float* spos = pos ? st.pos : nullptr;
     float* svel = vel ? st.vel : nullptr;
     float* srho = rho ? st.rho : nullptr;
     float* sp = p ? st.p : nullptr;
     int* stype = type ? st.type : nullptr;
-    cudaError_t e = launch_download_convert(k, c->y, spos, svel, srho, sp, stype, s);
-    if (e != cudaSuccess) return SPH_ERR_CUDA;
+    if (convert(spos, svel, srho, sp, stype) != cudaSuccess) return SPH_ERR_CUDA;
     if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (vel && cudaMemcpyAsync(vel, svel, (size_t)n * 12, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (rho && cudaMemcpyAsync(rho, srho, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (p && cudaMemcpyAsync(p, sp, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (type && cudaMemcpyAsync(type, stype, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess))
+        return SPH_ERR_CUDA;
+    return SPH_OK;
+}
+
+extern "C" int sph_download_f64(sph_ctx* c, double* pos, double* vel, double* rho, double* p,
+                                int to_host, void* stream) {
+    if (!c) return SPH_ERR_ARG;
+    if (!c->loaded) return SPH_ERR_STATE;
+    const int n = c->n;
+    if (n == 0) return SPH_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    auto convert = [&](double* dpos, double* dvel, double* drho, double* dp) {
+        return with_prec(c, [&](auto tag) {
+            using P = decltype(tag);
+            return launch_download_f64<P>(resident_kparams<typename P::T>(c), State<P>::y(c),
+                                          dpos, dvel, drho, dp, s);
+        });
+    };
+    if (!to_host) return to_status(convert(pos, vel, rho, p));
+    // staging in buffers that hold nothing between steps: the scratch set's records
+    // (>= 32 B per particle) for positions and the pass-1 records for velocities, the scratch
+    // set's predictor arrays (>= 16 B per particle) for density and pressure
+    const bool d = c->prec == SPH_PREC_FP64;
+    double* spos = d ? reinterpret_cast<double*>(c->xd.rec) : reinterpret_cast<double*>(c->x.rec);
+    double* svel = d ? reinterpret_cast<double*>(c->p1d.nrec) : reinterpret_cast<double*>(c->p1.nrec);
+    double* srho = d ? reinterpret_cast<double*>(c->xd.tpos) : reinterpret_cast<double*>(c->x.tpos);
+    double* sp = d ? reinterpret_cast<double*>(c->xd.tvel) : reinterpret_cast<double*>(c->x.tvel);
+    if (convert(pos ? spos : nullptr, vel ? svel : nullptr, rho ? srho : nullptr,
+                p ? sp : nullptr) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 24, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (vel && cudaMemcpyAsync(vel, svel, (size_t)n * 24, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (rho && cudaMemcpyAsync(rho, srho, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (p && cudaMemcpyAsync(p, sp, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess))
         return SPH_ERR_CUDA;
     return SPH_OK;
 }
@@ -523,8 +661,12 @@ extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
     if (c->rehash) {
         // the grid changed (sph_set_params, skin option): the keys pass 2 wrote for the
         // current positions index the old grid
-        if (launch_rehash(resident_kparams(c), c->y, c->hash_x, c->err, s) != cudaSuccess)
-            return SPH_ERR_CUDA;
+        const cudaError_t e = with_prec(c, [&](auto tag) {
+            using P = decltype(tag);
+            return launch_rehash<P>(resident_kparams<typename P::T>(c), State<P>::y(c), c->hash_x,
+                                    c->err, s);
+        });
+        if (e != cudaSuccess) return SPH_ERR_CUDA;
         c->rehash = false;
     }
     if (c->opt_profile) {
@@ -610,7 +752,7 @@ extern "C" int sph_ctx_sorted_view(sph_ctx* c, const int** cell_start, const int
     if (!c) return SPH_ERR_ARG;
     if (num_cells) *num_cells = c->Pi.num_cells;
     if (cell_start) *cell_start = c->cell_start;
-    if (sorted_id) *sorted_id = c->y.id;
+    if (sorted_id) *sorted_id = c->prec == SPH_PREC_FP64 ? c->yd.id : c->y.id;
     if (sorted_hash) *sorted_hash = reinterpret_cast<const int*>(c->keys_sorted);
     return SPH_OK;
 }
@@ -654,6 +796,7 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     (void)cell_start;
     (void)cell_end;  // the dense cell starts are rebuilt from the sorted hash
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
+    if (c->prec == SPH_PREC_FP64) return SPH_ERR_STATE;  // the drop-in runs the FP32 kernels
     if (n == 0) return SPH_OK;
     if (!s_pos || !s_vel || !s_rho || !s_p || !s_type || !rho_dt || !vel_dt || !hash || !dofv)
         return SPH_ERR_ARG;
@@ -666,10 +809,10 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     const NbrList* nl = list_for(c);
-    if (nl && (e = launch_nbr_build(k, c->x, c->keys_sorted, c->cell_start, *nl,
+    if (nl && (e = launch_nbr_build<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, *nl,
                                     c->opt_wall_rates, c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass1(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
+    if ((e = launch_pass1<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
                           s)) != cudaSuccess)
         return SPH_ERR_CUDA;
     if ((e = launch_pass2_rates(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt,

@@ -24,13 +24,16 @@ def _stream(stream) -> int | None:
 class Solver:
     """Resident solver context (sph_create ... sph_destroy)."""
 
-    def __init__(self, params: api.SphParams, capacity: int | None = None):
+    def __init__(self, params: api.SphParams, capacity: int | None = None,
+                 precision: str = "fp32"):
         self.params = params
         cap = capacity if capacity is not None else params.num_particles
         h = C.c_void_p()
         call("sph_create", C.byref(params), cap, C.byref(h))
         self.handle = h
         self.capacity = cap
+        if precision != "fp32":
+            self.set_option(api.SPH_OPT_PRECISION, api.PRECISIONS[precision])
 
     def close(self) -> None:
         if self.handle:
@@ -83,6 +86,18 @@ class Solver:
                "type": np.zeros(n, np.int32)}
         call("sph_download", self.handle, ptr(out["pos"]), ptr(out["vel"]), ptr(out["rho"]),
              ptr(out["p"]), ptr(out["type"]), 1, _stream(stream))
+        torch.cuda.synchronize()
+        return out
+
+    def download_f64(self, stream=None) -> dict:
+        """State in original order as host float64 arrays, in the solver's full precision
+        (synchronises)."""
+        import torch
+        n = self.n
+        out = {"pos": np.zeros((n, 3)), "vel": np.zeros((n, 3)), "rho": np.zeros(n),
+               "p": np.zeros(n)}
+        call("sph_download_f64", self.handle, ptr(out["pos"]), ptr(out["vel"]), ptr(out["rho"]),
+             ptr(out["p"]), 1, _stream(stream))
         torch.cuda.synchronize()
         return out
 

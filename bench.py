@@ -314,6 +314,28 @@ def main():
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     no_reuse = {"value": n * k0 / (ms0 / 1e3), "ms_per_step": ms0 / k0, "steps": k0}
 
+    # the same workload in the other precisions of the solver (same skin, graph replay)
+    def time_precision(precision: str, steps: int) -> dict:
+        v = S.Solver(p, n, precision=precision)
+        v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+        v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
+        v.step(3, stream=stream)
+        torch.cuda.synchronize()
+        r0 = v.rebuild_count(stream=stream)
+        ev0.record(stream)
+        v.step(steps, stream=stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t = ev0.elapsed_time(ev1)
+        out = {"value": n * steps / (t / 1e3), "ms_per_step": t / steps, "steps": steps,
+               "list_rebuilds": v.rebuild_count(stream=stream) - r0,
+               "device_error_flags": v.error_flags(stream=stream)}
+        v.close()
+        return out
+
+    variants = {"mixed": time_precision("mixed", min(args.steps, 50)),
+                "fp64": time_precision("fp64", min(args.steps, 10))}
+
     # per-kernel device time from CUDA events around every phase, same stream
     prof_steps = min(args.steps, 20)
     sol.set_option(api.SPH_OPT_PROFILE, 1)
@@ -386,6 +408,7 @@ def main():
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
                           "skin_permille": args.skin},
         "rebuild_every_half_step": no_reuse,
+        "precision_variants": variants,
         "clocks": clk.summary(),
         "device_error_flags": flags,
     }

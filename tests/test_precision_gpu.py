@@ -48,8 +48,11 @@ def errors(out, ref, st):
 
 @pytest.mark.parametrize("physics", ["reference", "config"])
 def test_fp64_matches_fp64_oracle(sphlib, oracle, cuda, report, physics):
-    """The FP64 solver against the oracle in FP64 (the reference's arithmetic, double): the
-    only differences left are FP64 rounding and summation order."""
+    """The FP64 solver against the oracle in FP64 (the reference's arithmetic, double).  The
+    oracle forms the constant products rho0 cs h, alpha h cs, delta h cs and eta^2 from the
+    float parameters in float, as the reference's kernels do; the FP64 solver forms them in
+    double.  Those constants differ by up to ~1e-7 relative and move the fields by ~1e-9, two
+    orders below the ~1e-5 of FP32 (measured 1 step: vel 1.6e-9 / 2.9e-9, rho 4e-11)."""
     from tmp_sph_gb300 import cases
     st, p = cases.build("small", physics=physics, dx=0.02, jitter=0.01)
     P = oracle.params_like(p)
@@ -59,13 +62,14 @@ def test_fp64_matches_fp64_oracle(sphlib, oracle, cuda, report, physics):
         assert out["flags"] == 0
         e = errors(out["f64"], ref, st)
         for k, v in e.items():
-            report(f"fp64 vs fp64 oracle {physics} {nsteps} steps {k}", v, 1e-9)
-        assert all(v < 1e-9 for v in e.values()), e
+            report(f"fp64 vs fp64 oracle {physics} {nsteps} steps {k}", v, 1e-7)
+        assert all(v < 1e-7 for v in e.values()), e
 
 
 def test_fp32_and_mixed_against_fp64(sphlib, cuda, report):
     """1000 steps of the small dam break (27,288 particles): FP32 and mixed precision against
-    the FP64 run of the same solver, relative L2 of displacement, velocity, rho - rho0, p."""
+    the FP64 run of the same solver, relative L2 of displacement, velocity, rho - rho0, p
+    (measured: FP32 3e-5 / 9e-5 / 4e-4 / 4e-4, mixed 1e-6 / 3e-6 / 1.3e-5 / 1.3e-5)."""
     from tmp_sph_gb300 import cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
     steps = 1000

@@ -313,6 +313,44 @@ int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
 /* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream). */
 int sph_read_rebuild_count(sph_ctx* ctx, unsigned* count, void* stream);
 
+/* ---------------------------------------------------------------- probes and reductions */
+/* Measurements of the resident state computed on the GPU (no reference counterpart: the
+ * reference copies the whole state to the host every output interval and scans it there for
+ * its gauges, src/io/io.cu:236-279). */
+#define SPH_PROBE_PRESSURE 0  /* Shepard-normalised Wendland average of fluid pressure within kh
+                                 of (x, y, z); 0 when no fluid is in range */
+#define SPH_PROBE_HEIGHT   1  /* water height: largest z of fluid particles with |x - x0| < radius,
+                                 |y - y0| < radius and, if zmax > 0, z < zmax (the reference's
+                                 gauges use radius 1.5 dx); 0 when none */
+#define SPH_PROBE_FRONT    2  /* surge front: largest x of any fluid particle */
+#define SPH_MAX_PROBES 32
+typedef struct sph_probe {
+    int   kind;
+    float x, y, z;
+    float radius;
+    float zmax;
+} sph_probe;
+
+/* Global FP64 reductions over the fluid particles. */
+typedef struct sph_stats {
+    long long fluid;     /* fluid particles */
+    long long parked;    /* of which parked at escape_park after leaving the escape box */
+    double mass;         /* sum of masses */
+    double kinetic;      /* sum m |v|^2 / 2 */
+    double potential;    /* sum -m g z (gravity along z) */
+    double max_speed;
+    double rho_min, rho_max;
+    double front_x;      /* largest x */
+    double cfl_dt;       /* cfl h / (cs + max_speed): the step a CFL rule with this number
+                            would take now (the solver itself keeps the fixed dt) */
+} sph_stats;
+
+/* Evaluate nprobes (<= SPH_MAX_PROBES) probes into values[] (Pa or m) and, if stats is not
+ * NULL, the reductions with CFL number cfl.  One kernel over the resident state; synchronises
+ * the stream to return the numbers. */
+int sph_probe_read(sph_ctx* ctx, const sph_probe* probes, int nprobes, double* values,
+                   double cfl, sph_stats* stats, void* stream);
+
 /* ---------------------------------------------------------------- reference-signature shim */
 /* The library also exports, with C++ linkage, the reference's own host functions calcHash,
  * sortParticles, reorder, recover, SPH_NS_simpleversion, PC_prediction, PC_correction,

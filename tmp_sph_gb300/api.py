@@ -114,6 +114,25 @@ class SphDamBreak(C.Structure):
     ]
 
 
+SPH_PROBE_PRESSURE, SPH_PROBE_HEIGHT, SPH_PROBE_FRONT = 0, 1, 2
+SPH_MAX_PROBES = 32
+
+
+class SphProbe(C.Structure):
+    _fields_ = [("kind", C.c_int), ("x", C.c_float), ("y", C.c_float), ("z", C.c_float),
+                ("radius", C.c_float), ("zmax", C.c_float)]
+
+
+class SphStats(C.Structure):
+    _fields_ = [("fluid", C.c_longlong), ("parked", C.c_longlong), ("mass", C.c_double),
+                ("kinetic", C.c_double), ("potential", C.c_double), ("max_speed", C.c_double),
+                ("rho_min", C.c_double), ("rho_max", C.c_double), ("front_x", C.c_double),
+                ("cfl_dt", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 _P = C.c_void_p
 _I = C.c_int
 _PP = C.POINTER(SphParams)
@@ -147,6 +166,8 @@ _PROTOS = {
     "sph_step_host": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I)]),
     "sph_read_rebuild_count": (_I, [_P, C.POINTER(C.c_uint), _P]),
+    "sph_probe_read": (_I, [_P, C.POINTER(SphProbe), _I, C.POINTER(C.c_double), C.c_double,
+                            C.POINTER(SphStats), _P]),
     "sph_read_error_flags": (_I, [_P, C.POINTER(C.c_uint), _P]),
     "sph_steps_taken": (_I, [_P, C.POINTER(C.c_longlong)]),
     "sph_profile_read": (_I, [_P, C.POINTER(C.c_double), C.POINTER(C.c_longlong), _I]),

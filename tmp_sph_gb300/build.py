@@ -31,6 +31,7 @@ SOURCES = [
     "sph/params.cpp",
     "sph/ref_shim.cu",
     "io/dam_break.cpp",
+    "io/probes.cu",
 ]
 HEADERS = ["header/sph_device.cuh", "header/sph_internal.h"]
 

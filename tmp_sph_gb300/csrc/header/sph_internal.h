@@ -165,6 +165,14 @@ template <class P>
 cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
                                 const ParticleSetT<typename P::T>& src, double* pos, double* vel,
                                 double* rho, double* p, cudaStream_t s);
+// Probes and FP64 reductions (io/probes.cu): launch_probes fills a device accumulator of
+// probe_acc_words() doubles, probe_results turns its host copy into sph_stats and probe values.
+size_t probe_acc_words();
+template <class P>
+cudaError_t launch_probes(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& set,
+                          const sph_probe* probes, int nprobes, double* acc, cudaStream_t s);
+void probe_results(const double* acc, const sph_probe* probes, int nprobes, double cfl, double h,
+                   double cs, sph_stats* stats, double* values);
 // Drop-in sph_ns glue: AoS sorted arrays -> SoA set (and back for the outputs).
 cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,
                               const float* s_rho, const float* s_p, const int* s_type,
@@ -203,6 +211,7 @@ struct sph_ctx {
     void* sort_scratch = nullptr;
     size_t sort_scratch_bytes = 0;
     unsigned* err = nullptr;         // device error word
+    double* probe_acc = nullptr;     // probe / reduction accumulator (probe_acc_words())
 
     // neighbour list, reused across half steps while every particle stays within skin/2 of
     // where it was when the list was built

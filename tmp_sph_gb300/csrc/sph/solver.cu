@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "sph_internal.h"
 
@@ -140,6 +141,8 @@ void release(sph_ctx* c) {
     c->nl = NbrList{};
     cudaFree(c->rb);
     c->rb = nullptr;
+    cudaFree(c->probe_acc);
+    c->probe_acc = nullptr;
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -420,6 +423,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sort_scratch, c->sort_scratch_bytes);
     if (e == cudaSuccess) e = dalloc(&c->err, 1);
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = dalloc(&c->probe_acc, probe_acc_words());
     if (e == cudaSuccess) e = dalloc(&c->rb, 4);
     if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
@@ -647,6 +651,29 @@ extern "C" int sph_download_f64(sph_ctx* c, double* pos, double* vel, double* rh
         (rho && cudaMemcpyAsync(rho, srho, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
         (p && cudaMemcpyAsync(p, sp, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess))
         return SPH_ERR_CUDA;
+    return SPH_OK;
+}
+
+extern "C" int sph_probe_read(sph_ctx* c, const sph_probe* probes, int nprobes, double* values,
+                              double cfl, sph_stats* stats, void* stream) {
+    if (!c || nprobes < 0 || nprobes > SPH_MAX_PROBES || (nprobes > 0 && (!probes || !values)))
+        return SPH_ERR_ARG;
+    if (!c->loaded) return SPH_ERR_STATE;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<double> acc(probe_acc_words(), 0.0);
+    if (c->n > 0) {
+        const cudaError_t e = with_prec(c, [&](auto tag) {
+            using P = decltype(tag);
+            return launch_probes<P>(resident_kparams<typename P::T>(c), State<P>::y(c), probes,
+                                    nprobes, c->probe_acc, s);
+        });
+        if (e != cudaSuccess ||
+            cudaMemcpyAsync(acc.data(), c->probe_acc, acc.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return SPH_ERR_CUDA;
+    }
+    probe_results(acc.data(), probes, nprobes, cfl, c->P.h, c->P.cs, stats, values);
     return SPH_OK;
 }
 

@@ -135,6 +135,18 @@ class Solver:
         call("sph_read_rebuild_count", self.handle, C.byref(v), _stream(stream))
         return v.value
 
+    def probe(self, probes=(), cfl: float = 0.25, stream=None) -> tuple[list, dict]:
+        """Probe values (one per (kind, x, y, z, radius, zmax) tuple or api.SphProbe) and the
+        FP64 fluid statistics, computed on the GPU (synchronises)."""
+        arr = (api.SphProbe * max(1, len(probes)))()
+        for i, pb in enumerate(probes):
+            arr[i] = pb if isinstance(pb, api.SphProbe) else api.SphProbe(*pb)
+        vals = (C.c_double * max(1, len(probes)))()
+        st = api.SphStats()
+        call("sph_probe_read", self.handle, arr, len(probes), vals, cfl, C.byref(st),
+             _stream(stream))
+        return [vals[i] for i in range(len(probes))], st.as_dict()
+
     def ns(self, s_pos, s_vel, s_rho, s_p, s_type, rho_dt, vel_dt, cell_start, cell_end, n,
            hash_, dofv, rhop_sum=None, w_sum=None, stream=None) -> None:
         """SPH_NS_simpleversion (src/header/ns.cuh:4) on this context's parameters."""

@@ -56,8 +56,8 @@ namespace sph {
 namespace {
 
 constexpr int NS_THREADS = 128;
-// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^27).
-constexpr int CODE_SHIFT = 27;
+// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^26).
+constexpr int CODE_SHIFT = 26;
 constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
 
 // Squared distance with an explicit rounding sequence, so the in-range test gives the same
@@ -99,8 +99,8 @@ struct Sum {
 
 // Visit every candidate slot j of the 27 cells around (cx, cy, cz): f(j, code).  Without CODES
 // each x-strip is one range and code is 0; with CODES the strip's three cells are visited one
-// by one and code = (dz+1)*9 + (dy+1)*3 + (dx+1) is j's cell relative to (cx, cy, cz).  Both
-// visit the same slots in the same order.
+// by one and code = (dz+1) << 4 | (dy+1) << 2 | (dx+1) is j's cell relative to (cx, cy, cz).
+// Both visit the same slots in the same order.
 template <bool CODES, class KP, class F>
 __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
                                                    int cx, int cy, int cz, F&& f) {
@@ -118,7 +118,8 @@ __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __res
             if constexpr (CODES) {
 #pragma unroll 1
                 for (int xc = xl; xc <= xh; xc++) {
-                    const unsigned code = (unsigned)((dz + 1) * 9 + (dy + 1) * 3 + (xc - cx + 1));
+                    const unsigned code =
+                        (unsigned)(((dz + 1) << 4) | ((dy + 1) << 2) | (xc - cx + 1));
                     const int j0 = max(__ldg(cs + row + xc), 0);
                     const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
                     for (int j = j0; j < j1; j++) f(j, code);
@@ -171,10 +172,9 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
                                         typename P::T& dy, typename P::T& dz) {
     using T = typename P::T;
     if constexpr (P::kMixed) {
-        const int rz = (int)(code / 9u) - 1;
-        const int rem = (int)(code % 9u);
-        const int ry = rem / 3 - 1;
-        const int rx = rem % 3 - 1;
+        const int rz = (int)(code >> 4) - 1;
+        const int ry = (int)((code >> 2) & 3u) - 1;
+        const int rx = (int)(code & 3u) - 1;
         dx = (pi.x - pj.x) - (T)rx * k.cell;
         dy = (pi.y - pj.y) - (T)ry * k.cell;
         dz = (pi.z - pj.z) - (T)rz * k.cell;

@@ -94,9 +94,9 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // the position i had when the list was built (cell-local offset in mixed precision).  The list
 // holds every pair closer than the list cutoff (KParams::kh2_list, the support radius plus a
 // skin), in candidate-walk order; count[i] > cap means the list overflowed for i and the
-// passes walk the cells for it instead.  Mixed precision stores with each slot, in bits 27-31,
-// the neighbour's cell relative to i's ((dz+1)*9 + (dy+1)*3 + (dx+1)), from which the passes
-// rebuild relative positions out of the cell-local offsets.
+// passes walk the cells for it instead.  Mixed precision stores with each slot, in bits 26-31,
+// the neighbour's cell relative to i's ((dz+1) << 4 | (dy+1) << 2 | (dx+1)), from which the
+// passes rebuild relative positions out of the cell-local offsets.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;

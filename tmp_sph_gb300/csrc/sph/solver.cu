@@ -547,8 +547,8 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
                           const float* p, const int* type, int n, int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
-    // mixed-precision list slots keep the neighbour index in 27 bits
-    if (c->prec == SPH_PREC_MIXED && n >= (1 << 27)) return SPH_ERR_ARG;
+    // mixed-precision list slots keep the neighbour index in 26 bits
+    if (c->prec == SPH_PREC_MIXED && n >= (1 << 26)) return SPH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     if (n != c->n) drop_graph(c);
     c->n = n;

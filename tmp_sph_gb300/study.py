@@ -2,8 +2,9 @@
 
 Runs the same seeded case in FP32, mixed precision and FP64 for `steps` steps, sampling the
 surge front (largest fluid x) and a wall pressure probe every `every` steps on the GPU, and
-reports the relative L2 difference of each precision's final fields (displacement, velocity,
-rho - rho0, p; fluid particles) and time series from the FP64 run of the same solver.
+reports the relative L2 difference of each precision's fields (displacement, velocity,
+rho - rho0, p; fluid particles) at checkpoints and at the end, and of the time series, from the
+FP64 run of the same solver.
 
     python -m tmp_sph_gb300.study --case precision --steps 5000 --every 50
 
@@ -30,7 +31,8 @@ def rel_l2(a, b, floor=0.0) -> float:
     return float(np.linalg.norm(a - b)) / den if den > 0 else float(np.linalg.norm(a - b))
 
 
-def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stream) -> dict:
+def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stream,
+                  checkpoints=()) -> dict:
     import torch
     n = len(st["rho"])
     probes = [(api.SPH_PROBE_FRONT, 0, 0, 0, 0, 0),
@@ -39,8 +41,12 @@ def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stre
     with S.Solver(p, n, precision=precision) as sol:
         sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         done = 0
+        snaps = {}
+        marks = sorted({c for c in checkpoints if 0 < c < steps})
         t0 = time.perf_counter()
         while True:
+            if done in marks:
+                snaps[done] = sol.download_f64(stream=stream)
             vals, stats = sol.probe(probes, stream=stream)
             series["t"].append(done * float(p.dt))
             series["front_x"].append(vals[0])
@@ -50,6 +56,9 @@ def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stre
             if done >= steps:
                 break
             k = min(every, steps - done)
+            nxt = [c for c in marks if c > done]
+            if nxt:
+                k = min(k, nxt[0] - done)
             sol.step(k, stream=stream)
             done += k
         torch.cuda.synchronize()
@@ -57,31 +66,39 @@ def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stre
         out = sol.download_f64(stream=stream)
         flags = sol.error_flags(stream=stream)
         rebuilds = sol.rebuild_count(stream=stream)
-    return {"fields": out, "series": series, "seconds": wall, "flags": flags,
+    snaps[steps] = out
+    return {"fields": out, "snaps": snaps, "series": series, "seconds": wall, "flags": flags,
             "rebuilds": rebuilds, "final_stats": stats}
 
 
-def compare(res: dict, ref: dict, st: dict) -> dict:
+def field_errors(a: dict, b: dict, st: dict) -> dict:
     fl = st["type"] == 1
     n_f = int(fl.sum())
-    a, b = res["fields"], ref["fields"]
-    sa, sb = res["series"], ref["series"]
     return {
         "disp": rel_l2(a["pos"][fl] - st["pos"][fl], b["pos"][fl] - st["pos"][fl]),
         "vel": rel_l2(a["vel"][fl], b["vel"][fl], floor=1e-3 * np.sqrt(n_f)),
         "drho": rel_l2(a["rho"][fl] - 1000.0, b["rho"][fl] - 1000.0),
         "p": rel_l2(a["p"][fl], b["p"][fl]),
-        "front_x_series": rel_l2(sa["front_x"], sb["front_x"]),
-        "wall_p_series": rel_l2(sa["wall_p"], sb["wall_p"]),
-        "kinetic_series": rel_l2(sa["kinetic"], sb["kinetic"]),
     }
 
 
-def study(case: str, steps: int, every: int, probe_xyz, precisions) -> dict:
+def compare(res: dict, ref: dict, st: dict) -> dict:
+    out = {f"step_{k}": field_errors(res["snaps"][k], ref["snaps"][k], st)
+           for k in sorted(res["snaps"]) if k in ref["snaps"]}
+    sa, sb = res["series"], ref["series"]
+    out["series"] = {
+        "front_x": rel_l2(sa["front_x"], sb["front_x"]),
+        "wall_p": rel_l2(sa["wall_p"], sb["wall_p"]),
+        "kinetic": rel_l2(sa["kinetic"], sb["kinetic"]),
+    }
+    return out
+
+
+def study(case: str, steps: int, every: int, probe_xyz, precisions, checkpoints=()) -> dict:
     import torch
     st, p = cases.build(case, physics="config")
     stream = torch.cuda.Stream()
-    runs = {prec: run_precision(st, p, prec, steps, every, probe_xyz, stream)
+    runs = {prec: run_precision(st, p, prec, steps, every, probe_xyz, stream, checkpoints)
             for prec in precisions}
     ref = runs.get("fp64")
     report = {"case": case, "particles": len(st["rho"]), "fluid": int((st["type"] == 1).sum()),
@@ -107,9 +124,12 @@ def main(argv=None) -> None:
     ap.add_argument("--every", type=int, default=50)
     ap.add_argument("--probe", type=float, nargs=3, default=(1.0, 0.25, 0.05))
     ap.add_argument("--precisions", nargs="+", default=["fp64", "fp32", "mixed"])
+    ap.add_argument("--compare-at", type=int, nargs="*", default=[1000],
+                    help="also compare the fields after these step counts")
     ap.add_argument("--out", default=None, help="also write the JSON here")
     args = ap.parse_args(argv)
-    rep = study(args.case, args.steps, args.every, tuple(args.probe), args.precisions)
+    rep = study(args.case, args.steps, args.every, tuple(args.probe), args.precisions,
+                args.compare_at)
     text = json.dumps(rep)
     if args.out:
         with open(args.out, "w") as f:

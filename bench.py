@@ -227,7 +227,7 @@ def run_reference(args):
 
 
 def config_block(args, p, n):
-    return {"workload": f"dam_break_{args.case}_fp32", "particles": n,
+    return {"workload": f"dam_break_{args.case}_{getattr(args, 'precision', 'fp32')}", "particles": n,
             "fluid_particles": n - p.num_boundary, "dx_m": p.dx, "h_over_dx": 1.3,
             "cells": p.num_cells, "eos": "tait", "dt_s": p.dt,
             "parallelism": f"replicas x{dist_env()[0]}",
@@ -249,6 +249,8 @@ def main():
     ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
                     help="rebuild kernels of the step graph under conditional nodes, or launched "
                          "every half step and returning at once when the lists are kept")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "fp64"],
+                    help="precision of the timed solver (the other two are timed beside it)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -268,7 +270,7 @@ def main():
     st, p = build_case(args.case)
     n = len(st["rho"])
     stream = torch.cuda.Stream()
-    sol = S.Solver(p, n)
+    sol = S.Solver(p, n, precision=args.precision)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
@@ -333,8 +335,8 @@ def main():
         v.close()
         return out
 
-    variants = {"mixed": time_precision("mixed", min(args.steps, 50)),
-                "fp64": time_precision("fp64", min(args.steps, 10))}
+    variants = {prec: time_precision(prec, min(args.steps, 10 if prec == "fp64" else 50))
+                for prec in ("fp32", "mixed", "fp64") if prec != args.precision}
 
     # per-kernel device time from CUDA events around every phase, same stream
     prof_steps = min(args.steps, 20)
@@ -393,7 +395,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "mixed": "f32+f64", "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
         "config": config_block(args, p, n),
         "hbm_gbs_algorithmic": value / ws * b_alg / 1e9,

@@ -249,7 +249,7 @@ def main():
     ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
                     help="rebuild kernels of the step graph under conditional nodes, or launched "
                          "every half step and returning at once when the lists are kept")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "fp64"],
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "mixed_comp", "fp64"],
                     help="precision of the timed solver (the other two are timed beside it)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
@@ -336,7 +336,7 @@ def main():
         return out
 
     variants = {prec: time_precision(prec, min(args.steps, 10 if prec == "fp64" else 50))
-                for prec in ("fp32", "mixed", "fp64") if prec != args.precision}
+                for prec in ("fp32", "mixed", "mixed_comp", "fp64") if prec != args.precision}
 
     # per-kernel device time from CUDA events around every phase, same stream
     prof_steps = min(args.steps, 20)
@@ -396,7 +396,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "mixed": "f32+f64", "fp64": "f64"}[args.precision],
+        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+                  "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
         "config": config_block(args, p, n),
         "hbm_gbs_algorithmic": value / ws * b_alg / 1e9,

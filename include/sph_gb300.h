@@ -252,9 +252,10 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */
 #define SPH_PREC_FP64  1  /* FP64 state and arithmetic: the accuracy reference for the others */
 #define SPH_PREC_MIXED 2  /* FP32 neighbour sums on relative positions rebuilt from cell-local
-                             offsets, compensated density and force sums; FP64 positions and
-                             density perturbation (rho - rho0) for the time integration;
-                             n < 2^26 */
+                             offsets; FP64 positions and density perturbation (rho - rho0) for
+                             the time integration; n < 2^26 */
+#define SPH_PREC_MIXED_COMP 3  /* SPH_PREC_MIXED with compensated (Neumaier) accumulation of the
+                             density and force sums */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
  * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;

@@ -69,14 +69,15 @@ def test_fp64_matches_fp64_oracle(sphlib, oracle, cuda, report, physics):
 def test_fp32_and_mixed_against_fp64(sphlib, cuda, report):
     """1000 steps of the small dam break (27,288 particles): FP32 and mixed precision against
     the FP64 run of the same solver, relative L2 of displacement, velocity, rho - rho0, p
-    (measured: FP32 3e-5 / 9e-5 / 4e-4 / 4e-4, mixed 1e-6 / 3e-6 / 1.3e-5 / 1.3e-5)."""
+    (measured: FP32 3e-5 / 9e-5 / 4e-4 / 4e-4, mixed 1e-6 / 3e-6 / 1.3e-5 / 1.3e-5 with
+    compensated sums)."""
     from tmp_sph_gb300 import cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
     steps = 1000
     ref = run_prec(st, p, steps, "fp64")
     assert ref["flags"] == 0
     res = {}
-    for prec in ("fp32", "mixed"):
+    for prec in ("fp32", "mixed", "mixed_comp"):
         out = run_prec(st, p, steps, prec)
         assert out["flags"] == 0, prec
         res[prec] = errors(out["f64"], ref["f64"], st)

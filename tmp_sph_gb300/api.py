@@ -41,8 +41,9 @@ SPH_OPT_NEIGHBOR_CAP = 5
 SPH_OPT_SKIN_PERMILLE = 6
 SPH_OPT_CONDITIONAL_GRAPH = 7
 SPH_OPT_PRECISION = 8
-SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED = 0, 1, 2
-PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED}
+SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
+PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
+              "mixed_comp": SPH_PREC_MIXED_COMP}
 SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
 SPH_PHASE_COUNT = 5
 PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")

@@ -36,24 +36,36 @@ cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
 //  PrecF32 — FP32 state and arithmetic (the reference's precision; the drop-in path).
 //  PrecF64 — FP64 state and arithmetic: the accuracy reference every result is measured
 //            against ("an FP64 run of the same solver").
-//  PrecMix — FP32 neighbour sums on relative positions rebuilt from cell-local offsets, with
-//            compensated (Neumaier) accumulation of the density and force sums; FP64 master
-//            positions and density perturbation rho - rho0 for the integration.
+//  PrecMix — FP32 neighbour sums on relative positions rebuilt from cell-local offsets; FP64
+//            master positions and density perturbation rho - rho0 for the integration.
+//  PrecMixC — PrecMix with compensated (Neumaier) accumulation of the density and force sums.
 struct PrecF32 {
     using T = float;
     static constexpr bool kMixed = false;
+    static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_FP32;
 };
 struct PrecF64 {
     using T = double;
     static constexpr bool kMixed = false;
+    static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_FP64;
 };
 struct PrecMix {
     using T = float;
     static constexpr bool kMixed = true;
+    static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_MIXED;
 };
+struct PrecMixC {
+    using T = float;
+    static constexpr bool kMixed = true;
+    static constexpr bool kComp = true;
+    static constexpr int kId = SPH_PREC_MIXED_COMP;
+};
+inline bool prec_is_mixed(int prec) {
+    return prec == SPH_PREC_MIXED || prec == SPH_PREC_MIXED_COMP;
+}
 
 // ---------------------------------------------------------------- resident state
 // One particle set.  rec holds two vec4 per particle, rec[2i] = (x, y, z, p) and

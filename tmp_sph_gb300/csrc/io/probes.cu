@@ -238,6 +238,7 @@ void probe_results(const double* acc, const sph_probe* probes, int nprobes, doub
 SPH_PROBE_INSTANTIATE(PrecF32)
 SPH_PROBE_INSTANTIATE(PrecF64)
 SPH_PROBE_INSTANTIATE(PrecMix)
+SPH_PROBE_INSTANTIATE(PrecMixC)
 #undef SPH_PROBE_INSTANTIATE
 
 }  // namespace sph

@@ -722,6 +722,7 @@ cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
 SPH_MESH_INSTANTIATE(PrecF32)
 SPH_MESH_INSTANTIATE(PrecF64)
 SPH_MESH_INSTANTIATE(PrecMix)
+SPH_MESH_INSTANTIATE(PrecMixC)
 #undef SPH_MESH_INSTANTIATE
 
 cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,

@@ -95,7 +95,7 @@ cudaError_t alloc_state(sph_ctx* c) {
         if ((e = alloc_set(c->yd, cap, false)) != cudaSuccess) return e;
         return alloc_p1(c->p1d, cap);
     }
-    const bool mixed = c->prec == SPH_PREC_MIXED;
+    const bool mixed = prec_is_mixed(c->prec);
     if ((e = alloc_set(c->x, cap, mixed)) != cudaSuccess) return e;
     if ((e = alloc_set(c->y, cap, mixed)) != cudaSuccess) return e;
     return alloc_p1(c->p1, cap);
@@ -119,6 +119,7 @@ auto with_prec(const sph_ctx* c, F&& f) {
     switch (c->prec) {
         case SPH_PREC_FP64: return f(PrecF64{});
         case SPH_PREC_MIXED: return f(PrecMix{});
+        case SPH_PREC_MIXED_COMP: return f(PrecMixC{});
         default: return f(PrecF32{});
     }
 }
@@ -495,7 +496,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_PRECISION: {
-            if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && value != SPH_PREC_MIXED)
+            if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && !prec_is_mixed(value))
                 return SPH_ERR_ARG;
             if (value == c->prec) return SPH_OK;
             drop_graph(c);
@@ -548,7 +549,7 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
     // mixed-precision list slots keep the neighbour index in 26 bits
-    if (c->prec == SPH_PREC_MIXED && n >= (1 << 26)) return SPH_ERR_ARG;
+    if (prec_is_mixed(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     if (n != c->n) drop_graph(c);
     c->n = n;

@@ -285,6 +285,20 @@ int sph_ns(sph_ctx* ctx, float* s_pos, float* s_vel, float* s_rho, float* s_p,
  * host (from_host = 1) or device memory.  Resets the step counter. */
 int sph_upload(sph_ctx* ctx, const float* pos, const float* vel, const float* rho,
                const float* p, const int* type, int n, int from_host, void* stream);
+/* Batched instances (no reference counterpart): n particles of n_inst independent simulations
+ * that share this context's sph_params (same tank, grid and constants), each in its own
+ * coordinates; instance b owns particles [offsets[b], offsets[b+1]) of the arrays (`offsets`:
+ * host array of n_inst + 1 ints, offsets[0] = 0, offsets[n_inst] = n).  Every kernel then
+ * advances all instances in one launch.  The solver's grid stacks the instances along z with an
+ * empty cell layer between them, so no neighbour search crosses instances and each instance
+ * evolves exactly as it would alone.  Allocates when the stacked grid needs more cells than the
+ * context holds.  sph_download returns all n particles in upload order; sph_probe_read reduces
+ * over all instances.  sph_upload returns the context to one simulation. */
+#define SPH_MAX_INSTANCES 4096
+int sph_upload_instances(sph_ctx* ctx, const float* pos, const float* vel, const float* rho,
+                         const float* p, const int* type, const int* offsets, int n_inst, int n,
+                         int from_host, void* stream);
+int sph_instances(const sph_ctx* ctx, int* n_inst);
 /* Write the current state back in original order; any pointer may be NULL. */
 int sph_download(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
                  int to_host, void* stream);

@@ -161,6 +161,8 @@ _PROTOS = {
     "sph_ctx_set_option": (_I, [_P, _I, _I]),
     "sph_ns": (_I, [_P] + [_P] * 9 + [_I] + [_P] * 4 + [_P]),
     "sph_upload": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "sph_upload_instances": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _P]),
+    "sph_instances": (_I, [_P, C.POINTER(_I)]),
     "sph_download": (_I, [_P, _P, _P, _P, _P, _P, _I, _P]),
     "sph_download_f64": (_I, [_P, _P, _P, _P, _P, _I, _P]),
     "sph_step": (_I, [_P, _I, _P]),

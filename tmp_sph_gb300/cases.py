@@ -11,6 +11,10 @@ Geometries are the five benchmark workloads of this project:
   refcase    the reference's own hard-coded tank 3.221 x 1 x 1, water 1.228 x 1 x 0.55
              (src/sph/sph_run.cu:11-13) at a chosen dx
 
+and batch(): 64 independent dam breaks in the 1.0 x 0.5 x 0.6 m tank at dx 0.005, water blocks
+of width U[0.2, 0.6] m and height U[0.15, 0.45] m (about 120k-1.08M fluid particles each,
+49M particles in all) for the batched solver.
+
 Physics variants:
 
   "config"     h = 1.3 dx, rho0 1000, c0 = 10 sqrt(2 g 0.3), Tait gamma 7, delta 0.1,
@@ -109,6 +113,36 @@ def config(d: api.SphDamBreak, physics: str = "config", n: int = 0, nb: int = 0,
     c.num_boundary = nb
     c.clamp_density = 1
     return c
+
+
+def batch(n_inst: int = 64, *, seed: int = 20240611, dx: float = 0.005,
+          tank=(1.0, 0.5, 0.6), width=(0.2, 0.6), height=(0.15, 0.45),
+          jitter: float = 0.0) -> tuple[list, api.SphParams]:
+    """Independent dam breaks for one batched solver: the same tank, water blocks of width
+    U[width] and height U[height] drawn from `seed` (full tank breadth, at x = 0).  They share
+    one parameter set, so the speed of sound is set by the tallest column,
+    c0 = 10 sqrt(2 g H_max), and dt = 0.25 h / c0 for all.  Returns (states, params)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    widths = rng.uniform(width[0], width[1], n_inst)
+    heights = rng.uniform(height[0], height[1], n_inst)
+    cs = 10.0 * math.sqrt(2.0 * 9.81 * float(heights.max()))
+    states, nb = [], 0
+    d = None
+    for b in range(n_inst):
+        d = geometry("precision", dx=dx, tank=tank, block=(float(widths[b]), tank[1],
+                                                         float(heights[b])),
+                     jitter=jitter, seed=seed + b)
+        d.cs = cs
+        st = api.dam_break_generate(d)
+        st["geometry"] = d
+        st["block"] = (float(widths[b]), float(heights[b]))
+        states.append(st)
+        nb += st["n_boundary"]
+    n = sum(len(st["rho"]) for st in states)
+    c = config(d, "config", n, nb)
+    c.cs = cs
+    return states, api.params_derive(c)
 
 
 def build(name: str, physics: str = "config", **kw) -> tuple[dict, api.SphParams]:

@@ -486,8 +486,10 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
             out.txm[i] = txm;
             out.tvel[i] = tv;
         }
+        const int inst = in.inst ? in.inst[i] : 0;
+        if (out.inst) out.inst[i] = inst;
         unsigned f = 0;
-        out_hash[i] = (unsigned)cell_hash_clamped(k, nxm.x, nxm.y, nxm.z, &f);
+        out_hash[i] = resident_key(k, inst, nxm.x, nxm.y, nxm.z, &f);
         raise_flags(err, f);
         if (!fi || !nl.xb) return 0.f;
         const float4 xb = nl.xb[i];
@@ -553,8 +555,10 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
             out.tpos[i] = tp;
             out.tvel[i] = tv;
         }
+        const int inst = in.inst ? in.inst[i] : 0;
+        if (out.inst) out.inst[i] = inst;
         unsigned f = 0;
-        out_hash[i] = (unsigned)cell_hash_clamped(k, np.x, np.y, np.z, &f);
+        out_hash[i] = resident_key(k, inst, np.x, np.y, np.z, &f);
         raise_flags(err, f);
         if (!fi || !nl.xb) return 0.f;
         const float4 xb = nl.xb[i];

@@ -41,6 +41,11 @@ struct KParamsT {
     int n;
     int gx, gy, gz;      // grid dimensions
     int num_cells;
+    // Batched instances are stacked along z, each gz_local cells high plus one empty layer,
+    // so the resident key of a particle of instance b is b * inst_cells + its cell in its own
+    // grid.  A single simulation has gz_local = gz and inst_cells = 0.
+    int gz_local;
+    int inst_cells;
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
     T h, inv_h, kh, kh2;
@@ -96,20 +101,22 @@ __device__ __forceinline__ void cell_of_key(int gx, int gy, unsigned key, int& c
 }
 
 // Origin of a cell of the (float) grid, in double: the frame of the mixed-precision offsets.
+// `key` is a resident key; the origin is in the coordinates of the particle's own instance.
 template <class KT>
 __device__ __forceinline__ void cell_origin(const KParamsT<KT>& k, unsigned key, double& ox,
                                             double& oy, double& oz) {
     int cx, cy, cz;
     cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+    if (k.inst_cells) cz %= k.gz_local + 1;
     ox = (double)k.gmin_x + (double)cx * (double)k.cell;
     oy = (double)k.gmin_y + (double)cy * (double)k.cell;
     oz = (double)k.gmin_z + (double)cz * (double)k.cell;
 }
 
 // Hash used by the resident solver: identical to the reference for in-grid positions; an
-// out-of-grid or non-finite position is clamped into the grid and reported through `flag`.
-// KT is the constant block's real type, PT the position's (a mixed-precision solver hashes its
-// double positions on the float grid, in double).
+// out-of-grid or non-finite position is clamped into the grid (of one instance) and reported
+// through `flag`.  KT is the constant block's real type, PT the position's (a mixed-precision
+// solver hashes its double positions on the float grid, in double).
 template <class KT, class PT>
 __device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT y, PT z,
                                                  unsigned* flag) {
@@ -123,13 +130,20 @@ __device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT
     int cy = cell_coord(y, (PT)k.gmin_y, (PT)k.cell);
     int cz = cell_coord(z, (PT)k.gmin_z, (PT)k.cell);
     if ((unsigned)cx >= (unsigned)k.gx || (unsigned)cy >= (unsigned)k.gy ||
-        (unsigned)cz >= (unsigned)k.gz) {
+        (unsigned)cz >= (unsigned)k.gz_local) {
         *flag |= SPH_FLAG_OUT_OF_GRID;
         cx = clampi(cx, 0, k.gx - 1);
         cy = clampi(cy, 0, k.gy - 1);
-        cz = clampi(cz, 0, k.gz - 1);
+        cz = clampi(cz, 0, k.gz_local - 1);
     }
     return (cz * k.gy + cy) * k.gx + cx;
+}
+
+// Resident key of a particle of instance `inst` (0 for a single simulation).
+template <class KT, class PT>
+__device__ __forceinline__ unsigned resident_key(const KParamsT<KT>& k, int inst, PT x, PT y, PT z,
+                                                 unsigned* flag) {
+    return (unsigned)cell_hash_clamped(k, x, y, z, flag) + (unsigned)inst * (unsigned)k.inst_cells;
 }
 
 // ---------------------------------------------------------------- equation of state

@@ -86,6 +86,7 @@ struct ParticleSetT {
     vec4_t<T>* tvel = nullptr;
     dvec4* xm = nullptr;
     dvec4* txm = nullptr;
+    int* inst = nullptr;  // batched instances: the particle's instance (0 for one simulation)
 };
 using ParticleSet = ParticleSetT<float>;
 
@@ -164,11 +165,14 @@ cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,
 template <class P>
 cudaError_t launch_rehash(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& set,
                           unsigned* hash, unsigned* err, cudaStream_t s);
+// inst_off (device, n_inst + 1 entries; may be NULL for one simulation): instance b owns
+// particles [inst_off[b], inst_off[b+1]).
 template <class P>
 cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float* pos,
                                   const float* vel, const float* rho, const float* p,
-                                  const int* type, ParticleSetT<typename P::T> dst,
-                                  unsigned* hash, unsigned* err, cudaStream_t s);
+                                  const int* type, const int* inst_off, int n_inst,
+                                  ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
+                                  cudaStream_t s);
 template <class P>
 cudaError_t launch_download_convert(const KParamsT<typename P::T>& k,
                                     const ParticleSetT<typename P::T>& src, float* pos,
@@ -228,7 +232,10 @@ struct sph_ctx {
     // neighbour list, reused across half steps while every particle stays within skin/2 of
     // where it was when the list was built
     sph::NbrList nl;
-    sph_params Pi{};                 // internal grid: cells of kh (1 + skin)
+    sph_params Pi{};                 // internal grid: cells of kh (1 + skin), instances stacked
+    int n_inst = 1;                  // batched instances (sph_upload_instances)
+    int gz_inst = 0;                 // grid height of one instance
+    int* inst_off = nullptr;         // [SPH_MAX_INSTANCES + 1] instance particle offsets
     double skin = 0.1;               // list skin as a fraction of the support radius kh
     unsigned* rb = nullptr;          // [0] rebuild gate, [1] max squared displacement (float
                                      // bits), [2] forced rebuild, [3] rebuild count

@@ -420,13 +420,26 @@ __global__ void k_gather(KParamsT<typename P::T> kp, const int* __restrict__ per
     dst.xyz[k] = make4<T>(a.x, a.y, a.z, b.w > T(0) ? T(1) : T(-1));
     dst.type[k] = src.type[s];
     dst.id[k] = src.id[s];
+    if (src.inst && dst.inst) dst.inst[k] = src.inst[s];
     if (with_tmp) dst.tvel[k] = src.tvel[s];
+}
+
+// Instance of particle i when instance b owns [off[b], off[b+1]) (upper bound search).
+__device__ __forceinline__ int instance_of(const int* __restrict__ off, int n_inst, int i) {
+    if (!off || n_inst <= 1) return 0;
+    int lo = 0, hi = n_inst;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
 template <class P>
 __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __restrict__ pos,
                                  const float* __restrict__ vel, const float* __restrict__ rho,
                                  const float* __restrict__ p, const int* __restrict__ type,
+                                 const int* __restrict__ inst_off, int n_inst,
                                  ParticleSetT<typename P::T> dst, unsigned* __restrict__ hash,
                                  unsigned* err) {
     using T = typename P::T;
@@ -435,14 +448,16 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
     const float vx = vel[3 * i], vy = vel[3 * i + 1], vz = vel[3 * i + 2];
     const int t = type[i];
+    const int inst = instance_of(inst_off, n_inst, i);
     unsigned f = 0;
     dst.type[i] = t;
     dst.id[i] = i;
+    if (dst.inst) dst.inst[i] = inst;
     dst.tvel[i] = make4<T>(vx, vy, vz, T(0));
     dst.rec[2 * (size_t)i + 1] = make4<T>(vx, vy, vz, signed_rho_t<T>(t, (T)rho[i]));
     if constexpr (P::kMixed) {
         const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[i] - (double)kp.rho0};
-        const unsigned h = (unsigned)cell_hash_clamped(kp, xm.x, xm.y, xm.z, &f);
+        const unsigned h = resident_key(kp, inst, xm.x, xm.y, xm.z, &f);
         dst.xm[i] = xm;
         dst.txm[i] = xm;
         dst.rec[2 * (size_t)i] = offsets_in_cell(kp, h, xm, p[i]);
@@ -450,7 +465,7 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     } else {
         dst.rec[2 * (size_t)i] = make4<T>(x, y, z, (T)p[i]);
         dst.tpos[i] = make4<T>(x, y, z, (T)rho[i]);
-        hash[i] = (unsigned)cell_hash_clamped(kp, (T)x, (T)y, (T)z, &f);
+        hash[i] = resident_key(kp, inst, (T)x, (T)y, (T)z, &f);
     }
     raise_flags(err, f);
 }
@@ -462,12 +477,13 @@ __global__ void k_rehash(KParamsT<typename P::T> kp, ParticleSetT<typename P::T>
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     unsigned f = 0;
+    const int inst = set.inst ? set.inst[i] : 0;
     if constexpr (P::kMixed) {
         const dvec4 q = set.xm[i];
-        hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+        hash[i] = resident_key(kp, inst, q.x, q.y, q.z, &f);
     } else {
         const auto q = set.xyz[i];
-        hash[i] = (unsigned)cell_hash_clamped(kp, q.x, q.y, q.z, &f);
+        hash[i] = resident_key(kp, inst, q.x, q.y, q.z, &f);
     }
     raise_flags(err, f);
 }
@@ -668,11 +684,12 @@ cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,
 template <class P>
 cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float* pos,
                                   const float* vel, const float* rho, const float* p,
-                                  const int* type, ParticleSetT<typename P::T> dst,
-                                  unsigned* hash, unsigned* err, cudaStream_t s) {
+                                  const int* type, const int* inst_off, int n_inst,
+                                  ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
+                                  cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    k_upload_convert<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, dst, hash,
-                                                             err);
+    k_upload_convert<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, inst_off,
+                                                             n_inst, dst, hash, err);
     return cudaGetLastError();
 }
 
@@ -712,8 +729,9 @@ cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
                                           const unsigned*, cudaStream_t, const unsigned*);      \
     template cudaError_t launch_upload_convert<P>(const KParamsT<P::T>&, const float*,          \
                                                   const float*, const float*, const float*,     \
-                                                  const int*, ParticleSetT<P::T>, unsigned*,    \
-                                                  unsigned*, cudaStream_t);                     \
+                                                  const int*, const int*, int,                  \
+                                                  ParticleSetT<P::T>, unsigned*, unsigned*,     \
+                                                  cudaStream_t);                                \
     template cudaError_t launch_rehash<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&,     \
                                           unsigned*, unsigned*, cudaStream_t);                  \
     template cudaError_t launch_download_convert<P>(const KParamsT<P::T>&,                      \

@@ -32,6 +32,8 @@ KParams make_kparams(const sph_params& p, int n) {
     k.gy = p.grid_dim[1];
     k.gz = p.grid_dim[2];
     k.num_cells = p.num_cells;
+    k.gz_local = p.grid_dim[2];
+    k.inst_cells = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
@@ -86,6 +88,8 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.gy = p.grid_dim[1];
     k.gz = p.grid_dim[2];
     k.num_cells = p.num_cells;
+    k.gz_local = p.grid_dim[2];
+    k.inst_cells = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];

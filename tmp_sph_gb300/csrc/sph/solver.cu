@@ -43,7 +43,7 @@ cudaError_t dalloc(T** p, size_t count) {
 template <class T>
 void free_set(ParticleSetT<T>& s) {
     cudaFree(s.rec); cudaFree(s.xyz); cudaFree(s.type); cudaFree(s.id);
-    cudaFree(s.tpos); cudaFree(s.tvel); cudaFree(s.xm); cudaFree(s.txm);
+    cudaFree(s.tpos); cudaFree(s.tvel); cudaFree(s.xm); cudaFree(s.txm); cudaFree(s.inst);
     s = ParticleSetT<T>{};
 }
 
@@ -56,6 +56,7 @@ cudaError_t alloc_set(ParticleSetT<T>& s, int cap, bool mixed) {
     if ((e = dalloc(&s.id, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tpos, cap)) != cudaSuccess) return e;
     if ((e = dalloc(&s.tvel, cap)) != cudaSuccess) return e;
+    if ((e = dalloc(&s.inst, cap)) != cudaSuccess) return e;
     if (mixed) {
         if ((e = dalloc(&s.xm, cap)) != cudaSuccess) return e;
         if ((e = dalloc(&s.txm, cap)) != cudaSuccess) return e;
@@ -144,6 +145,8 @@ void release(sph_ctx* c) {
     c->rb = nullptr;
     cudaFree(c->probe_acc);
     c->probe_acc = nullptr;
+    cudaFree(c->inst_off);
+    c->inst_off = nullptr;
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -207,9 +210,29 @@ sph_params internal_params(const sph_params& P, double skin) {
     return Q;
 }
 
+// The solver's grid for n_inst batched instances: the instances' grids stacked along z, one
+// empty cell layer between consecutive instances, so no 27-cell walk reaches another instance.
+// *gz_local receives the height of one instance's grid.  Returns false when the stacked grid
+// does not fit the key range.
+bool stacked_params(const sph_params& P, double skin, int n_inst, sph_params* out, int* gz_local) {
+    sph_params Q = internal_params(P, skin);
+    *gz_local = Q.grid_dim[2];
+    if (n_inst > 1) {
+        const long long gz = (long long)n_inst * (Q.grid_dim[2] + 1);
+        const long long cells = (long long)Q.grid_dim[0] * Q.grid_dim[1] * gz;
+        if (cells >= (1LL << 30)) return false;
+        Q.grid_dim[2] = (int)gz;
+        Q.num_cells = (int)cells;
+    }
+    *out = Q;
+    return true;
+}
+
 template <class T>
 KParamsT<T> resident_kparams(const sph_ctx* c) {
     KParamsT<T> k = make_kparams_t<T>(c->Pi, c->n);
+    k.gz_local = c->gz_inst;
+    k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
@@ -409,7 +432,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     sph_ctx* c = new (std::nothrow) sph_ctx();
     if (!c) return SPH_ERR_NOMEM;
     c->P = *p;
-    c->Pi = internal_params(*p, c->skin);
+    stacked_params(*p, c->skin, 1, &c->Pi, &c->gz_inst);
     c->capacity = capacity;
     cudaGetDevice(&c->device);
     cudaError_t e = cudaSuccess;
@@ -425,6 +448,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = dalloc(&c->err, 1);
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = dalloc(&c->probe_acc, probe_acc_words());
+    if (e == cudaSuccess) e = dalloc(&c->inst_off, SPH_MAX_INSTANCES + 1);
     if (e == cudaSuccess) e = dalloc(&c->rb, 4);
     if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
@@ -466,10 +490,13 @@ static cudaError_t ensure_cells(sph_ctx* c, int cells) {
 
 extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     if (!c || !params_ok(p)) return SPH_ERR_ARG;
-    const sph_params pi = internal_params(*p, c->skin);
+    sph_params pi;
+    int gz_local;
+    if (!stacked_params(*p, c->skin, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
     if (ensure_cells(c, std::max(p->num_cells, pi.num_cells)) != cudaSuccess) return SPH_ERR_NOMEM;
     c->P = *p;
     c->Pi = pi;
+    c->gz_inst = gz_local;
     c->rehash = c->loaded;
     drop_graph(c);
     // and the neighbour list, when the support radius holds more lattice neighbours
@@ -526,10 +553,14 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
                 c->opt_nbr_cap = value;
             } else {
                 if (c->P.num_cells <= 0) return SPH_ERR_STATE;
-                const sph_params pi = internal_params(c->P, value / 1000.0);
+                sph_params pi;
+                int gz_local;
+                if (!stacked_params(c->P, value / 1000.0, c->n_inst, &pi, &gz_local))
+                    return SPH_ERR_ARG;
                 if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
                 c->skin = value / 1000.0;
                 c->Pi = pi;
+                c->gz_inst = gz_local;
                 c->rehash = c->loaded;
             }
             drop_graph(c);
@@ -544,13 +575,34 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
     return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
-extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const float* rho,
-                          const float* p, const int* type, int n, int from_host, void* stream) {
+// Upload n particles of n_inst instances (offsets: host array of n_inst + 1, NULL for one).
+static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const float* rho,
+                       const float* p, const int* type, const int* offsets, int n_inst, int n,
+                       int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
     // mixed-precision list slots keep the neighbour index in 26 bits
     if (prec_is_mixed(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
+    if (n_inst < 1 || n_inst > SPH_MAX_INSTANCES) return SPH_ERR_ARG;
+    if (n_inst > 1) {
+        if (!offsets || offsets[0] != 0 || offsets[n_inst] != n) return SPH_ERR_ARG;
+        for (int b = 0; b < n_inst; b++)
+            if (offsets[b + 1] < offsets[b]) return SPH_ERR_ARG;
+    }
     cudaStream_t s = (cudaStream_t)stream;
+    if (n_inst != c->n_inst) {
+        sph_params pi;
+        int gz_local;
+        if (!stacked_params(c->P, c->skin, n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
+        if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
+        c->Pi = pi;
+        c->gz_inst = gz_local;
+        c->n_inst = n_inst;
+        drop_graph(c);
+    }
+    if (n_inst > 1 && cudaMemcpyAsync(c->inst_off, offsets, (size_t)(n_inst + 1) * sizeof(int),
+                                      cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return SPH_ERR_CUDA;
     if (n != c->n) drop_graph(c);
     c->n = n;
     c->steps = 0;
@@ -586,8 +638,27 @@ extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const 
     return to_status(with_prec(c, [&](auto tag) {
         using P = decltype(tag);
         return launch_upload_convert<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho, dp,
-                                        dtype, State<P>::y(c), c->hash_x, c->err, s);
+                                        dtype, n_inst > 1 ? c->inst_off : nullptr, n_inst,
+                                        State<P>::y(c), c->hash_x, c->err, s);
     }));
+}
+
+extern "C" int sph_upload(sph_ctx* c, const float* pos, const float* vel, const float* rho,
+                          const float* p, const int* type, int n, int from_host, void* stream) {
+    return upload_impl(c, pos, vel, rho, p, type, nullptr, 1, n, from_host, stream);
+}
+
+extern "C" int sph_upload_instances(sph_ctx* c, const float* pos, const float* vel,
+                                    const float* rho, const float* p, const int* type,
+                                    const int* offsets, int n_inst, int n, int from_host,
+                                    void* stream) {
+    return upload_impl(c, pos, vel, rho, p, type, offsets, n_inst, n, from_host, stream);
+}
+
+extern "C" int sph_instances(const sph_ctx* c, int* n_inst) {
+    if (!c || !n_inst) return SPH_ERR_ARG;
+    *n_inst = c->n_inst;
+    return SPH_OK;
 }
 
 extern "C" int sph_download(sph_ctx* c, float* pos, float* vel, float* rho, float* p, int* type,

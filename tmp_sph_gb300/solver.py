@@ -70,6 +70,24 @@ class Solver:
             torch.cuda.synchronize()
         self.n = n
 
+    def upload_instances(self, states: list, stream=None) -> np.ndarray:
+        """Upload several independent simulations (host state dicts sharing this solver's
+        parameters); returns the particle offsets of the instances."""
+        import torch
+        counts = [len(s["rho"]) for s in states]
+        off = np.zeros(len(states) + 1, np.int32)
+        off[1:] = np.cumsum(counts)
+        cat = {k: np.ascontiguousarray(np.concatenate([s[k] for s in states]),
+                                       np.int32 if k == "type" else np.float32)
+               for k in ("pos", "vel", "rho", "p", "type")}
+        n = int(off[-1])
+        call("sph_upload_instances", self.handle, ptr(cat["pos"]), ptr(cat["vel"]),
+             ptr(cat["rho"]), ptr(cat["p"]), ptr(cat["type"]), ptr(off), len(states), n, 1,
+             _stream(stream))
+        torch.cuda.synchronize()
+        self.n = n
+        return off
+
     def step(self, nsteps: int = 1, stream=None) -> None:
         call("sph_step", self.handle, nsteps, _stream(stream))
 

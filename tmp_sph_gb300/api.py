@@ -115,6 +115,7 @@ class SphDamBreak(C.Structure):
     ]
 
 
+SPH_MAX_INSTANCES = 4096
 SPH_PROBE_PRESSURE, SPH_PROBE_HEIGHT, SPH_PROBE_FRONT = 0, 1, 2
 SPH_MAX_PROBES = 32
 

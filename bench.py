@@ -247,9 +247,16 @@ def run_batch(args):
     states, p = cases.batch(n_inst)
     n = sum(len(st["rho"]) for st in states)
     stream = torch.cuda.Stream()
+    tuned = None
+    if args.autotune:
+        from tmp_sph_gb300 import autotune
+        tuned = autotune.tune(p, states, precision=args.precision)
+        args.skin = tuned["skin_permille"]
     sol = S.Solver(p, n, precision=args.precision)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+    if tuned:
+        autotune.apply(sol, tuned)
     sol.upload_instances(states, stream=stream)
     sol.step(args.warmup, stream=stream)
     torch.cuda.synchronize()
@@ -279,6 +286,7 @@ def run_batch(args):
                    "neighbour_list_skin_over_kh": args.skin / 1000.0,
                    "graph_mode": args.graph_mode},
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps},
+        "autotune": autotune.summary(tuned) if tuned else None,
         "gpu_launches": count_launches(sol_cells_batch(p, n_inst, args.skin), 2 * args.steps,
                                        rebuilds, args.graph_mode),
         "clocks": clk.summary(),
@@ -310,6 +318,9 @@ def main():
                          "every half step and returning at once when the lists are kept")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "mixed_comp", "fp64"],
                     help="precision of the timed solver (the other two are timed beside it)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick threads per block, particles per thread and skin with the "
+                         "autotuner first (overrides --skin)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -331,9 +342,16 @@ def main():
     st, p = build_case(args.case)
     n = len(st["rho"])
     stream = torch.cuda.Stream()
+    tuned = None
+    if args.autotune:
+        from tmp_sph_gb300 import autotune
+        tuned = autotune.tune(p, st, precision=args.precision)
+        args.skin = tuned["skin_permille"]
     sol = S.Solver(p, n, precision=args.precision)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+    if tuned:
+        autotune.apply(sol, tuned)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
 
     def barrier():
@@ -473,6 +491,7 @@ def main():
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
                           "skin_permille": args.skin},
         "rebuild_every_half_step": no_reuse,
+        "autotune": autotune.summary(tuned) if tuned else None,
         "precision_variants": variants,
         "clocks": clk.summary(),
         "device_error_flags": flags,

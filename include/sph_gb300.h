@@ -247,6 +247,10 @@ typedef struct sph_ctx sph_ctx;
                                     conditional nodes) */
 #define SPH_OPT_PRECISION     8  /* SPH_PREC_* below; set before sph_upload (the state is
                                     reallocated; the uploaded state is dropped) */
+#define SPH_OPT_BLOCK_THREADS 9  /* threads per block of the neighbour kernels: 32..256, a
+                                    multiple of 32 (default 128) */
+#define SPH_OPT_PARTICLES_PER_THREAD 10  /* particles each thread of the neighbour kernels
+                                    handles, grid-stride (1..64, default 1) */
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */

@@ -315,3 +315,33 @@ def test_large_case_properties(sphlib, cuda, report):
     occ = np.unique(keys)
     assert (cs[occ + 1] - cs[occ] == np.bincount(keys, minlength=ncells)[occ]).all()
     report("large 5 steps max |v|", float(np.abs(out["vel"][fl]).max()))
+
+
+@pytest.mark.parametrize("threads,ppt", [(64, 1), (256, 1), (128, 2), (96, 4)])
+def test_launch_shape_is_bitwise_neutral(sphlib, cuda, threads, ppt):
+    """Threads per block and particles per thread of the neighbour kernels change only the
+    launch shape: each particle's arithmetic and order are the same, so are the bits."""
+    from tmp_sph_gb300 import api, cases
+    from gpu_util import perturbed
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    st = perturbed(st, vamp=2.0, ramp=0.0)
+    a, fa = run_opts(st, p, 6, {})
+    b, fb = run_opts(st, p, 6, {api.SPH_OPT_BLOCK_THREADS: threads,
+                                api.SPH_OPT_PARTICLES_PER_THREAD: ppt})
+    assert fa == 0 and fb == 0 and a["rebuilds"] == b["rebuilds"]
+    for k in ("pos", "vel", "rho", "p", "type"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_launch_shape_options_are_checked(sphlib):
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.04)
+    with S.Solver(p, len(st["rho"])) as sol:
+        lib = api.lib()
+        for bad in (0, 16, 48, 288):
+            assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_BLOCK_THREADS, bad) == \
+                api.SPH_ERR_ARG
+        for bad in (0, 65):
+            assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_PARTICLES_PER_THREAD, bad) == \
+                api.SPH_ERR_ARG
+        assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_BLOCK_THREADS, 192) == api.SPH_OK

@@ -1,0 +1,138 @@
+"""Autotuner for the resident solver's launch shape and cell size.
+
+Picks, for one workload on the GPU at hand, the threads per block and particles per thread of
+the neighbour kernels and the neighbour-list skin (which sets the cell size, kh (1 + skin)).
+It loads the workload once; for every candidate it forces one list rebuild, runs two profiled
+steps and reads the per-phase device time (SPH_OPT_PROFILE): the cost of a rebuild (sort,
+gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The step
+cost it ranks by is
+
+    2 t_pass + r t_rebuild,    r = 2 v dt / (skin kh)   (r = 2 with skin 0),
+
+with r the rebuilds per step a flow whose fastest particle moves at v needs (the list is
+rebuilt once some particle has moved skin kh / 2).  v defaults to the dam-break surge-front
+speed 2 sqrt(g H) of the tallest water column H, so a short tuning run from rest does not
+reward a large skin for rebuilds the flow has not needed yet.
+
+    from tmp_sph_gb300 import autotune
+    best = autotune.tune(params, states)            # one state dict or a list (batched)
+    autotune.apply(solver, best)
+"""
+from __future__ import annotations
+
+import itertools
+import math
+
+from . import api
+from . import solver as S
+
+THREADS = (64, 128, 256)
+PPT = (1, 2, 4)
+SKINS = (0, 50, 100, 150, 200, 300)
+
+# profile phases: 0 sort, 1 gather + cell starts, 2 list build, 3 pass 1, 4 pass 2
+_REBUILD = ("sort", "gather_cells", "nbr_build")
+_PASSES = ("pass1", "pass2_integrate")
+
+
+def surge_speed(states: list, gravity: float) -> float:
+    """2 sqrt(g H) of the tallest fluid column among the states."""
+    h = 0.0
+    for st in states:
+        fl = st["type"] == 1
+        if fl.any():
+            h = max(h, float(st["pos"][fl, 2].max()))
+    return 2.0 * math.sqrt(abs(gravity) * max(h, 1e-6))
+
+
+def _upload(sol, states, stream):
+    if len(states) == 1:
+        st = states[0]
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
+    else:
+        sol.upload_instances(states, stream=stream)
+
+
+def measure(sol, stream, threads: int, ppt: int, skin: int) -> dict:
+    """Rebuild and pass costs (ms) of one candidate on the loaded state, from two profiled
+    steps (setting the skin forces the next half step to rebuild; the state advances)."""
+    sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
+    sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+    sol.step(1, stream=stream)  # warm: first launches of this shape
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
+    r0 = sol.rebuild_count(stream=stream)
+    sol.set_option(api.SPH_OPT_PROFILE, 1)
+    sol.profile(reset=True)
+    sol.step(2, stream=stream)
+    prof = sol.profile(reset=True)
+    sol.set_option(api.SPH_OPT_PROFILE, 0)
+    rebuilds = sol.rebuild_count(stream=stream) - r0
+    t_re = sum(prof[k]["ms"] for k in _REBUILD)
+    t_pass = sum(prof[k]["ms"] for k in _PASSES) / 4.0  # per half step
+    # with every half step rebuilding (skin 0) the rebuild time covers four rebuilds
+    return {"threads": threads, "ppt": ppt, "skin_permille": skin,
+            "rebuild_ms": t_re / max(1, rebuilds), "pass_ms_per_half_step": t_pass,
+            "rebuilds_seen": rebuilds, "flags": sol.error_flags(stream=stream)}
+
+
+def step_cost(m: dict, p, v: float) -> float:
+    skin = m["skin_permille"] / 1000.0
+    rate = 2.0 if skin <= 0.0 else min(2.0, 2.0 * v * float(p.dt) / (skin * float(p.kh)))
+    return 2.0 * m["pass_ms_per_half_step"] + rate * m["rebuild_ms"]
+
+
+def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=SKINS,
+         speed: float | None = None) -> dict:
+    """Best (threads, ppt, skin) for this workload; `states` is one state dict or a list of
+    them (batched instances).  Returns the choice with the measured table."""
+    import torch
+    states = states if isinstance(states, list) else [states]
+    n = sum(len(st["rho"]) for st in states)
+    v = speed if speed is not None else surge_speed(states, float(p.gravity))
+    stream = torch.cuda.Stream()
+    table = []
+    with S.Solver(p, n, precision=precision) as sol:
+        _upload(sol, states, stream)
+        for t, k, s in itertools.product(threads, ppt, skins):
+            m = measure(sol, stream, t, k, s)
+            m["step_ms_estimate"] = step_cost(m, p, v)
+            table.append(m)
+    ok = [m for m in table if m["flags"] == 0] or table
+    best = min(ok, key=lambda m: m["step_ms_estimate"])
+    return {"threads": best["threads"], "ppt": best["ppt"],
+            "skin_permille": best["skin_permille"], "speed_m_s": v,
+            "step_ms_estimate": best["step_ms_estimate"], "table": table}
+
+
+def apply(sol, best: dict) -> None:
+    """Set a tuned choice on a solver (before its upload)."""
+    sol.set_option(api.SPH_OPT_BLOCK_THREADS, best["threads"])
+    sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, best["ppt"])
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, best["skin_permille"])
+
+
+def summary(best: dict) -> dict:
+    """The choice without the table, plus the estimate of the default (128, 1, 100)."""
+    out = {k: v for k, v in best.items() if k != "table"}
+    for m in best["table"]:
+        if (m["threads"], m["ppt"], m["skin_permille"]) == (128, 1, 100):
+            out["default_step_ms_estimate"] = m["step_ms_estimate"]
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    from . import cases
+    ap = argparse.ArgumentParser(description="tune the solver for a named case")
+    ap.add_argument("--case", default="large")
+    ap.add_argument("--precision", default="fp32")
+    args = ap.parse_args()
+    if args.case.startswith("batch"):
+        sts, prm = cases.batch(int(args.case[5:] or 64))
+    else:
+        st, prm = cases.build(args.case)
+        sts = [st]
+    res = tune(prm, sts, precision=args.precision)
+    print(json.dumps(res))

@@ -57,7 +57,11 @@ namespace sph {
 
 namespace {
 
-constexpr int NS_THREADS = 128;
+// Block size of the neighbour kernels is a launch parameter (KParams::threads, a multiple of
+// 32 up to NS_MAX_THREADS), as is the number of particles a thread handles (KParams::ppt); both
+// are picked by the autotuner.  ppt > 1 runs the grid-stride instantiation (GS), which holds
+// its loop state in registers (pass 2: 64 instead of 48), so ppt = 1 has its own.
+constexpr int NS_MAX_THREADS = 256;
 // Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^26).
 constexpr int CODE_SHIFT = 26;
 constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
@@ -275,14 +279,12 @@ __device__ __forceinline__ float4 as_float4(const dvec4& v) {
 // Slots are warp-interleaved (nbr_col): the passes read them coalesced, the build writes them
 // scattered within its warp's block, which L2 merges before they reach HBM.
 template <class P>
-__global__ void __launch_bounds__(NS_THREADS)
-k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
-            const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-            int walls_all, unsigned* err, const unsigned* gate) {
+__device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
+                                              const vec4_t<typename P::T>* __restrict__ X,
+                                              const unsigned* __restrict__ keys,
+                                              const int* __restrict__ cs, const NbrList& nl,
+                                              int walls_all, unsigned* err, int i) {
     using T = typename P::T;
-    if (gated_off(gate)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
     const vec4_t<T> pi = X[i];
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
@@ -300,18 +302,34 @@ k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__
     raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }
 
+template <class P, bool GS>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
+k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
+            const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+            int walls_all, unsigned* err, const unsigned* gate) {
+    if (gated_off(gate)) return;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (GS) {
+        for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
+            nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, i);
+    } else if (i0 < k.n) {
+        nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, i0);
+    }
+}
+
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
 // particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
 // neighbour record and the particle's own (p', rho', dofv).
 template <class P, bool WRITE_SUMS, bool LIST>
-__global__ void __launch_bounds__(NS_THREADS)
-k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
-        const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-        Pass1OutT<typename P::T> out, float* __restrict__ rhop_sum, float* __restrict__ w_sum) {
+__device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
+                                          const ParticleSetT<typename P::T>& in,
+                                          const unsigned* __restrict__ keys,
+                                          const int* __restrict__ cs, const NbrList& nl,
+                                          const Pass1OutT<typename P::T>& out,
+                                          float* __restrict__ rhop_sum, float* __restrict__ w_sum,
+                                          int i) {
     using T = typename P::T;
     using V = vec4_t<T>;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
     const V* __restrict__ R = in.rec;
     const V pi = R[2 * (size_t)i];      // x, y, z, p
     const V vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
@@ -351,6 +369,20 @@ k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     if constexpr (WRITE_SUMS) {
         rhop_sum[i] = (float)rsum;
         w_sum[i] = (float)wsum;
+    }
+}
+
+template <class P, bool WRITE_SUMS, bool LIST, bool GS>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
+k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+        const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+        Pass1OutT<typename P::T> out, float* __restrict__ rhop_sum, float* __restrict__ w_sum) {
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (GS) {
+        for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
+            pass1_one<P, WRITE_SUMS, LIST>(k, in, keys, cs, nl, out, rhop_sum, w_sum, i);
+    } else if (i0 < k.n) {
+        pass1_one<P, WRITE_SUMS, LIST>(k, in, keys, cs, nl, out, rhop_sum, w_sum, i0);
     }
 }
 
@@ -566,49 +598,89 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
     }
 }
 
-template <class P, int MODE, bool LIST>
-__global__ void __launch_bounds__(NS_THREADS)
+template <class P, int MODE, bool LIST, bool GS>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
 k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
         Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
         int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
         unsigned* err, unsigned* disp) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
-    if (i < k.n)
-        d2 = pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (GS) {
+        for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
+            d2 = fmaxf(d2, pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt,
+                                                    wall_rates, out, out_hash, err));
+    } else if (i0 < k.n) {
+        d2 = pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
                                       out, out_hash, err);
+    }
     if (MODE == MODE_RATES || disp == nullptr) return;
     // block maximum of the squared displacement, one atomic per block (non-negative floats
-    // order like their bit patterns)
-    __shared__ unsigned s_max[NS_THREADS / 32];
+    // order like their bit patterns); blockDim is a multiple of 32, every thread gets here
+    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
     const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
     if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned m = s_max[0];
-#pragma unroll
-        for (int w = 1; w < NS_THREADS / 32; w++) m = max(m, s_max[w]);
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
         if (m) atomicMax(disp, m);
     }
 }
 
-inline int blocks_for(long n, int t) { return (int)((n + t - 1) / t); }
+// Launch shape of a neighbour kernel: KParams::threads per block, KParams::ppt particles per
+// thread.
+template <class KP>
+inline dim3 ns_grid(const KP& k) {
+    const long per_block = (long)k.threads * (k.ppt > 0 ? k.ppt : 1);
+    const long b = ((long)k.n + per_block - 1) / per_block;
+    return dim3((unsigned)(b > 0 ? b : 1));
+}
+
+template <class P, bool LIST, bool GS>
+void pass1_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                     const unsigned* keys, const int* cs, const NbrList& nl,
+                     const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
+                     cudaStream_t s) {
+    const dim3 b = ns_grid(k);
+    if constexpr (P::kId == SPH_PREC_FP32) {
+        if (rhop_sum && w_sum) {
+            k_pass1<P, true, LIST, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, nl, o, rhop_sum,
+                                                               w_sum);
+            return;
+        }
+    }
+    k_pass1<P, false, LIST, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, nl, o, nullptr,
+                                                        nullptr);
+}
 
 template <class P, bool LIST>
 void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
                   const unsigned* keys, const int* cs, const NbrList& nl,
                   const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
-    const int b = blocks_for(k.n, NS_THREADS);
-    if constexpr (P::kId == SPH_PREC_FP32) {
-        if (rhop_sum && w_sum) {
-            k_pass1<P, true, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, rhop_sum,
-                                                            w_sum);
-            return;
-        }
-    }
-    k_pass1<P, false, LIST><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, nl, o, nullptr, nullptr);
+    if (k.ppt > 1)
+        pass1_launch_gs<P, LIST, true>(k, in, keys, cs, nl, o, rhop_sum, w_sum, s);
+    else
+        pass1_launch_gs<P, LIST, false>(k, in, keys, cs, nl, o, rhop_sum, w_sum, s);
+}
+
+template <class P, int MODE, bool GS>
+void pass2_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
+                     const unsigned* keys, const int* cs, const NbrList* nl,
+                     const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
+                     int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
+                     unsigned* err, unsigned* disp, cudaStream_t s) {
+    const dim3 b = ns_grid(k);
+    if (nl)
+        k_pass2<P, MODE, true, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt,
+                                                            vel_dt, wall_rates, out, out_hash,
+                                                            err, disp);
+    else
+        k_pass2<P, MODE, false, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, NbrList{}, p1,
+                                                             rho_dt, vel_dt, wall_rates, out,
+                                                             out_hash, err, nullptr);
 }
 
 template <class P, int MODE>
@@ -617,14 +689,12 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                   unsigned* err, unsigned* disp, cudaStream_t s) {
-    const int b = blocks_for(k.n, NS_THREADS);
-    if (nl)
-        k_pass2<P, MODE, true><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt, vel_dt,
-                                                         wall_rates, out, out_hash, err, disp);
+    if (k.ppt > 1)
+        pass2_launch_gs<P, MODE, true>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                       out_hash, err, disp, s);
     else
-        k_pass2<P, MODE, false><<<b, NS_THREADS, 0, s>>>(k, in, keys, cs, NbrList{}, p1, rho_dt,
-                                                          vel_dt, wall_rates, out, out_hash, err,
-                                                          nullptr);
+        pass2_launch_gs<P, MODE, false>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
+                                        out, out_hash, err, disp, s);
 }
 
 }  // namespace
@@ -644,8 +714,12 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    k_nbr_build<P><<<blocks_for(k.n, NS_THREADS), NS_THREADS, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                                      walls_all, err, gate);
+    if (k.ppt > 1)
+        k_nbr_build<P, true><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl, walls_all,
+                                                              err, gate);
+    else
+        k_nbr_build<P, false><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                               walls_all, err, gate);
     return cudaGetLastError();
 }
 

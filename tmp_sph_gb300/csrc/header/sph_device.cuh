@@ -46,6 +46,10 @@ struct KParamsT {
     // grid.  A single simulation has gz_local = gz and inst_cells = 0.
     int gz_local;
     int inst_cells;
+    // Launch shape of the neighbour kernels (host side): threads per block (multiple of 32, at
+    // most 256) and particles per thread.
+    int threads;
+    int ppt;
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
     T h, inv_h, kh, kh2;

@@ -247,6 +247,8 @@ struct sph_ctx {
     int opt_nbr_list = 1;
     int opt_nbr_cap = 0;  // 0: nbr_capacity_for(P)
     int opt_cond_graph = 1;  // graph replay skips the rebuild kernels through conditional nodes
+    int opt_threads = 128;   // neighbour kernels: threads per block
+    int opt_ppt = 1;         // neighbour kernels: particles per thread
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

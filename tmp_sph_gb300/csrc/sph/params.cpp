@@ -34,6 +34,8 @@ KParams make_kparams(const sph_params& p, int n) {
     k.num_cells = p.num_cells;
     k.gz_local = p.grid_dim[2];
     k.inst_cells = 0;
+    k.threads = 128;
+    k.ppt = 1;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
@@ -90,6 +92,8 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.num_cells = p.num_cells;
     k.gz_local = p.grid_dim[2];
     k.inst_cells = 0;
+    k.threads = 128;
+    k.ppt = 1;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];

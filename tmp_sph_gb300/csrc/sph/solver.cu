@@ -232,6 +232,8 @@ template <class T>
 KParamsT<T> resident_kparams(const sph_ctx* c) {
     KParamsT<T> k = make_kparams_t<T>(c->Pi, c->n);
     k.gz_local = c->gz_inst;
+    k.threads = c->opt_threads;
+    k.ppt = c->opt_ppt;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
@@ -519,6 +521,16 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
         case SPH_OPT_USE_GRAPH: c->opt_use_graph = value != 0; drop_graph(c); return SPH_OK;
         case SPH_OPT_CONDITIONAL_GRAPH:
             c->opt_cond_graph = value != 0;
+            drop_graph(c);
+            return SPH_OK;
+        case SPH_OPT_BLOCK_THREADS:
+            if (value < 32 || value > 256 || value % 32) return SPH_ERR_ARG;
+            c->opt_threads = value;
+            drop_graph(c);
+            return SPH_OK;
+        case SPH_OPT_PARTICLES_PER_THREAD:
+            if (value < 1 || value > 64) return SPH_ERR_ARG;
+            c->opt_ppt = value;
             drop_graph(c);
             return SPH_OK;
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;

@@ -371,6 +371,25 @@ typedef struct sph_stats {
 int sph_probe_read(sph_ctx* ctx, const sph_probe* probes, int nprobes, double* values,
                    double cfl, sph_stats* stats, void* stream);
 
+/* ---------------------------------------------------------------- output */
+/* Asynchronous snapshot (no reference counterpart: the reference copies the state to the host
+ * synchronously before each output, src/sph/sph_run.cu:262-267).  Writes the state in original
+ * order into buffers of the context on `stream`, then copies it into the given host buffers
+ * (pinned for the copy to overlap; any may be NULL) on an internal copy stream, so steps
+ * launched after this call run while the copy is in flight.  A second snapshot waits for the
+ * first one's copies. */
+int sph_snapshot_begin(sph_ctx* ctx, float* pos, float* vel, float* rho, float* p, int* type,
+                       void* stream);
+/* Wait until the last snapshot is in the host buffers. */
+int sph_snapshot_wait(sph_ctx* ctx);
+/* *done = 1 when the last snapshot's copies have completed (or there is none), else 0. */
+int sph_snapshot_query(sph_ctx* ctx, int* done);
+/* Legacy-VTK particle file in the reference's layout (src/io/io.cu:154-199,
+ * opt_src_v3/io/io.cu:121-200): UNSTRUCTURED_GRID POINTS with POINT_DATA "p" and "velocity",
+ * plus "type" when given; binary = 1 writes big-endian floats, 0 text. */
+int sph_write_vtk(const char* path, int n, const float* pos, const float* vel, const float* p,
+                  const int* type, int binary);
+
 /* ---------------------------------------------------------------- reference-signature shim */
 /* The library also exports, with C++ linkage, the reference's own host functions calcHash,
  * sortParticles, reorder, recover, SPH_NS_simpleversion, PC_prediction, PC_correction,

@@ -172,6 +172,10 @@ _PROTOS = {
     "sph_step_host": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I)]),
     "sph_read_rebuild_count": (_I, [_P, C.POINTER(C.c_uint), _P]),
+    "sph_snapshot_begin": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "sph_snapshot_wait": (_I, [_P]),
+    "sph_snapshot_query": (_I, [_P, C.POINTER(_I)]),
+    "sph_write_vtk": (_I, [C.c_char_p, _I, _P, _P, _P, _P, _I]),
     "sph_probe_read": (_I, [_P, C.POINTER(SphProbe), _I, C.POINTER(C.c_double), C.c_double,
                             C.POINTER(SphStats), _P]),
     "sph_read_error_flags": (_I, [_P, C.POINTER(C.c_uint), _P]),

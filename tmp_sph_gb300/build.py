@@ -32,6 +32,7 @@ SOURCES = [
     "sph/ref_shim.cu",
     "io/dam_break.cpp",
     "io/probes.cu",
+    "io/vtk.cpp",
 ]
 HEADERS = ["header/sph_device.cuh", "header/sph_internal.h"]
 

@@ -518,8 +518,9 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
             out.txm[i] = txm;
             out.tvel[i] = tv;
         }
-        const int inst = in.inst ? in.inst[i] : 0;
-        if (out.inst) out.inst[i] = inst;
+        // instance ids only move with the particles when instances are batched
+        const int inst = k.inst_cells ? in.inst[i] : 0;
+        if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
         out_hash[i] = resident_key(k, inst, nxm.x, nxm.y, nxm.z, &f);
         raise_flags(err, f);
@@ -587,8 +588,9 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
             out.tpos[i] = tp;
             out.tvel[i] = tv;
         }
-        const int inst = in.inst ? in.inst[i] : 0;
-        if (out.inst) out.inst[i] = inst;
+        // instance ids only move with the particles when instances are batched
+        const int inst = k.inst_cells ? in.inst[i] : 0;
+        if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
         out_hash[i] = resident_key(k, inst, np.x, np.y, np.z, &f);
         raise_flags(err, f);
@@ -601,6 +603,40 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
 template <class P, int MODE, bool LIST, bool GS>
 __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+        const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+        Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
+        int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
+        unsigned* err, unsigned* disp) {
+    float d2 = 0.f;
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (GS) {
+        for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
+            d2 = fmaxf(d2, pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt,
+                                                    wall_rates, out, out_hash, err));
+    } else if (i0 < k.n) {
+        d2 = pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
+                                      out, out_hash, err);
+    }
+    if (MODE == MODE_RATES || disp == nullptr) return;
+    // block maximum of the squared displacement, one atomic per block (non-negative floats
+    // order like their bit patterns); blockDim is a multiple of 32, every thread gets here
+    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned m = s_max[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
+        if (m) atomicMax(disp, m);
+    }
+}
+
+// The same kernel held to 48 registers: the FP32 one-particle-per-thread step kernel fits in
+// 48 with an 8-byte stack frame, and 48 keeps ten 128-thread blocks resident per SM where the
+// unconstrained 53 keeps nine.
+template <class P, int MODE, bool LIST, bool GS>
+__global__ void __maxnreg__(48)
+k_pass2_r48(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
         Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
         int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
@@ -673,6 +709,14 @@ void pass2_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typena
                      int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                      unsigned* err, unsigned* disp, cudaStream_t s) {
     const dim3 b = ns_grid(k);
+    if constexpr (P::kId == SPH_PREC_FP32 && MODE != MODE_RATES && !GS) {
+        if (nl) {
+            k_pass2_r48<P, MODE, true, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, *nl, p1,
+                                                                    rho_dt, vel_dt, wall_rates,
+                                                                    out, out_hash, err, disp);
+            return;
+        }
+    }
     if (nl)
         k_pass2<P, MODE, true, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt,
                                                             vel_dt, wall_rates, out, out_hash,

@@ -228,6 +228,13 @@ struct sph_ctx {
     size_t sort_scratch_bytes = 0;
     unsigned* err = nullptr;         // device error word
     double* probe_acc = nullptr;     // probe / reduction accumulator (probe_acc_words())
+    // asynchronous snapshots: original-order state written on the compute stream, copied to the
+    // host on copy_stream while later steps run
+    float* snap_f = nullptr;         // pos [3n], vel [3n], rho [n], p [n]
+    int* snap_type = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
+    bool snap_pending = false;
 
     // neighbour list, reused across half steps while every particle stays within skin/2 of
     // where it was when the list was built

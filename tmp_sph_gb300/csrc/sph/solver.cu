@@ -147,6 +147,16 @@ void release(sph_ctx* c) {
     c->probe_acc = nullptr;
     cudaFree(c->inst_off);
     c->inst_off = nullptr;
+    if (c->snap_pending && c->snap_done) cudaEventSynchronize(c->snap_done);
+    cudaFree(c->snap_f);
+    cudaFree(c->snap_type);
+    c->snap_f = nullptr;
+    c->snap_type = nullptr;
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->snap_ready) cudaEventDestroy(c->snap_ready);
+    if (c->snap_done) cudaEventDestroy(c->snap_done);
+    c->copy_stream = nullptr;
+    c->snap_ready = c->snap_done = nullptr;
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -451,6 +461,11 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = dalloc(&c->probe_acc, probe_acc_words());
     if (e == cudaSuccess) e = dalloc(&c->inst_off, SPH_MAX_INSTANCES + 1);
+    if (e == cudaSuccess) e = dalloc(&c->snap_f, 8 * (size_t)cap);
+    if (e == cudaSuccess) e = dalloc(&c->snap_type, cap);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->snap_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = dalloc(&c->rb, 4);
     if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
@@ -758,6 +773,65 @@ extern "C" int sph_probe_read(sph_ctx* c, const sph_probe* probes, int nprobes, 
             return SPH_ERR_CUDA;
     }
     probe_results(acc.data(), probes, nprobes, cfl, c->P.h, c->P.cs, stats, values);
+    return SPH_OK;
+}
+
+extern "C" int sph_snapshot_wait(sph_ctx* c) {
+    if (!c) return SPH_ERR_ARG;
+    if (!c->snap_pending) return SPH_OK;
+    const cudaError_t e = cudaEventSynchronize(c->snap_done);
+    c->snap_pending = false;
+    return to_status(e);
+}
+
+extern "C" int sph_snapshot_query(sph_ctx* c, int* done) {
+    if (!c || !done) return SPH_ERR_ARG;
+    if (!c->snap_pending) {
+        *done = 1;
+        return SPH_OK;
+    }
+    const cudaError_t e = cudaEventQuery(c->snap_done);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return SPH_OK;
+    }
+    *done = 1;
+    return to_status(e);
+}
+
+extern "C" int sph_snapshot_begin(sph_ctx* c, float* pos, float* vel, float* rho, float* p,
+                                  int* type, void* stream) {
+    if (!c) return SPH_ERR_ARG;
+    if (!c->loaded) return SPH_ERR_STATE;
+    // the snapshot buffers are reused: the previous snapshot's copies must have finished
+    int st = sph_snapshot_wait(c);
+    if (st != SPH_OK) return st;
+    const int n = c->n;
+    if (n == 0) return SPH_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    float* spos = c->snap_f;
+    float* svel = c->snap_f + 3 * (size_t)n;
+    float* srho = c->snap_f + 6 * (size_t)n;
+    float* sp = c->snap_f + 7 * (size_t)n;
+    const cudaError_t e = with_prec(c, [&](auto tag) {
+        using P = decltype(tag);
+        return launch_download_convert<P>(resident_kparams<typename P::T>(c), State<P>::y(c),
+                                          pos ? spos : nullptr, vel ? svel : nullptr,
+                                          rho ? srho : nullptr, p ? sp : nullptr,
+                                          type ? c->snap_type : nullptr, s);
+    });
+    if (e != cudaSuccess || cudaEventRecord(c->snap_ready, s) != cudaSuccess ||
+        cudaStreamWaitEvent(c->copy_stream, c->snap_ready, 0) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    cudaStream_t cs = c->copy_stream;
+    if ((pos && cudaMemcpyAsync(pos, spos, (size_t)n * 12, cudaMemcpyDeviceToHost, cs) != cudaSuccess) ||
+        (vel && cudaMemcpyAsync(vel, svel, (size_t)n * 12, cudaMemcpyDeviceToHost, cs) != cudaSuccess) ||
+        (rho && cudaMemcpyAsync(rho, srho, (size_t)n * 4, cudaMemcpyDeviceToHost, cs) != cudaSuccess) ||
+        (p && cudaMemcpyAsync(p, sp, (size_t)n * 4, cudaMemcpyDeviceToHost, cs) != cudaSuccess) ||
+        (type && cudaMemcpyAsync(type, c->snap_type, (size_t)n * 4, cudaMemcpyDeviceToHost, cs) != cudaSuccess) ||
+        cudaEventRecord(c->snap_done, cs) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    c->snap_pending = true;
     return SPH_OK;
 }
 

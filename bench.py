@@ -52,10 +52,8 @@ PHASE_KERNEL = {"sort": "k_rs_upsweep/k_rs_scan/k_rs_downsweep",
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from tmp_sph_gb300.replicas import dist_env as env
+    return env()
 
 
 PHASE_NCU_NAME = {"nbr_build": "k_nbr_build", "pass1": "k_pass1", "pass2_integrate": "k_pass2"}
@@ -241,10 +239,16 @@ def run_batch(args):
     width U[0.2, 0.6] m and height U[0.15, 0.45] m) advanced together by one batched solver.
     Device-resident throughput only (all instances' particles per second)."""
     import torch
-    from tmp_sph_gb300 import api, build, cases, solver as S
+    import torch.distributed as dist
+    from tmp_sph_gb300 import api, build, cases, replicas, solver as S
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
     n_inst = int(args.case[5:] or 64)
-    states, p = cases.batch(n_inst)
+    # weak scaling: every rank advances its own batch of n_inst instances (its own seed)
+    states, p = cases.batch(n_inst, seed=20240611 + 1009 * rank)
     n = sum(len(st["rho"]) for st in states)
     stream = torch.cuda.Stream()
     tuned = None
@@ -262,26 +266,31 @@ def run_batch(args):
     torch.cuda.synchronize()
     r0 = sol.rebuild_count(stream=stream)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(gpu_uuid(0)) as clk:
+    with ClockSampler(gpu_uuid(local)) as clk:
+        replicas.barrier()
         torch.cuda.synchronize()
         ev0.record(stream)
         sol.step(args.steps, stream=stream)
         ev1.record(stream)
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+        replicas.barrier()
+    ms = replicas.reduce_max(ev0.elapsed_time(ev1))
+    n_job = int(replicas.reduce_sum(n))
     rebuilds = sol.rebuild_count(stream=stream) - r0
     flags = sol.error_flags(stream=stream)
     sol.close()
     fluid = [int((st["type"] == 1).sum()) for st in states]
     line = {
-        "metric": METRIC, "value": n * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": 1,
+        "metric": METRIC, "value": n_job * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
                   "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
-        "config": {"workload": f"dam_break_batch{n_inst}_{args.precision}", "instances": n_inst,
-                   "particles": n, "fluid_min": min(fluid), "fluid_max": max(fluid),
+        "config": {"workload": f"dam_break_batch{n_inst}_{args.precision}",
+                   "instances_per_gpu": n_inst, "particles": n_job, "particles_rank0": n,
+                   "fluid_min": min(fluid), "fluid_max": max(fluid),
+                   "parallelism": f"instances x{ws} (independent batches, no collective)",
                    "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
                    "neighbour_list_skin_over_kh": args.skin / 1000.0,
                    "graph_mode": args.graph_mode},
@@ -292,7 +301,10 @@ def run_batch(args):
         "clocks": clk.summary(),
         "device_error_flags": flags,
     }
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
 
 
 def sol_cells_batch(p, n_inst: int, skin: int) -> int:

@@ -8,12 +8,11 @@
 // rec[2i] = (x, y, z, p) and rec[2i+1] = (vx, vy, vz, ±rho) with the sign of rho marking a
 // fluid (+) or boundary (-) particle, so everything a neighbour contributes to pass 1 is one
 // aligned 32-byte sector in FP32.  Pass 1 writes the record pass 2 gathers, nrec[2i] =
-// (x, y, z, q), nrec[2i+1] = (vx, vy, vz, ±V'), where q = p' - rho0 cs h dofv: the
+// (x, y, z, q), nrec[2i+1] = (vx, vy, vz, ±rho'), where q = p' - rho0 cs h dofv: the
 // acoustic-damper term of a fluid-fluid pair, rho0 cs h (dofv_i + dofv_j), splits into an i part
 // and a j part, and the j part is folded into the neighbour's pressure (boundary particles
-// have dofv = 0, so q = p'); V' = m / rho' is the neighbour's volume, every term of pass 2 is
-// proportional to it, so the division happens once per particle instead of once per pair.
-// Pass 1 also writes self[i] = (p', rho', dofv, 0) for the particle's own side.
+// have dofv = 0, so q = p').  It also writes self[i] = (p', rho', dofv, 0) for the particle's
+// own side.
 //
 // Cells are walked as nine x-strips: the three cells (x-1 .. x+1) of one (y, z) row are
 // consecutive in the sorted order, so each strip is one contiguous slot range
@@ -385,9 +384,8 @@ __device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
         rho = eos_density(k, p);
     }
     const T qv = fi ? p - k.damper * dv : p;
-    const T vol = k.mass / rho;  // the neighbour volume pass 2 multiplies by, once per particle
     out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
-    out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? vol : -vol);
+    out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
     out.self[i] = make4<T>(p, rho, dv, T(0));
     if constexpr (WRITE_SUMS) {
         rhop_sum[i] = (float)rsum;
@@ -440,20 +438,21 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
     if (fi || (MODE == MODE_RATES && wall_rates)) {
         const T damp_i = k.damper * dofvi;
         Sum<T, P::kComp> sd, sx, sy, sz;
-        // aj = (x, y, z, q), vj = (vx, vy, vz, ±V) of the neighbour, V = m / rho
+        // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour.  rho_i - rho_j stays an
+        // exact difference of two close floats; writing the density-diffusion term with the
+        // volume m / rho_j instead (rho_i V_j - m) cancels and lost three digits of rho_dt.
         visit_records<P, LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
                                   [&](int j, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
             const bool fj = fluid_rec(vj.w);
-            const T volj = dabs(vj.w);
+            const T rhoj = dabs(vj.w);
             const T rr = pair_sqrt(r2);
             const T q = rr * k.inv_h;
             const T t = T(1) - T(0.5) * q;
             const T fr = k.c_fr * t * t * t;
             const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            const T volj = k.mass * pair_rcp(rhoj);
             const T inv_r2e = pair_rcp(r2 + k.eta2);
-            // (m / rho_j) (rho_i vdotr + (rho_i - rho_j) delta h cs r^2 / (r^2 + eta^2)), with
-            // (rho_i - rho_j) m / rho_j = rho_i V_j - m
-            sd.add(fr * (volj * rhoi * vdotr + k.delta_h_cs * r2 * inv_r2e * (rhoi * volj - k.mass)));
+            sd.add(volj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
             T S;
             if (fi) {
                 S = -presi - aj.w;

@@ -91,9 +91,8 @@ struct ParticleSetT {
 using ParticleSet = ParticleSetT<float>;
 
 // Pass-1 output.  nrec[2i] = (x, y, z, q) with q = p' - rho0 cs h dofv for fluid particles and
-// q = p' for boundary particles, nrec[2i+1] = (vx, vy, vz, ±V') with the volume V' = m / rho'
-// (negative for boundary particles): the record pass 2 gathers per neighbour.
-// self[i] = (p', rho', dofv, 0): the particle's own side.
+// q = p' for boundary particles, nrec[2i+1] = (vx, vy, vz, ±rho'): the record pass 2 gathers per
+// neighbour.  self[i] = (p', rho', dofv, 0): the particle's own side.
 template <class T>
 struct Pass1OutT {
     vec4_t<T>* nrec = nullptr;

@@ -100,17 +100,25 @@ def test_resident_steps_match_reference(sphlib, cuda, report, case):
     n = len(st["rho"])
     fl = st["type"] == 1
     s = torch.cuda.Stream()
+    # Early displacements are tens of ulp of the position, so a velocity differing in its last
+    # bits flips the rounding of pos + dt v for a few particles (a few ulp each): the
+    # displacement is checked at 1e-3 and the positions to within 4 ulp.
     for nsteps, tol in ((1, 2e-5), (5, 2e-4)):
         with S.Solver(p, n) as sol:
             sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
             sol.step(nsteps, stream=s)
             out = sol.download(stream=s)
+        ref_pos = d[f"step{nsteps}_pos"]
         e = {
-            "disp": rel_l2((out["pos"] - st["pos"])[fl], (d[f"step{nsteps}_pos"] - st["pos"])[fl]),
+            "disp": rel_l2((out["pos"] - st["pos"])[fl], (ref_pos - st["pos"])[fl]),
             "vel": rel_l2(out["vel"][fl], d[f"step{nsteps}_vel"][fl]),
             "drho": rel_l2(out["rho"][fl] - 1000, d[f"step{nsteps}_rho"][fl] - 1000),
         }
+        ulps = (np.abs(out["pos"] - ref_pos) / np.spacing(np.abs(ref_pos).astype(np.float32))).max()
         for k, v in e.items():
-            report(f"gpu resident vs reference {case} {nsteps} steps {k}", v, tol)
-        assert all(v < tol for v in e.values()), (nsteps, e)
-        assert np.array_equal(out["pos"][~fl], d[f"step{nsteps}_pos"][~fl])
+            report(f"gpu resident vs reference {case} {nsteps} steps {k}", v,
+                   1e-3 if k == "disp" else tol)
+        report(f"gpu resident vs reference {case} {nsteps} steps max position ulp", ulps, 4)
+        assert e["disp"] < 1e-3 and e["vel"] < tol and e["drho"] < tol, (nsteps, e)
+        assert ulps <= 4
+        assert np.array_equal(out["pos"][~fl], ref_pos[~fl])

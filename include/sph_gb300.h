@@ -251,6 +251,9 @@ typedef struct sph_ctx sph_ctx;
                                     multiple of 32 (default 128) */
 #define SPH_OPT_PARTICLES_PER_THREAD 10  /* particles each thread of the neighbour kernels
                                     handles, grid-stride (1..64, default 1) */
+#define SPH_OPT_PAIRS 11  /* 1: the neighbour kernels take two consecutive particles per thread
+                             over the union of their neighbour lists, gathering each neighbour
+                             record once for both (FP32 and FP64; ignored in mixed precision) */
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */

@@ -341,23 +341,23 @@ k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
 // particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
 // neighbour record and the particle's own (p', rho', dofv).
-template <class P, bool WRITE_SUMS, bool LIST>
-__device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
-                                          const ParticleSetT<typename P::T>& in,
-                                          const unsigned* __restrict__ keys,
-                                          const int* __restrict__ cs, const NbrList& nl,
-                                          const Pass1OutT<typename P::T>& out,
-                                          float* __restrict__ rhop_sum, float* __restrict__ w_sum,
-                                          int i) {
+// Pass-1 state of one particle: its own record and the three neighbour sums.
+template <class P>
+struct Pass1Acc {
     using T = typename P::T;
     using V = vec4_t<T>;
-    const V* __restrict__ R = in.rec;
-    const V pi = R[2 * (size_t)i];      // x, y, z, p
-    const V vi = R[2 * (size_t)i + 1];  // vx, vy, vz, ±rho
-    const bool fi = fluid_rec(vi.w);
+    V pi, vi;  // x, y, z, p / vx, vy, vz, ±rho
+    bool fi;
     Sum<T, P::kComp> dofv, rs, ws;
-    visit_records<P, LIST, 1>(k, cs, keys, nl, in.xyz, R, i, pi,
-                              [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
+
+    __device__ __forceinline__ void load(const V* __restrict__ R, int i) {
+        pi = R[2 * (size_t)i];
+        vi = R[2 * (size_t)i + 1];
+        fi = fluid_rec(vi.w);
+    }
+    // One neighbour inside the support radius.
+    __device__ __forceinline__ void pair(const KParamsT<T>& k, const V& aj, const V& vj, T dx,
+                                         T dy, T dz, T r2) {
         if (!fluid_rec(vj.w)) return;
         const T rr = pair_sqrt(r2);
         const T q = rr * k.inv_h;
@@ -372,25 +372,49 @@ __device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
             const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
             dofv.add(-(fr * vdotr * (k.mass * pair_rcp(vj.w))));
         }
+    }
+    template <bool WRITE_SUMS>
+    __device__ __forceinline__ void finish(const KParamsT<T>& k, const Pass1OutT<T>& out,
+                                           float* __restrict__ rhop_sum,
+                                           float* __restrict__ w_sum, int i) {
+        T p, rho;
+        const T dv = dofv.get(), rsum = rs.get(), wsum = ws.get();
+        if (fi) {
+            p = pi.w;
+            rho = vi.w;
+        } else {
+            p = dabs(wsum) > T(1.0e-8) ? rsum / wsum : T(0);
+            if (p < T(0)) p = T(0);
+            rho = eos_density(k, p);
+        }
+        const T qv = fi ? p - k.damper * dv : p;
+        out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
+        out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
+        out.self[i] = make4<T>(p, rho, dv, T(0));
+        if constexpr (WRITE_SUMS) {
+            rhop_sum[i] = (float)rsum;
+            w_sum[i] = (float)wsum;
+        }
+    }
+};
+
+template <class P, bool WRITE_SUMS, bool LIST>
+__device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
+                                          const ParticleSetT<typename P::T>& in,
+                                          const unsigned* __restrict__ keys,
+                                          const int* __restrict__ cs, const NbrList& nl,
+                                          const Pass1OutT<typename P::T>& out,
+                                          float* __restrict__ rhop_sum, float* __restrict__ w_sum,
+                                          int i) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    Pass1Acc<P> acc;
+    acc.load(in.rec, i);
+    visit_records<P, LIST, 1>(k, cs, keys, nl, in.xyz, in.rec, i, acc.pi,
+                              [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
+        acc.pair(k, aj, vj, dx, dy, dz, r2);
     });
-    T p, rho;
-    const T dv = dofv.get(), rsum = rs.get(), wsum = ws.get();
-    if (fi) {
-        p = pi.w;
-        rho = vi.w;
-    } else {
-        p = dabs(wsum) > T(1.0e-8) ? rsum / wsum : T(0);
-        if (p < T(0)) p = T(0);
-        rho = eos_density(k, p);
-    }
-    const T qv = fi ? p - k.damper * dv : p;
-    out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
-    out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
-    out.self[i] = make4<T>(p, rho, dv, T(0));
-    if constexpr (WRITE_SUMS) {
-        rhop_sum[i] = (float)rsum;
-        w_sum[i] = (float)wsum;
-    }
+    acc.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i);
 }
 
 template <class P, bool WRITE_SUMS, bool LIST, bool GS>
@@ -417,6 +441,67 @@ enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
 // `out` may alias `in`: the update touches only particle i's own rows, and neighbours (also
 // the positions of a cell walk) come from the pass-1 records.  Returns the squared distance
 // of particle i from its position when the neighbour list was built (0 without a list).
+// Pass-2 state of one particle: its pass-1 record, own side and the four neighbour sums.
+template <class P, int MODE>
+struct Pass2Acc {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    V pi, vi;  // x, y, z, q / vx, vy, vz, ±rho
+    T rhoi, presi, damp_i;
+    bool fi, active;
+    Sum<T, P::kComp> sd, sx, sy, sz;
+
+    __device__ __forceinline__ void load(const KParamsT<T>& k, const Pass1OutT<T>& p1, int i,
+                                         int wall_rates) {
+        pi = p1.nrec[2 * (size_t)i];
+        vi = p1.nrec[2 * (size_t)i + 1];
+        const V si = p1.self[i];  // p_i, rho_i, dofv_i
+        fi = fluid_rec(vi.w);
+        rhoi = si.y;
+        presi = si.x;
+        damp_i = k.damper * si.z;
+        active = fi || (MODE == MODE_RATES && wall_rates);
+    }
+    // One neighbour inside the support radius.  aj = (x, y, z, q), vj = (vx, vy, vz, ±rho).
+    // rho_i - rho_j stays an exact difference of two close floats; writing the
+    // density-diffusion term with the volume m / rho_j instead (rho_i V_j - m) cancels and lost
+    // three digits of rho_dt.
+    __device__ __forceinline__ void pair(const KParamsT<T>& k, const Pass1OutT<T>& p1, int j,
+                                         const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
+        const bool fj = fluid_rec(vj.w);
+        const T rhoj = dabs(vj.w);
+        const T rr = pair_sqrt(r2);
+        const T q = rr * k.inv_h;
+        const T t = T(1) - T(0.5) * q;
+        const T fr = k.c_fr * t * t * t;
+        const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+        const T volj = k.mass * pair_rcp(rhoj);
+        const T inv_r2e = pair_rcp(r2 + k.eta2);
+        sd.add(volj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
+        T S;
+        if (fi) {
+            S = -presi - aj.w;
+            if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
+        } else {
+            S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
+        }
+        const T c = fr * S * volj;
+        sx.add(c * dx);
+        sy.add(c * dy);
+        sz.add(c * dz);
+    }
+};
+
+template <class P, int MODE>
+__device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, int i,
+                                              const Pass2Acc<P, MODE>& acc,
+                                              const ParticleSetT<typename P::T>& in,
+                                              const unsigned* __restrict__ keys,
+                                              const NbrList& nl, float* __restrict__ rho_dt,
+                                              float* __restrict__ vel_dt, int wall_rates,
+                                              const ParticleSetT<typename P::T>& out,
+                                              unsigned* __restrict__ out_hash, unsigned* err);
+
 template <class P, int MODE, bool LIST>
 __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int i,
                                            const ParticleSetT<typename P::T>& in,
@@ -428,48 +513,41 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
                                            unsigned* __restrict__ out_hash, unsigned* err) {
     using T = typename P::T;
     using V = vec4_t<T>;
-    const V* __restrict__ NR = p1.nrec;
-    const V pi = NR[2 * (size_t)i];
-    const V vi = NR[2 * (size_t)i + 1];
-    const V si = p1.self[i];  // p_i, rho_i, dofv_i
-    const bool fi = fluid_rec(vi.w);
-    const T rhoi = si.y, presi = si.x, dofvi = si.z;
-    T drho = T(0), ax = T(0), ay = T(0), az = T(0);
-    if (fi || (MODE == MODE_RATES && wall_rates)) {
-        const T damp_i = k.damper * dofvi;
-        Sum<T, P::kComp> sd, sx, sy, sz;
-        // aj = (x, y, z, q), vj = (vx, vy, vz, ±rho) of the neighbour.  rho_i - rho_j stays an
-        // exact difference of two close floats; writing the density-diffusion term with the
-        // volume m / rho_j instead (rho_i V_j - m) cancels and lost three digits of rho_dt.
-        visit_records<P, LIST, 2>(k, cs, keys, nl, NR, NR, i, pi,
+    Pass2Acc<P, MODE> acc;
+    acc.load(k, p1, i, wall_rates);
+    if (acc.active)
+        visit_records<P, LIST, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i, acc.pi,
                                   [&](int j, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
-            const bool fj = fluid_rec(vj.w);
-            const T rhoj = dabs(vj.w);
-            const T rr = pair_sqrt(r2);
-            const T q = rr * k.inv_h;
-            const T t = T(1) - T(0.5) * q;
-            const T fr = k.c_fr * t * t * t;
-            const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            const T volj = k.mass * pair_rcp(rhoj);
-            const T inv_r2e = pair_rcp(r2 + k.eta2);
-            sd.add(volj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
-            T S;
-            if (fi) {
-                S = -presi - aj.w;
-                if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
-            } else {
-                S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
-            }
-            const T c = fr * S * volj;
-            sx.add(c * dx);
-            sy.add(c * dy);
-            sz.add(c * dz);
+            acc.pair(k, p1, j, aj, vj, dx, dy, dz, r2);
         });
-        drho = sd.get();
+    return pass2_finish<P, MODE>(k, i, acc, in, keys, nl, rho_dt, vel_dt, wall_rates, out,
+                                 out_hash, err);
+}
+
+// Rates, or the predictor / corrector update and the next key of particle i; returns its
+// squared distance from its list-build position (0 without a list).
+template <class P, int MODE>
+__device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, int i,
+                                              const Pass2Acc<P, MODE>& acc,
+                                              const ParticleSetT<typename P::T>& in,
+                                              const unsigned* __restrict__ keys,
+                                              const NbrList& nl, float* __restrict__ rho_dt,
+                                              float* __restrict__ vel_dt, int wall_rates,
+                                              const ParticleSetT<typename P::T>& out,
+                                              unsigned* __restrict__ out_hash, unsigned* err) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const V& pi = acc.pi;
+    const V& vi = acc.vi;
+    const bool fi = acc.fi;
+    const T rhoi = acc.rhoi, presi = acc.presi;
+    T drho = T(0), ax = T(0), ay = T(0), az = T(0);
+    if (acc.active) {
+        drho = acc.sd.get();
         const T inv_rhoi = T(1) / rhoi;
-        ax = sx.get() * inv_rhoi;
-        ay = sy.get() * inv_rhoi;
-        az = sz.get() * inv_rhoi;
+        ax = acc.sx.get() * inv_rhoi;
+        ay = acc.sy.get() * inv_rhoi;
+        az = acc.sz.get() * inv_rhoi;
     }
     az += k.g;
 
@@ -688,6 +766,244 @@ k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     }
 }
 
+// ---------------------------------------------------------------- particle pairs
+// Pair mode (KParams::pairs, FP32 and FP64): a thread handles the two consecutive sorted
+// particles 2c and 2c+1 (a "pair", usually in one cell) over the union of their neighbour
+// lists, so each listed record is gathered once for both.  The passes are limited by those
+// gathers (one L1 data-stage wavefront per distinct line a warp instruction touches), and the
+// union of two consecutive particles' lists is about 1.38 times one list: 31% fewer gathers
+// for up to twice the pair bodies per gather.  The list is indexed by pair (warp-interleaved
+// over pairs); its slots hold every j within the list cutoff of either particle, in walk
+// order; each particle tests r < kh (and j != itself) on every slot.  A pair whose union
+// overflowed walks the cells for each of its two particles.
+
+template <class P>
+__device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
+                                               const vec4_t<typename P::T>* __restrict__ X,
+                                               const unsigned* __restrict__ keys,
+                                               const int* __restrict__ cs, const NbrList& nl,
+                                               int walls_all, unsigned* err, int c) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const int i0 = 2 * c, i1 = 2 * c + 1;
+    const bool has1 = i1 < k.n;
+    const V p0 = X[i0];
+    const V p1 = has1 ? X[i1] : p0;
+    if (nl.xb) {
+        nl.xb[i0] = as_float4(p0);
+        if (has1) nl.xb[i1] = as_float4(p1);
+    }
+    const bool keep0 = fluid_rec(p0.w) || walls_all;
+    const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
+    int cnt = 0;
+    int* __restrict__ col = nl.idx + nbr_col(nl, c);
+    const int cap = nl.cap;
+    auto visit = [&](int j) {
+        const V pj = ld_pos(X, (size_t)j);
+        const bool fj = fluid_rec(pj.w);
+        bool in = dist2(p0.x - pj.x, p0.y - pj.y, p0.z - pj.z) < k.kh2_list && j != i0 &&
+                  (keep0 || fj);
+        if (has1)
+            in = in || (dist2(p1.x - pj.x, p1.y - pj.y, p1.z - pj.z) < k.kh2_list && j != i1 &&
+                        (keep1 || fj));
+        if (in) {
+            if (cnt < cap) col[(size_t)cnt << 5] = j;
+            cnt++;
+        }
+    };
+    int x0, y0, z0;
+    cell_of_key(k.gx, k.gy, keys[i0], x0, y0, z0);
+    for_each_candidate<false>(k, cs, x0, y0, z0, [&](int j, unsigned) { visit(j); });
+    if (has1 && keys[i1] != keys[i0]) {
+        // the cells around the second particle's cell that the first walk did not cover
+        int x1, y1, z1;
+        cell_of_key(k.gx, k.gy, keys[i1], x1, y1, z1);
+#pragma unroll 1
+        for (int z = z1 - 1; z <= z1 + 1; z++) {
+            if ((unsigned)z >= (unsigned)k.gz) continue;
+#pragma unroll 1
+            for (int y = y1 - 1; y <= y1 + 1; y++) {
+                if ((unsigned)y >= (unsigned)k.gy) continue;
+                const int row = (z * k.gy + y) * k.gx;
+                const bool row_seen = abs(z - z0) <= 1 && abs(y - y0) <= 1;
+#pragma unroll 1
+                for (int x = max(x1 - 1, 0); x <= min(x1 + 1, k.gx - 1); x++) {
+                    if (row_seen && abs(x - x0) <= 1) continue;
+                    const int j0 = max(__ldg(cs + row + x), 0);
+                    const int j1 = min(__ldg(cs + row + x + 1), k.n);  // bounds guard only
+                    for (int j = j0; j < j1; j++) visit(j);
+                }
+            }
+        }
+    }
+    nl.count[c] = cnt;
+    raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
+}
+
+// Iterate a pair's union list: f(j, a, b) with the record of every slot.  Returns false (and
+// calls nothing) when the union overflowed the list.
+template <class P, class F>
+__device__ __forceinline__ bool visit_union(const NbrList& nl,
+                                            const vec4_t<typename P::T>* __restrict__ R, int c,
+                                            F&& f) {
+    using V = vec4_t<typename P::T>;
+    const int cnt = __ldg(nl.count + c);
+    if (cnt > nl.cap) return false;
+    const int* __restrict__ col = nl.idx + nbr_col(nl, c);
+    int j = cnt > 0 ? ld_slot(col) : 0;
+#pragma unroll 1
+    for (int e = 0; e < cnt; e++) {
+        const int jn = e + 1 < cnt ? ld_slot(col + ((size_t)(e + 1) << 5)) : 0;
+        V a, b;
+        ld_rec(R, j, a, b);
+        f(j, a, b);
+        j = jn;
+    }
+    return true;
+}
+
+template <class P, bool WRITE_SUMS>
+__device__ __forceinline__ void pass1_pair(const KParamsT<typename P::T>& k,
+                                           const ParticleSetT<typename P::T>& in,
+                                           const unsigned* __restrict__ keys,
+                                           const int* __restrict__ cs, const NbrList& nl,
+                                           const Pass1OutT<typename P::T>& out,
+                                           float* __restrict__ rhop_sum,
+                                           float* __restrict__ w_sum, int c) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const int i0 = 2 * c, i1 = 2 * c + 1;
+    const bool has1 = i1 < k.n;
+    Pass1Acc<P> a0, a1;
+    a0.load(in.rec, i0);
+    if (has1) a1.load(in.rec, i1);
+    auto one = [&](Pass1Acc<P>& acc, int i, int j, const V& a, const V& b) {
+        const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;
+        const T r2 = dist2(dx, dy, dz);
+        if (r2 < k.kh2 && j != i) acc.pair(k, a, b, dx, dy, dz, r2);
+    };
+    const bool listed = visit_union<P>(nl, in.rec, c, [&](int j, const V& a, const V& b) {
+        one(a0, i0, j, a, b);
+        if (has1) one(a1, i1, j, a, b);
+    });
+    if (!listed) {
+        visit_records<P, false, 1>(k, cs, keys, nl, in.xyz, in.rec, i0, a0.pi,
+                                   [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
+            a0.pair(k, aj, vj, dx, dy, dz, r2);
+        });
+        if (has1)
+            visit_records<P, false, 1>(k, cs, keys, nl, in.xyz, in.rec, i1, a1.pi,
+                                       [&](int, const V& aj, const V& vj, T dx, T dy, T dz,
+                                           T r2) { a1.pair(k, aj, vj, dx, dy, dz, r2); });
+    }
+    a0.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i0);
+    if (has1) a1.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i1);
+}
+
+template <class P, int MODE>
+__device__ __forceinline__ float pass2_pair(const KParamsT<typename P::T>& k, int c,
+                                            const ParticleSetT<typename P::T>& in,
+                                            const unsigned* __restrict__ keys,
+                                            const int* __restrict__ cs, const NbrList& nl,
+                                            const Pass1OutT<typename P::T>& p1,
+                                            float* __restrict__ rho_dt,
+                                            float* __restrict__ vel_dt, int wall_rates,
+                                            const ParticleSetT<typename P::T>& out,
+                                            unsigned* __restrict__ out_hash, unsigned* err) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const int i0 = 2 * c, i1 = 2 * c + 1;
+    const bool has1 = i1 < k.n;
+    Pass2Acc<P, MODE> a0, a1;
+    a0.load(k, p1, i0, wall_rates);
+    if (has1) a1.load(k, p1, i1, wall_rates);
+    const bool act1 = has1 && a1.active;
+    if (a0.active || act1) {
+        auto one = [&](Pass2Acc<P, MODE>& acc, int i, int j, const V& a, const V& b) {
+            const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;
+            const T r2 = dist2(dx, dy, dz);
+            if (r2 < k.kh2 && j != i) acc.pair(k, p1, j, a, b, dx, dy, dz, r2);
+        };
+        const bool listed = visit_union<P>(nl, p1.nrec, c, [&](int j, const V& a, const V& b) {
+            if (a0.active) one(a0, i0, j, a, b);
+            if (act1) one(a1, i1, j, a, b);
+        });
+        if (!listed) {
+            if (a0.active)
+                visit_records<P, false, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i0, a0.pi,
+                                           [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
+                                               T r2) { a0.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
+            if (act1)
+                visit_records<P, false, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i1, a1.pi,
+                                           [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
+                                               T r2) { a1.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
+        }
+    }
+    float d2 = pass2_finish<P, MODE>(k, i0, a0, in, keys, nl, rho_dt, vel_dt, wall_rates, out,
+                                     out_hash, err);
+    if (has1)
+        d2 = fmaxf(d2, pass2_finish<P, MODE>(k, i1, a1, in, keys, nl, rho_dt, vel_dt, wall_rates,
+                                             out, out_hash, err));
+    return d2;
+}
+
+template <class P>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
+k_nbr_build_pairs(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
+                  const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+                  int walls_all, unsigned* err, const unsigned* gate) {
+    if (gated_off(gate)) return;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < (k.n + 1) / 2) nbr_build_pair<P>(k, X, keys, cs, nl, walls_all, err, c);
+}
+
+template <class P, bool WRITE_SUMS>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
+k_pass1_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+              const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+              Pass1OutT<typename P::T> out, float* __restrict__ rhop_sum,
+              float* __restrict__ w_sum) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < (k.n + 1) / 2) pass1_pair<P, WRITE_SUMS>(k, in, keys, cs, nl, out, rhop_sum, w_sum, c);
+}
+
+template <class P, int MODE>
+__global__ void __launch_bounds__(NS_MAX_THREADS)
+k_pass2_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
+              const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
+              Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt,
+              float* __restrict__ vel_dt, int wall_rates, ParticleSetT<typename P::T> out,
+              unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (c < (k.n + 1) / 2)
+        d2 = pass2_pair<P, MODE>(k, c, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                 out_hash, err);
+    if (MODE == MODE_RATES || disp == nullptr) return;
+    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
+    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned m = s_max[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
+        if (m) atomicMax(disp, m);
+    }
+}
+
+// Pair mode applies to the FP32 and FP64 policies (mixed-precision slots carry each
+// neighbour's cell relative to one particle, which a pair of particles in two cells cannot
+// share).
+template <class P, class KP>
+inline bool use_pairs(const KP& k) {
+    return !P::kMixed && k.pairs;
+}
+template <class KP>
+inline dim3 pair_grid(const KP& k) {
+    const long pairs = ((long)k.n + 1) / 2;
+    return dim3((unsigned)((pairs + k.threads - 1) / k.threads > 0 ? (pairs + k.threads - 1) / k.threads : 1));
+}
+
 // Launch shape of a neighbour kernel: KParams::threads per block, KParams::ppt particles per
 // thread.
 template <class KP>
@@ -719,6 +1035,15 @@ void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const unsigned* keys, const int* cs, const NbrList& nl,
                   const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
+    if (LIST && use_pairs<P>(k)) {
+        if (rhop_sum && w_sum && P::kId == SPH_PREC_FP32)
+            k_pass1_pairs<P, true><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
+                                                                       rhop_sum, w_sum);
+        else
+            k_pass1_pairs<P, false><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
+                                                                        nullptr, nullptr);
+        return;
+    }
     if (k.ppt > 1)
         pass1_launch_gs<P, LIST, true>(k, in, keys, cs, nl, o, rhop_sum, w_sum, s);
     else
@@ -756,6 +1081,11 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                   unsigned* err, unsigned* disp, cudaStream_t s) {
+    if (nl && use_pairs<P>(k)) {
+        k_pass2_pairs<P, MODE><<<pair_grid(k), k.threads, 0, s>>>(
+            k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
+        return;
+    }
     if (k.ppt > 1)
         pass2_launch_gs<P, MODE, true>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
                                        out_hash, err, disp, s);
@@ -766,10 +1096,11 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
 
 }  // namespace
 
-int nbr_capacity_for(const sph_params& p, double skin) {
-    // 1.5x the particles of a lattice inside the list sphere, rounded up to 16
+int nbr_capacity_for(const sph_params& p, double skin, bool pairs) {
+    // 1.5x the particles of a lattice inside the list sphere (of the union of two spheres, about
+    // 1.4 times one, for a pair), rounded up to 16
     const double r = (double)p.kh * (1.0 + skin) / (double)p.dx;
-    const double lattice = 4.18879020478639 * r * r * r;
+    const double lattice = 4.18879020478639 * r * r * r * (pairs ? 1.4 : 1.0);
     int cap = (int)(1.5 * lattice) + 16;
     cap = (cap + 15) & ~15;
     return cap < 32 ? 32 : cap;
@@ -781,7 +1112,10 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    if (k.ppt > 1)
+    if (use_pairs<P>(k))
+        k_nbr_build_pairs<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                 walls_all, err, gate);
+    else if (k.ppt > 1)
         k_nbr_build<P, true><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl, walls_all,
                                                               err, gate);
     else

@@ -50,6 +50,7 @@ struct KParamsT {
     // most 256) and particles per thread.
     int threads;
     int ppt;
+    int pairs;  // two consecutive particles per thread over the union of their lists
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
     T h, inv_h, kh, kh2;

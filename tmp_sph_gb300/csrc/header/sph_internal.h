@@ -116,8 +116,9 @@ struct NbrList {
     int cap = 0;
     float4* xb = nullptr;
 };
-// List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
-int nbr_capacity_for(const sph_params& p, double skin = 0.0);
+// List slots per particle (per pair of particles with pairs): 1.5x the lattice particles within
+// kh (1 + skin), rounded up to 16.
+int nbr_capacity_for(const sph_params& p, double skin = 0.0, bool pairs = false);
 
 // Neighbour passes (equation/ns.cu), one instantiation per precision policy P.
 // nl == NULL walks the cells in every pass.
@@ -256,6 +257,7 @@ struct sph_ctx {
     int opt_cond_graph = 1;  // graph replay skips the rebuild kernels through conditional nodes
     int opt_threads = 128;   // neighbour kernels: threads per block
     int opt_ppt = 1;         // neighbour kernels: particles per thread
+    int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

@@ -244,6 +244,7 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.gz_local = c->gz_inst;
     k.threads = c->opt_threads;
     k.ppt = c->opt_ppt;
+    k.pairs = c->opt_pairs;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
@@ -418,8 +419,11 @@ void free_list(NbrList& nl) {
 
 cudaError_t alloc_list(sph_ctx* c) {
     // the option is rounded up to a multiple of 16, like the derived capacity
+    // pair mode keeps one union list per two particles (also used per particle by sph_ns, so
+    // the rows still cover every particle)
+    const bool pairs = c->opt_pairs != 0;
     const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
-                                       : nbr_capacity_for(c->P, c->skin);
+                                       : nbr_capacity_for(c->P, c->skin, pairs);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
     free_list(c->nl);
     // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
@@ -548,6 +552,14 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             c->opt_ppt = value;
             drop_graph(c);
             return SPH_OK;
+        case SPH_OPT_PAIRS:
+            c->opt_pairs = value != 0;
+            drop_graph(c);
+            if (alloc_list(c) != cudaSuccess) {
+                cudaGetLastError();
+                return SPH_ERR_NOMEM;
+            }
+            break;  // the list layout changed: rebuild
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_PRECISION: {
             if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && !prec_is_mixed(value))

@@ -231,7 +231,7 @@ def config_block(args, p, n):
             "parallelism": f"replicas x{dist_env()[0]}",
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
-            "graph_mode": args.graph_mode}
+            "graph_mode": args.graph_mode, "pairs": args.pairs}
 
 
 def run_batch(args):
@@ -259,6 +259,7 @@ def run_batch(args):
     sol = S.Solver(p, n, precision=args.precision)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+    sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload_instances(states, stream=stream)
@@ -333,6 +334,8 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="pick threads per block, particles per thread and skin with the "
                          "autotuner first (overrides --skin)")
+    ap.add_argument("--pairs", type=int, default=0, choices=[0, 1],
+                    help="two particles per thread over a union neighbour list (FP32, FP64)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -362,6 +365,7 @@ def main():
     sol = S.Solver(p, n, precision=args.precision)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+    sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)

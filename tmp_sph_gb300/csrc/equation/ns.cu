@@ -323,68 +323,6 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }
 
-// List build for two consecutive particles per thread.  When both lie in one cell (about 96%
-// of pairs) a single walk of the 27 cells serves both: each candidate position is loaded once
-// and tested against the two particles, and each particle's hits go to its own list in walk
-// order, exactly as its own walk would store them.  A pair in two cells walks twice.
-template <class P>
-__device__ __forceinline__ void nbr_build_two(const KParamsT<typename P::T>& k,
-                                              const vec4_t<typename P::T>* __restrict__ X,
-                                              const unsigned* __restrict__ keys,
-                                              const int* __restrict__ cs, const NbrList& nl,
-                                              int walls_all, unsigned* err, int c) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    const int i0 = 2 * c, i1 = 2 * c + 1;
-    if (i1 >= k.n || keys[i0] != keys[i1]) {
-        nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, i0);
-        if (i1 < k.n) nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, i1);
-        return;
-    }
-    const V p0 = X[i0], p1 = X[i1];
-    if (nl.xb) {
-        nl.xb[i0] = as_float4(p0);
-        nl.xb[i1] = as_float4(p1);
-    }
-    const bool keep0 = fluid_rec(p0.w) || walls_all;
-    const bool keep1 = fluid_rec(p1.w) || walls_all;
-    int n0 = 0, n1 = 0;
-    int* __restrict__ col0 = nl.idx + nbr_col(nl, i0);
-    int* __restrict__ col1 = nl.idx + nbr_col(nl, i1);
-    const int cap = nl.cap;
-    int cx, cy, cz;
-    cell_of_key(k.gx, k.gy, keys[i0], cx, cy, cz);
-    for_each_candidate<P::kMixed>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
-        const V pj = ld_pos(X, (size_t)j);
-        const bool fj = fluid_rec(pj.w);
-        const int slot = P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j;
-        T dx, dy, dz;
-        rel_pos<P>(k, p0, pj, code, dx, dy, dz);
-        if (dist2(dx, dy, dz) < k.kh2_list && j != i0 && (keep0 || fj)) {
-            if (n0 < cap) col0[(size_t)n0 << 5] = slot;
-            n0++;
-        }
-        rel_pos<P>(k, p1, pj, code, dx, dy, dz);
-        if (dist2(dx, dy, dz) < k.kh2_list && j != i1 && (keep1 || fj)) {
-            if (n1 < cap) col1[(size_t)n1 << 5] = slot;
-            n1++;
-        }
-    });
-    nl.count[i0] = n0;
-    nl.count[i1] = n1;
-    raise_flags(err, (n0 > cap || n1 > cap) ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
-}
-
-template <class P>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_nbr_build_two(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
-                const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-                int walls_all, unsigned* err, const unsigned* gate) {
-    if (gated_off(gate)) return;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < (k.n + 1) / 2) nbr_build_two<P>(k, X, keys, cs, nl, walls_all, err, c);
-}
-
 template <class P, bool GS>
 __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
@@ -1181,7 +1119,7 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
         k_nbr_build<P, true><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl, walls_all,
                                                               err, gate);
     else
-        k_nbr_build_two<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+        k_nbr_build<P, false><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
                                                                walls_all, err, gate);
     return cudaGetLastError();
 }

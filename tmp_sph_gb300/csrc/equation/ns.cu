@@ -26,8 +26,9 @@
 // once per list build and stores the hits of particle i, in walk order, in column i of its
 // warp's slot block (nbr_col); both passes then iterate only true neighbours, in the same
 // order, so the sums are the same as a walking pass.  The passes are limited by L1 data-stage
-// wavefronts (each lane gathers a different record): interleaving the slots makes a warp's
-// list read one line per step instead of one line per lane.  A particle with more hits than
+// wavefronts (each lane gathers a different record): interleaving the slots (in groups of four
+// per lane) makes a warp's list read four lines per four steps instead of one line per lane
+// and step.  A particle with more hits than
 // the list capacity is marked and walks the cells itself (same order again).
 //
 // With a Verlet skin the list is built with the cutoff kh(1 + skin) (kh2_list) on cells that
@@ -228,20 +229,46 @@ __device__ __forceinline__ void walk_pairs(const KParamsT<typename P::T>& k,
     });
 }
 
-// Column of particle i in the warp-interleaved list: entry c of i is col[32 c].  The 32
-// particles of a warp share one block of cap x 32 slots, so a warp reading entry c of all its
-// lanes touches one 128-byte line.
+// Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
+// col + 32 * 4g (col = the warp's block + 4 * lane).  The 32 particles of a warp share one block
+// of cap x 32 slots, so a warp reading slot group g of all its lanes touches four consecutive
+// lines (512 bytes) with one 16-byte load per lane, and the build stores four slots at a time.
 __device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
-    return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + (size_t)(i & 31);
+    return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + ((size_t)(i & 31) << 2);
 }
 
-// One list slot.  The slots stream past once per pass, so they are read without allocating
+// Four list slots.  The slots stream past once per pass, so they are read without allocating
 // in L1, which keeps L1 for the neighbour records (measured: passes 0.6% faster).
-__device__ __forceinline__ int ld_slot(const int* p) {
-    int v;
-    asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+__device__ __forceinline__ int4 ld_slots(const int* p) {
+    int4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
     return v;
 }
+
+// Appends slots to a list column four at a time (one 16-byte store per four slots).
+struct SlotWriter {
+    int* __restrict__ col;
+    int cap;
+    int cnt = 0;
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    __device__ __forceinline__ void put(int v) {
+        const int s = cnt & 3;
+        b0 = s == 0 ? v : b0;
+        b1 = s == 1 ? v : b1;
+        b2 = s == 2 ? v : b2;
+        b3 = s == 3 ? v : b3;
+        cnt++;
+        if (s == 3 && cnt <= cap)
+            *reinterpret_cast<int4*>(col + ((size_t)(cnt - 4) << 5)) = make_int4(b0, b1, b2, b3);
+    }
+    // the last, partial group (its unused slots are never read: count bounds the readers)
+    __device__ __forceinline__ void flush() {
+        if ((cnt & 3) && cnt < cap)
+            *reinterpret_cast<int4*>(col + ((size_t)(cnt & ~3) << 5)) = make_int4(b0, b1, b2, b3);
+    }
+};
 
 // Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one record
 // load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond the
@@ -262,10 +289,7 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             const int* __restrict__ col = nl.idx + nbr_col(nl, i);
-            int e = cnt > 0 ? ld_slot(col) : 0;
-#pragma unroll 1
-            for (int c = 0; c < cnt; c++) {
-                const int en = c + 1 < cnt ? ld_slot(col + ((size_t)(c + 1) << 5)) : 0;
+            auto one = [&](int e) {
                 const int j = P::kMixed ? (int)((unsigned)e & IDX_MASK) : e;
                 V a, b;
                 ld_rec(R, j, a, b);
@@ -273,7 +297,17 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
                 rel_pos<P>(k, pi, a, (unsigned)e >> CODE_SHIFT, dx, dy, dz);
                 const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
-                e = en;
+            };
+            int4 q = cnt > 0 ? ld_slots(col) : make_int4(0, 0, 0, 0);
+#pragma unroll 1
+            for (int c = 0; c < cnt; c += 4) {
+                // the next group is loaded one group ahead
+                const int4 qn = c + 4 < cnt ? ld_slots(col + ((size_t)(c + 4) << 5)) : q;
+                one(q.x);
+                if (c + 1 < cnt) one(q.y);
+                if (c + 2 < cnt) one(q.z);
+                if (c + 3 < cnt) one(q.w);
+                q = qn;
             }
             return;
         }
@@ -309,18 +343,15 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     const vec4_t<T> pi = X[i];
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
-    int cnt = 0;
-    int* __restrict__ col = nl.idx + nbr_col(nl, i);
-    const int cap = nl.cap;
+    SlotWriter w{nl.idx + nbr_col(nl, i), nl.cap};
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, k.kh2_list,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
-        if (keep_all || fluid_rec(pj.w)) {
-            if (cnt < cap) col[(size_t)cnt << 5] = P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j;
-            cnt++;
-        }
+        if (keep_all || fluid_rec(pj.w))
+            w.put(P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j);
     });
-    nl.count[i] = cnt;
-    raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
+    w.flush();
+    nl.count[i] = w.cnt;
+    raise_flags(err, w.cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }
 
 template <class P, bool GS>
@@ -795,9 +826,7 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
     }
     const bool keep0 = fluid_rec(p0.w) || walls_all;
     const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
-    int cnt = 0;
-    int* __restrict__ col = nl.idx + nbr_col(nl, c);
-    const int cap = nl.cap;
+    SlotWriter w{nl.idx + nbr_col(nl, c), nl.cap};
     auto visit = [&](int j) {
         const V pj = ld_pos(X, (size_t)j);
         const bool fj = fluid_rec(pj.w);
@@ -806,10 +835,7 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
         if (has1)
             in = in || (dist2(p1.x - pj.x, p1.y - pj.y, p1.z - pj.z) < k.kh2_list && j != i1 &&
                         (keep1 || fj));
-        if (in) {
-            if (cnt < cap) col[(size_t)cnt << 5] = j;
-            cnt++;
-        }
+        if (in) w.put(j);
     };
     int x0, y0, z0;
     cell_of_key(k.gx, k.gy, keys[i0], x0, y0, z0);
@@ -836,8 +862,9 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
             }
         }
     }
-    nl.count[c] = cnt;
-    raise_flags(err, cnt > cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
+    w.flush();
+    nl.count[c] = w.cnt;
+    raise_flags(err, w.cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }
 
 // Iterate a pair's union list: f(j, a, b) with the record of every slot.  Returns false (and
@@ -850,14 +877,20 @@ __device__ __forceinline__ bool visit_union(const NbrList& nl,
     const int cnt = __ldg(nl.count + c);
     if (cnt > nl.cap) return false;
     const int* __restrict__ col = nl.idx + nbr_col(nl, c);
-    int j = cnt > 0 ? ld_slot(col) : 0;
-#pragma unroll 1
-    for (int e = 0; e < cnt; e++) {
-        const int jn = e + 1 < cnt ? ld_slot(col + ((size_t)(e + 1) << 5)) : 0;
+    auto one = [&](int j) {
         V a, b;
         ld_rec(R, j, a, b);
         f(j, a, b);
-        j = jn;
+    };
+    int4 q = cnt > 0 ? ld_slots(col) : make_int4(0, 0, 0, 0);
+#pragma unroll 1
+    for (int e = 0; e < cnt; e += 4) {
+        const int4 qn = e + 4 < cnt ? ld_slots(col + ((size_t)(e + 4) << 5)) : q;
+        one(q.x);
+        if (e + 1 < cnt) one(q.y);
+        if (e + 2 < cnt) one(q.z);
+        if (e + 3 < cnt) one(q.w);
+        q = qn;
     }
     return true;
 }
@@ -993,11 +1026,7 @@ k_pass2_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
 
 // Pair mode applies to the FP32 and FP64 policies (mixed-precision slots carry each
 // neighbour's cell relative to one particle, which a pair of particles in two cells cannot
-// share).
-template <class P, class KP>
-inline bool use_pairs(const KP& k) {
-    return !P::kMixed && k.pairs;
-}
+// share); the launchers below dispatch on KParams::pairs.
 template <class KP>
 inline dim3 pair_grid(const KP& k) {
     const long pairs = ((long)k.n + 1) / 2;
@@ -1035,14 +1064,16 @@ void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const unsigned* keys, const int* cs, const NbrList& nl,
                   const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
-    if (LIST && use_pairs<P>(k)) {
-        if (rhop_sum && w_sum && P::kId == SPH_PREC_FP32)
-            k_pass1_pairs<P, true><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
-                                                                       rhop_sum, w_sum);
-        else
-            k_pass1_pairs<P, false><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
-                                                                        nullptr, nullptr);
-        return;
+    if constexpr (LIST && !P::kMixed) {
+        if (k.pairs) {
+            if (rhop_sum && w_sum && P::kId == SPH_PREC_FP32)
+                k_pass1_pairs<P, true><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
+                                                                           rhop_sum, w_sum);
+            else
+                k_pass1_pairs<P, false><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl,
+                                                                            o, nullptr, nullptr);
+            return;
+        }
     }
     if (k.ppt > 1)
         pass1_launch_gs<P, LIST, true>(k, in, keys, cs, nl, o, rhop_sum, w_sum, s);
@@ -1081,10 +1112,12 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                   unsigned* err, unsigned* disp, cudaStream_t s) {
-    if (nl && use_pairs<P>(k)) {
-        k_pass2_pairs<P, MODE><<<pair_grid(k), k.threads, 0, s>>>(
-            k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
-        return;
+    if constexpr (!P::kMixed) {
+        if (nl && k.pairs) {
+            k_pass2_pairs<P, MODE><<<pair_grid(k), k.threads, 0, s>>>(
+                k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
+            return;
+        }
     }
     if (k.ppt > 1)
         pass2_launch_gs<P, MODE, true>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
@@ -1112,10 +1145,14 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    if (use_pairs<P>(k))
-        k_nbr_build_pairs<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                                 walls_all, err, gate);
-    else if (k.ppt > 1)
+    if constexpr (!P::kMixed) {
+        if (k.pairs) {
+            k_nbr_build_pairs<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                     walls_all, err, gate);
+            return cudaGetLastError();
+        }
+    }
+    if (k.ppt > 1)
         k_nbr_build<P, true><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl, walls_all,
                                                               err, gate);
     else

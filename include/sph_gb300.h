@@ -97,7 +97,10 @@ typedef struct sph_params {
     float escape_min[3];     /* a fluid particle outside [escape_min, escape_max] ... */
     float escape_max[3];
     float escape_park[3];    /* ... is parked here with v = 0, p = 0, rho = rho0 */
-    int   reserved[8];
+    int   park_inactive;     /* 0: parked particles stay in the neighbour search at the
+                              * parking point (reference behaviour); 1: a fluid particle outside
+                              * the escape box leaves it (sorted after every cell, no pairs) */
+    int   reserved[7];
 } sph_params;
 
 /* Inputs from which sph_params_derive computes the derived constants with the same
@@ -289,7 +292,12 @@ int sph_ns(sph_ctx* ctx, float* s_pos, float* s_vel, float* s_rho, float* s_p,
            float* w_sum, void* stream);
 
 /* Load a particle state given in original order (AoS pos/vel [3n], rho, p, type [n]) from
- * host (from_host = 1) or device memory.  Resets the step counter. */
+ * host (from_host = 1) or device memory.  Resets the step counter.  After sph_step has run, an
+ * upload of the same number of particles (and, batched, the same offsets) keeps the cell order
+ * and neighbour lists: the next half step rebuilds them only if a particle moved more than half
+ * the skin from where the lists were built, or changed kind.  The results equal those of a
+ * continued sph_step run given the state it would hold (a loop of sph_step_host calls in FP32
+ * gives the bits of one resident run). */
 int sph_upload(sph_ctx* ctx, const float* pos, const float* vel, const float* rho,
                const float* p, const int* type, int n, int from_host, void* stream);
 /* Batched instances (no reference counterpart): n particles of n_inst independent simulations

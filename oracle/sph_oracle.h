@@ -35,7 +35,8 @@ typedef struct or_params {
     float tait_gamma, tait_b;
     int   clamp_density;
     float escape_min[3], escape_max[3], escape_park[3];
-    int   reserved[8];
+    int   park_inactive;    /* 1: fluid outside the escape box is left out of the cell lists */
+    int   reserved[7];
 } or_params;
 
 /* Derivation of the reference's host block, src/sph/sph_run.cu:60-101, for its hard-coded

@@ -37,6 +37,8 @@ def load(kind, case):
 def oracle_params(O, d):
     P = O.OrParams()
     for name, ctype in O.OrParams._fields_:
+        if name == "reserved" or "param_" + name not in d:
+            continue  # fields added after the fixtures were made keep their zero default
         v = d["param_" + name]
         setattr(P, name, ctype(*v.tolist()) if v.ndim else v.item())
     P.eos = 0

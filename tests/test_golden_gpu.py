@@ -19,6 +19,8 @@ def product_params(d):
     from tmp_sph_gb300 import api
     p = api.SphParams()
     for name, ctype in api.SphParams._fields_:
+        if name == "reserved" or "param_" + name not in d:
+            continue  # fields added after the fixtures were made keep their zero default
         v = d["param_" + name]
         setattr(p, name, ctype(*v.tolist()) if v.ndim else v.item())
     p.eos = api.SPH_EOS_LINEAR  # the reference kernels implement only the linear EOS

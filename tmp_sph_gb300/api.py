@@ -64,7 +64,8 @@ class SphParams(C.Structure):
         ("adh", C.c_float), ("mass", C.c_float), ("rho0", C.c_float), ("cs", C.c_float),
         ("eos", C.c_int), ("tait_gamma", C.c_float), ("tait_b", C.c_float),
         ("clamp_density", C.c_int), ("escape_min", F3), ("escape_max", F3),
-        ("escape_park", F3), ("reserved", C.c_int * 8),
+        ("escape_park", F3), ("park_inactive", C.c_int),
+        ("reserved", C.c_int * 7),
     ]
 
     def as_dict(self) -> dict:

@@ -218,8 +218,10 @@ __device__ __forceinline__ void walk_pairs(const KParamsT<typename P::T>& k,
                                            const vec4_t<typename P::T>& pi, typename P::T cut2,
                                            F&& f) {
     using T = typename P::T;
+    const unsigned key = keys[i];
+    if (inactive_key(k, key)) return;  // outside the neighbour search (park_inactive)
     int cx, cy, cz;
-    cell_of_key(k.gx, k.gy, keys[i], cx, cy, cz);
+    cell_of_key(k.gx, k.gy, key, cx, cy, cz);
     for_each_candidate<P::kMixed>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
         const vec4_t<T> pj = ld_pos(X, (size_t)STRIDE * (size_t)j);
         T dx, dy, dz;
@@ -654,8 +656,16 @@ __device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, 
         const int inst = k.inst_cells ? in.inst[i] : 0;
         if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
-        out_hash[i] = resident_key(k, inst, nxm.x, nxm.y, nxm.z, &f);
+        const unsigned nk = slot_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f);
+        out_hash[i] = nk;
         raise_flags(err, f);
+        if (k.park_inactive) {
+            // a particle that leaves (or rejoins) the neighbour search needs new lists; one
+            // outside it is in no list, so its moves do not count
+            const bool now = inactive_key(k, nk);
+            if (now != inactive_key(k, keys[i])) return 3.0e38f;
+            if (now) return 0.f;
+        }
         if (!fi || !nl.xb) return 0.f;
         const float4 xb = nl.xb[i];
         return dist2(px - xb.x, py - xb.y, pz - xb.z);
@@ -724,8 +734,16 @@ __device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, 
         const int inst = k.inst_cells ? in.inst[i] : 0;
         if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
-        out_hash[i] = resident_key(k, inst, np.x, np.y, np.z, &f);
+        const unsigned nk = slot_key(k, inst, fi, np.x, np.y, np.z, &f);
+        out_hash[i] = nk;
         raise_flags(err, f);
+        if (k.park_inactive) {
+            // a particle that leaves (or rejoins) the neighbour search needs new lists; one
+            // outside it is in no list, so its moves do not count
+            const bool now = inactive_key(k, nk);
+            if (now != inactive_key(k, keys[i])) return 3.0e38f;
+            if (now) return 0.f;
+        }
         if (!fi || !nl.xb) return 0.f;
         const float4 xb = nl.xb[i];
         return (float)dist2(np.x - (T)xb.x, np.y - (T)xb.y, np.z - (T)xb.z);
@@ -817,12 +835,17 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
     using T = typename P::T;
     using V = vec4_t<T>;
     const int i0 = 2 * c, i1 = 2 * c + 1;
-    const bool has1 = i1 < k.n;
     const V p0 = X[i0];
-    const V p1 = has1 ? X[i1] : p0;
+    const V p1 = i1 < k.n ? X[i1] : p0;
     if (nl.xb) {
         nl.xb[i0] = as_float4(p0);
-        if (has1) nl.xb[i1] = as_float4(p1);
+        if (i1 < k.n) nl.xb[i1] = as_float4(p1);
+    }
+    // particles outside the neighbour search (park_inactive) sort last: take no candidates
+    const bool has1 = i1 < k.n && !inactive_key(k, keys[i1]);
+    if (inactive_key(k, keys[i0])) {
+        nl.count[c] = 0;
+        return;
     }
     const bool keep0 = fluid_rec(p0.w) || walls_all;
     const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
@@ -910,14 +933,17 @@ __device__ __forceinline__ void pass1_pair(const KParamsT<typename P::T>& k,
     Pass1Acc<P> a0, a1;
     a0.load(in.rec, i0);
     if (has1) a1.load(in.rec, i1);
+    // particles outside the neighbour search (park_inactive) take no pairs
+    const bool use0 = !inactive_key(k, keys[i0]);
+    const bool use1 = has1 && !inactive_key(k, keys[i1]);
     auto one = [&](Pass1Acc<P>& acc, int i, int j, const V& a, const V& b) {
         const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;
         const T r2 = dist2(dx, dy, dz);
         if (r2 < k.kh2 && j != i) acc.pair(k, a, b, dx, dy, dz, r2);
     };
     const bool listed = visit_union<P>(nl, in.rec, c, [&](int j, const V& a, const V& b) {
-        one(a0, i0, j, a, b);
-        if (has1) one(a1, i1, j, a, b);
+        if (use0) one(a0, i0, j, a, b);
+        if (use1) one(a1, i1, j, a, b);
     });
     if (!listed) {
         visit_records<P, false, 1>(k, cs, keys, nl, in.xyz, in.rec, i0, a0.pi,
@@ -950,7 +976,9 @@ __device__ __forceinline__ float pass2_pair(const KParamsT<typename P::T>& k, in
     Pass2Acc<P, MODE> a0, a1;
     a0.load(k, p1, i0, wall_rates);
     if (has1) a1.load(k, p1, i1, wall_rates);
-    const bool act1 = has1 && a1.active;
+    // particles outside the neighbour search (park_inactive) take no pairs
+    a0.active = a0.active && !inactive_key(k, keys[i0]);
+    const bool act1 = has1 && a1.active && !inactive_key(k, keys[i1]);
     if (a0.active || act1) {
         auto one = [&](Pass2Acc<P, MODE>& acc, int i, int j, const V& a, const V& b) {
             const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;

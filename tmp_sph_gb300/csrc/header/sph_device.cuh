@@ -68,6 +68,9 @@ struct KParamsT {
     int clamp_density;
     T esc_min_x, esc_min_y, esc_min_z, esc_max_x, esc_max_y, esc_max_z;
     T park_x, park_y, park_z;
+    // 1: a fluid particle outside the escape box takes key num_cells (sorted after every cell,
+    // outside the neighbour search); 0: it is parked and stays in the search (reference)
+    int park_inactive;
 };
 using KParams = KParamsT<float>;
 
@@ -184,6 +187,21 @@ template <class KT, class PT>
 __device__ __forceinline__ bool escaped(const KParamsT<KT>& k, PT x, PT y, PT z) {
     return x > (PT)k.esc_max_x || x < (PT)k.esc_min_x || y > (PT)k.esc_max_y ||
            y < (PT)k.esc_min_y || z > (PT)k.esc_max_z || z < (PT)k.esc_min_z;
+}
+
+// Sort key of a resident slot: its cell, or, with park_inactive, num_cells for a fluid particle
+// outside the escape box — past every cell's range, so it is nobody's candidate and walks no
+// cells itself.
+template <class KT, class PT>
+__device__ __forceinline__ unsigned slot_key(const KParamsT<KT>& k, int inst, bool fluid, PT x,
+                                             PT y, PT z, unsigned* flag) {
+    if (k.park_inactive && fluid && escaped(k, x, y, z)) return (unsigned)k.num_cells;
+    return resident_key(k, inst, x, y, z, flag);
+}
+
+template <class KT>
+__device__ __forceinline__ bool inactive_key(const KParamsT<KT>& k, unsigned key) {
+    return key >= (unsigned)k.num_cells;
 }
 
 __device__ __forceinline__ bool is_fluid(float typef) { return typef == 1.0f; }

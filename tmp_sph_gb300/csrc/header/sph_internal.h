@@ -6,6 +6,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "sph_gb300.h"
 #include "sph_device.cuh"
 
@@ -174,6 +176,15 @@ cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float*
                                   const int* type, const int* inst_off, int n_inst,
                                   ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
                                   cudaStream_t s);
+// Upload original-order arrays into the current sorted order (slot k takes particle id[k]),
+// measuring displacements from the list-build positions xb into *disp; a changed particle
+// kind sets *force.
+template <class P>
+cudaError_t launch_upload_sorted(const KParamsT<typename P::T>& k, const float* pos,
+                                 const float* vel, const float* rho, const float* p,
+                                 const int* type, const unsigned* keys, const float4* xb,
+                                 ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
+                                 unsigned* disp, unsigned* force, cudaStream_t s);
 template <class P>
 cudaError_t launch_download_convert(const KParamsT<typename P::T>& k,
                                     const ParticleSetT<typename P::T>& src, float* pos,
@@ -211,6 +222,10 @@ struct sph_ctx {
     int device = 0;
     bool loaded = false;
     bool rehash = false;  // the grid changed since the keys in hash_x were computed
+    // y is in the cell order its keys_sorted, cell starts and neighbour lists were built for,
+    // on the current grid and options (a half step ran since the last upload or change), so an
+    // upload of the same particles can go straight into that order
+    bool sorted = false;
     long long steps = 0;
 
     int prec = SPH_PREC_FP32;   // SPH_OPT_PRECISION
@@ -242,6 +257,7 @@ struct sph_ctx {
     sph::NbrList nl;
     sph_params Pi{};                 // internal grid: cells of kh (1 + skin), instances stacked
     int n_inst = 1;                  // batched instances (sph_upload_instances)
+    std::vector<int> inst_off_h;     // their offsets, as last uploaded
     int gz_inst = 0;                 // grid height of one instance
     int* inst_off = nullptr;         // [SPH_MAX_INSTANCES + 1] instance particle offsets
     double skin = 0.1;               // list skin as a fraction of the support radius kh

@@ -248,7 +248,8 @@ __global__ void k_cell_mark(const unsigned* __restrict__ keys, int n, int num_ce
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned key = keys[k];
-    if ((k == 0 || keys[k - 1] != key) && key < (unsigned)num_cells) cs[key] = k;
+    // key num_cells starts the tail of slots outside every cell (park_inactive)
+    if ((k == 0 || keys[k - 1] != key) && key <= (unsigned)num_cells) cs[key] = k;
 }
 
 constexpr int FILL_THREADS = 256;
@@ -281,7 +282,7 @@ k_cell_fill(int* __restrict__ cs, int num_cells, const unsigned* __restrict__ ke
 #pragma unroll
     for (int j = 0; j < FILL_PER_THREAD; j++) {
         long c = cbase + j;
-        v[j] = c < num_cells ? cs[c] : (c == num_cells ? n : BIG);
+        v[j] = c < num_cells ? cs[c] : (c == num_cells ? min(cs[c], n) : BIG);
     }
     int tmin = v[FILL_PER_THREAD - 1];
 #pragma unroll
@@ -457,7 +458,7 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     dst.rec[2 * (size_t)i + 1] = make4<T>(vx, vy, vz, signed_rho_t<T>(t, (T)rho[i]));
     if constexpr (P::kMixed) {
         const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[i] - (double)kp.rho0};
-        const unsigned h = resident_key(kp, inst, xm.x, xm.y, xm.z, &f);
+        const unsigned h = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
         dst.xm[i] = xm;
         dst.txm[i] = xm;
         dst.rec[2 * (size_t)i] = offsets_in_cell(kp, h, xm, p[i]);
@@ -465,9 +466,75 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     } else {
         dst.rec[2 * (size_t)i] = make4<T>(x, y, z, (T)p[i]);
         dst.tpos[i] = make4<T>(x, y, z, (T)rho[i]);
-        hash[i] = resident_key(kp, inst, (T)x, (T)y, (T)z, &f);
+        hash[i] = slot_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f);
     }
     raise_flags(err, f);
+}
+
+// Upload into the current cell order.  Slot k of the sorted live set takes particle id[k] of
+// the original-order arrays, so the cell starts and neighbour lists built for that order stay
+// in use.  Every slot measures its squared displacement from the position its list was built
+// at (xb) into *disp (the half step's rebuild test then decides, as after a pass-2 update), and
+// a particle whose kind changed (boundary lists hold fluid neighbours only) sets *force.
+// Mixed precision: positions become offsets in the slot's sorted cell, as pass 2 writes them.
+template <class P>
+__global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restrict__ pos,
+                                const float* __restrict__ vel, const float* __restrict__ rho,
+                                const float* __restrict__ p, const int* __restrict__ type,
+                                const unsigned* __restrict__ keys, const float4* __restrict__ xb,
+                                ParticleSetT<typename P::T> dst, unsigned* __restrict__ hash,
+                                unsigned* err, unsigned* disp, unsigned* force) {
+    using T = typename P::T;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (k < kp.n) {
+        const int r = dst.id[k];
+        if ((unsigned)r < (unsigned)kp.n) {
+            const float x = pos[3 * r], y = pos[3 * r + 1], z = pos[3 * r + 2];
+            const float vx = vel[3 * r], vy = vel[3 * r + 1], vz = vel[3 * r + 2];
+            const int t = type[r];
+            if (t != dst.type[k]) atomicOr(force, 1u);
+            const int inst = dst.inst ? dst.inst[k] : 0;
+            unsigned f = 0;
+            dst.type[k] = t;
+            dst.tvel[k] = make4<T>(vx, vy, vz, T(0));
+            const T srho = signed_rho_t<T>(t, (T)rho[r]);
+            dst.rec[2 * (size_t)k + 1] = make4<T>(vx, vy, vz, srho);
+            vec4_t<T> a;
+            unsigned nk;
+            const unsigned key = keys[k];
+            if constexpr (P::kMixed) {
+                const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[r] - (double)kp.rho0};
+                dst.xm[k] = xm;
+                dst.txm[k] = xm;
+                a = offsets_in_cell(kp, key, xm, p[r]);
+                nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
+            } else {
+                a = make4<T>(x, y, z, (T)p[r]);
+                dst.tpos[k] = make4<T>(x, y, z, (T)rho[r]);
+                nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f);
+            }
+            hash[k] = nk;
+            // a particle entering or leaving the neighbour search (park_inactive) needs new
+            // lists; one that stays outside it is in no list
+            const bool out_now = inactive_key(kp, nk);
+            if (out_now != inactive_key(kp, key)) atomicOr(force, 1u);
+            dst.rec[2 * (size_t)k] = a;
+            dst.xyz[k] = make4<T>(a.x, a.y, a.z, srho > T(0) ? T(1) : T(-1));
+            raise_flags(err, f);
+            if (xb && !out_now) {
+                const float4 b = xb[k];
+                const float dx = (float)a.x - b.x, dy = (float)a.y - b.y, dz = (float)a.z - b.z;
+                d2 = dx * dx + dy * dy + dz * dz;
+                if (!(d2 <= 3.0e38f)) d2 = 3.0e38f;  // NaN or overflow: rebuild
+            }
+        } else {
+            atomicOr(force, 1u);  // a consistent permutation never takes this
+        }
+    }
+    // non-negative floats order like their bit patterns; blockDim is 256, every thread gets here
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(disp, m);
 }
 
 // Cell keys of a resident set on the current grid (after the grid changed under it).
@@ -478,12 +545,13 @@ __global__ void k_rehash(KParamsT<typename P::T> kp, ParticleSetT<typename P::T>
     if (i >= kp.n) return;
     unsigned f = 0;
     const int inst = set.inst ? set.inst[i] : 0;
+    const bool fluid = set.type[i] == SPH_TYPE_FLUID;
     if constexpr (P::kMixed) {
         const dvec4 q = set.xm[i];
-        hash[i] = resident_key(kp, inst, q.x, q.y, q.z, &f);
+        hash[i] = slot_key(kp, inst, fluid, q.x, q.y, q.z, &f);
     } else {
         const auto q = set.xyz[i];
-        hash[i] = resident_key(kp, inst, q.x, q.y, q.z, &f);
+        hash[i] = slot_key(kp, inst, fluid, q.x, q.y, q.z, &f);
     }
     raise_flags(err, f);
 }
@@ -694,6 +762,18 @@ cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float*
 }
 
 template <class P>
+cudaError_t launch_upload_sorted(const KParamsT<typename P::T>& k, const float* pos,
+                                 const float* vel, const float* rho, const float* p,
+                                 const int* type, const unsigned* keys, const float4* xb,
+                                 ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
+                                 unsigned* disp, unsigned* force, cudaStream_t s) {
+    if (k.n <= 0) return cudaSuccess;
+    k_upload_sorted<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, pos, vel, rho, p, type, keys, xb,
+                                                            dst, hash, err, disp, force);
+    return cudaGetLastError();
+}
+
+template <class P>
 cudaError_t launch_rehash(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& set,
                           unsigned* hash, unsigned* err, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
@@ -732,6 +812,11 @@ cudaError_t launch_download_f64(const KParamsT<typename P::T>& k,
                                                   const int*, const int*, int,                  \
                                                   ParticleSetT<P::T>, unsigned*, unsigned*,     \
                                                   cudaStream_t);                                \
+    template cudaError_t launch_upload_sorted<P>(const KParamsT<P::T>&, const float*,           \
+                                                 const float*, const float*, const float*,      \
+                                                 const int*, const unsigned*, const float4*,    \
+                                                 ParticleSetT<P::T>, unsigned*, unsigned*,      \
+                                                 unsigned*, unsigned*, cudaStream_t);           \
     template cudaError_t launch_rehash<P>(const KParamsT<P::T>&, const ParticleSetT<P::T>&,     \
                                           unsigned*, unsigned*, cudaStream_t);                  \
     template cudaError_t launch_download_convert<P>(const KParamsT<P::T>&,                      \

@@ -73,6 +73,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.park_x = p.escape_park[0];
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
+    k.park_inactive = p.park_inactive;
     return k;
 }
 
@@ -133,6 +134,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.park_x = p.escape_park[0];
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
+    k.park_inactive = p.park_inactive;
     return k;
 }
 

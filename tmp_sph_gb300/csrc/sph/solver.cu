@@ -280,7 +280,8 @@ struct CondCapture {
 template <class P>
 cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStream_t s,
                           cudaEvent_t* ev) {
-    const int bits = key_bits_for(c->Pi.num_cells);
+    // with park_inactive, key num_cells marks the slots outside the neighbour search
+    const int bits = key_bits_for(c->Pi.num_cells + (c->P.park_inactive ? 1 : 0));
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
     cudaError_t e;
@@ -407,6 +408,7 @@ cudaError_t build_conditional_graph(sph_ctx* c, cudaStream_t s, cudaGraph_t* out
 
 // Next half step rebuilds the cell and neighbour lists whatever the displacement.
 cudaError_t force_rebuild(sph_ctx* c, cudaStream_t s) {
+    c->sorted = false;
     return cudaMemsetAsync(c->rb + 2, 1, sizeof(unsigned), s);
 }
 
@@ -519,6 +521,7 @@ extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     c->Pi = pi;
     c->gz_inst = gz_local;
     c->rehash = c->loaded;
+    c->sorted = false;
     drop_graph(c);
     // and the neighbour list, when the support radius holds more lattice neighbours
     if (alloc_list(c) != cudaSuccess) {
@@ -569,6 +572,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             free_state(c);
             c->prec = value;
             c->loaded = false;
+            c->sorted = false;
             c->n = 0;
             if (alloc_state(c) != cudaSuccess) {
                 cudaGetLastError();
@@ -611,6 +615,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
         default: return SPH_ERR_ARG;
     }
     // the cell and neighbour lists no longer match: rebuild them next half step
+    c->sorted = false;
     return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -629,6 +634,12 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
             if (offsets[b + 1] < offsets[b]) return SPH_ERR_ARG;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    // the same particles again (same count and instances) after a half step: keep the cell
+    // order, cell starts and neighbour lists, and let the displacement test decide
+    const bool same_inst = n_inst == c->n_inst &&
+                           (n_inst == 1 || std::equal(offsets, offsets + n_inst + 1,
+                                                      c->inst_off_h.begin(), c->inst_off_h.end()));
+    const bool into_order = c->sorted && c->loaded && !c->rehash && n == c->n && n > 0 && same_inst;
     if (n_inst != c->n_inst) {
         sph_params pi;
         int gz_local;
@@ -639,9 +650,12 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
         c->n_inst = n_inst;
         drop_graph(c);
     }
-    if (n_inst > 1 && cudaMemcpyAsync(c->inst_off, offsets, (size_t)(n_inst + 1) * sizeof(int),
-                                      cudaMemcpyHostToDevice, s) != cudaSuccess)
+    if (n_inst > 1 && !into_order &&
+        cudaMemcpyAsync(c->inst_off, offsets, (size_t)(n_inst + 1) * sizeof(int),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
         return SPH_ERR_CUDA;
+    if (n_inst > 1) c->inst_off_h.assign(offsets, offsets + n_inst + 1);
+    else c->inst_off_h.clear();
     if (n != c->n) drop_graph(c);
     c->n = n;
     c->steps = 0;
@@ -668,6 +682,18 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
             (e = cudaMemcpyAsync(stype, type, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
             return SPH_ERR_CUDA;
         dpos = spos; dvel = svel; drho = srho; dp = sp; dtype = stype;
+    }
+    if (into_order) {
+        // rb[1] restarts from the uploaded positions; a pending forced rebuild (rb[2]) stays
+        if (cudaMemsetAsync(c->rb + 1, 0, sizeof(unsigned), s) != cudaSuccess) return SPH_ERR_CUDA;
+        const NbrList* nl = list_for(c);
+        return to_status(with_prec(c, [&](auto tag) {
+            using P = decltype(tag);
+            return launch_upload_sorted<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho,
+                                           dp, dtype, c->keys_sorted, nl ? nl->xb : nullptr,
+                                           State<P>::y(c), c->hash_x, c->err, c->rb + 1,
+                                           c->rb + 2, s);
+        }));
     }
     // the state goes straight into the live set, hashed on the solver's grid; the first half
     // step sorts it
@@ -847,9 +873,19 @@ extern "C" int sph_snapshot_begin(sph_ctx* c, float* pos, float* vel, float* rho
     return SPH_OK;
 }
 
+static int step_impl(sph_ctx* c, int nsteps, void* stream);
+
 extern "C" int sph_step(sph_ctx* c, int nsteps, void* stream) {
     if (!c || nsteps < 0) return SPH_ERR_ARG;
     if (!c->loaded) return SPH_ERR_STATE;
+    const int st = step_impl(c, nsteps, stream);
+    // after a half step the live set is in the order of its cell and neighbour lists
+    if (st != SPH_OK) c->sorted = false;
+    else if (nsteps > 0 && c->n > 0) c->sorted = true;
+    return st;
+}
+
+static int step_impl(sph_ctx* c, int nsteps, void* stream) {
     if (c->n == 0 || nsteps == 0) {
         c->steps += nsteps;
         return SPH_OK;
@@ -999,6 +1035,7 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
         return SPH_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     KParams k = make_kparams(c->P, n);
+    k.park_inactive = 0;  // the drop-in takes the caller's cells as they are
     cudaError_t e;
     if ((e = launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->x, c->keys_sorted,
                                c->err, s)) != cudaSuccess)

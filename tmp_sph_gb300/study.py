@@ -10,7 +10,11 @@ FP64 run of the same solver.
 
 prints one JSON object.  The default case is the 765,828-particle dam break (tank
 1.0 x 0.5 x 0.6 m, water 0.4 x 0.5 x 0.3 m, dx 5 mm); the default probe is the wall pressure at
-(1.0, 0.25, 0.05) m on the far wall.
+(1.0, 0.25, 0.05) m on the far wall.  Water-height gauges (the reference's H2 and H4 at
+x = 2.228 and 0.582 m, y = 0.5 m, src/io/io.cu:236-256) are added with --gauges x y zmax ...:
+
+    python -m tmp_sph_gb300.study --case obstacle --probe 2.31 0.5 0.03 \
+        --gauges 2.228 0.5 0.4 0.582 0.5 0
 """
 from __future__ import annotations
 
@@ -32,12 +36,17 @@ def rel_l2(a, b, floor=0.0) -> float:
 
 
 def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stream,
-                  checkpoints=()) -> dict:
+                  checkpoints=(), gauges=()) -> dict:
     import torch
     n = len(st["rho"])
     probes = [(api.SPH_PROBE_FRONT, 0, 0, 0, 0, 0),
               (api.SPH_PROBE_PRESSURE, *probe_xyz, 0, 0)]
+    # water-height gauges, 1.5 dx wide as the reference's (src/io/io.cu:239-252)
+    probes += [(api.SPH_PROBE_HEIGHT, gx, gy, 0, 1.5 * float(p.dx), zmax)
+               for gx, gy, zmax in gauges]
     series = {"t": [], "front_x": [], "wall_p": [], "kinetic": [], "potential": []}
+    for g in range(len(gauges)):
+        series[f"gauge_{g}"] = []
     with S.Solver(p, n, precision=precision) as sol:
         sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         done = 0
@@ -53,6 +62,8 @@ def run_precision(st, p, precision: str, steps: int, every: int, probe_xyz, stre
             series["wall_p"].append(vals[1])
             series["kinetic"].append(stats["kinetic"])
             series["potential"].append(stats["potential"])
+            for g in range(len(gauges)):
+                series[f"gauge_{g}"].append(vals[2 + g])
             if done >= steps:
                 break
             k = min(every, steps - done)
@@ -86,29 +97,30 @@ def compare(res: dict, ref: dict, st: dict) -> dict:
     out = {f"step_{k}": field_errors(res["snaps"][k], ref["snaps"][k], st)
            for k in sorted(res["snaps"]) if k in ref["snaps"]}
     sa, sb = res["series"], ref["series"]
-    out["series"] = {
-        "front_x": rel_l2(sa["front_x"], sb["front_x"]),
-        "wall_p": rel_l2(sa["wall_p"], sb["wall_p"]),
-        "kinetic": rel_l2(sa["kinetic"], sb["kinetic"]),
-    }
+    out["series"] = {k: rel_l2(sa[k], sb[k]) for k in sa
+                     if k not in ("t", "potential") and k in sb}
     return out
 
 
-def study(case: str, steps: int, every: int, probe_xyz, precisions, checkpoints=()) -> dict:
+def study(case: str, steps: int, every: int, probe_xyz, precisions, checkpoints=(),
+          gauges=()) -> dict:
     import torch
     st, p = cases.build(case, physics="config")
     stream = torch.cuda.Stream()
-    runs = {prec: run_precision(st, p, prec, steps, every, probe_xyz, stream, checkpoints)
+    runs = {prec: run_precision(st, p, prec, steps, every, probe_xyz, stream, checkpoints,
+                                gauges)
             for prec in precisions}
     ref = runs.get("fp64")
     report = {"case": case, "particles": len(st["rho"]), "fluid": int((st["type"] == 1).sum()),
               "steps": steps, "dt_s": float(p.dt), "sample_every": every,
-              "wall_probe_m": list(probe_xyz), "runs": {}}
+              "wall_probe_m": list(probe_xyz), "gauges_m": [list(g) for g in gauges],
+              "runs": {}}
     for prec, r in runs.items():
         entry = {"seconds": r["seconds"], "ms_per_step": 1e3 * r["seconds"] / max(1, steps),
                  "device_error_flags": r["flags"], "list_rebuilds": r["rebuilds"],
                  "final_front_x": r["series"]["front_x"][-1],
-                 "final_wall_p": r["series"]["wall_p"][-1]}
+                 "final_wall_p": r["series"]["wall_p"][-1],
+                 "max_wall_p": max(r["series"]["wall_p"])}
         if ref is not None and prec != "fp64":
             entry["rel_l2_vs_fp64"] = compare(r, ref, st)
         report["runs"][prec] = entry
@@ -126,10 +138,15 @@ def main(argv=None) -> None:
     ap.add_argument("--precisions", nargs="+", default=["fp64", "fp32", "mixed", "mixed_comp"])
     ap.add_argument("--compare-at", type=int, nargs="*", default=[1000],
                     help="also compare the fields after these step counts")
+    ap.add_argument("--gauges", type=float, nargs="*", default=[],
+                    help="water-height gauges as x y zmax triples (zmax 0: no cap)")
     ap.add_argument("--out", default=None, help="also write the JSON here")
     args = ap.parse_args(argv)
+    if len(args.gauges) % 3:
+        ap.error("--gauges takes x y zmax triples")
+    gauges = [tuple(args.gauges[i:i + 3]) for i in range(0, len(args.gauges), 3)]
     rep = study(args.case, args.steps, args.every, tuple(args.probe), args.precisions,
-                args.compare_at)
+                args.compare_at, gauges)
     text = json.dumps(rep)
     if args.out:
         with open(args.out, "w") as f:

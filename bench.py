@@ -231,7 +231,8 @@ def config_block(args, p, n):
             "parallelism": f"replicas x{dist_env()[0]}",
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
-            "graph_mode": args.graph_mode, "pairs": args.pairs}
+            "graph_mode": args.graph_mode, "pairs": args.pairs,
+            "lanes_per_particle": args.lanes}
 
 
 def run_batch(args):
@@ -260,6 +261,7 @@ def run_batch(args):
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
+    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload_instances(states, stream=stream)
@@ -336,6 +338,8 @@ def main():
                          "autotuner first (overrides --skin)")
     ap.add_argument("--pairs", type=int, default=0, choices=[0, 1],
                     help="two particles per thread over a union neighbour list (FP32, FP64)")
+    ap.add_argument("--lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
+                    help="lanes per particle in the neighbour-list kernels")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -366,6 +370,7 @@ def main():
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
+    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
@@ -415,6 +420,7 @@ def main():
     def time_precision(precision: str, steps: int) -> dict:
         v = S.Solver(p, n, precision=precision)
         v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+        v.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
         v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         v.step(3, stream=stream)
         torch.cuda.synchronize()

@@ -257,6 +257,9 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_PAIRS 11  /* 1: the neighbour kernels take two consecutive particles per thread
                              over the union of their neighbour lists, gathering each neighbour
                              record once for both (FP32 and FP64; ignored in mixed precision) */
+#define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in the list kernels:
+                             1 (one thread per particle), 2, 4, 8 or 16 (a group of lanes shares a
+                             particle's list and reduces its sums; not with SPH_OPT_PAIRS) */
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */

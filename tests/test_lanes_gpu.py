@@ -1,0 +1,143 @@
+"""GPU tests of the lane-group list kernels (SPH_OPT_LANES_PER_PARTICLE): G lanes share one
+particle's neighbour list and reduce their partial sums with shuffles.  The list holds the same
+entries in the same order as the one-lane build, and the sums associate differently, so the
+results match the oracle and the one-lane kernels to FP32 rounding; for a fixed G they are
+deterministic and independent of the block size, of graph replay, and of batching."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from test_solver_gpu import field_errors
+
+pytestmark = pytest.mark.gpu
+
+LANES = [2, 4, 8, 16]
+
+
+def run(st, p, nsteps, lanes, precision="fp32", opts=None, graph=True):
+    import torch
+    from tmp_sph_gb300 import api, solver as S
+    s = torch.cuda.Stream()
+    with S.Solver(p, len(st["rho"]), precision=precision) as sol:
+        sol.set_option(api.SPH_OPT_USE_GRAPH, int(graph))
+        sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, lanes)
+        for k, v in (opts or {}).items():
+            sol.set_option(k, v)
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(nsteps, stream=s)
+        out = sol.download(stream=s)
+        out["flags"] = sol.error_flags(stream=s)
+        out["rebuilds"] = sol.rebuild_count(stream=s)
+    return out
+
+
+def small(perturb=False):
+    from tmp_sph_gb300 import cases
+    from gpu_util import perturbed
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    if perturb:
+        st = perturbed(st, vamp=2.0, ramp=0.0)
+    return st, p
+
+
+@pytest.mark.parametrize("lanes", LANES)
+def test_lanes_match_oracle(sphlib, oracle, cuda, report, lanes):
+    st, p = small()
+    P = oracle.params_like(p)
+    for nsteps, tol, tol_disp in ((1, 2e-5, 5e-4), (20, 2e-4, 2e-4)):
+        out = run(st, p, nsteps, lanes)
+        ref = oracle.run(P, st, nsteps)
+        assert out["flags"] == 0
+        e = field_errors(out, ref, st)
+        for k, v in e.items():
+            report(f"lanes {lanes}, {nsteps} steps {k}", v, tol_disp if k == "disp" else tol)
+        assert e["disp"] < tol_disp and all(v < tol for k, v in e.items() if k != "disp"), e
+        wl = st["type"] != 1
+        assert np.array_equal(out["pos"][wl], st["pos"][wl])
+
+
+@pytest.mark.parametrize("lanes", [4, 8])
+def test_lanes_close_to_one_lane(sphlib, cuda, report, lanes):
+    """Fast flow (list rebuilds along the way): the lane groups follow the one-lane kernels to
+    FP32 rounding, with the same rebuild schedule."""
+    st, p = small(perturb=True)
+    a = run(st, p, 10, 1)
+    b = run(st, p, 10, lanes)
+    fl = st["type"] == 1
+    e = rel_l2(b["vel"][fl], a["vel"][fl], floor=1e-3 * np.sqrt(fl.sum()))
+    report(f"lanes {lanes} vs 1, 10 fast steps, vel", e, 1e-5)
+    assert e < 1e-5
+    assert a["rebuilds"] == b["rebuilds"] and a["rebuilds"] >= 2
+    assert a["flags"] == 0 and b["flags"] == 0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_comp", "fp64"])
+def test_lanes_other_precisions(sphlib, oracle, cuda, report, precision):
+    st, p = small()
+    out = run(st, p, 5, 8, precision=precision)
+    ref = oracle.run(oracle.params_like(p), st, 5)
+    e = field_errors(out, ref, st)
+    for k, v in e.items():
+        report(f"lanes 8 {precision}, 5 steps {k}", v, 2e-4)
+    assert out["flags"] == 0
+    assert all(v < 2e-4 for v in e.values()), e
+
+
+def test_lanes_deterministic_across_shapes_and_graphs(sphlib, cuda):
+    from tmp_sph_gb300 import api
+    st, p = small(perturb=True)
+    ref = run(st, p, 6, 8)
+    for opts, graph in (({api.SPH_OPT_BLOCK_THREADS: 64}, True),
+                        ({api.SPH_OPT_BLOCK_THREADS: 256}, True),
+                        ({}, False),
+                        ({api.SPH_OPT_CONDITIONAL_GRAPH: 0}, True)):
+        out = run(st, p, 6, 8, opts=opts, graph=graph)
+        for k in ("pos", "vel", "rho", "p"):
+            assert np.array_equal(out[k], ref[k]), (opts, graph, k)
+
+
+def test_lanes_overflow_walks(sphlib, cuda, report):
+    """With a 16-slot list every fluid particle overflows and its group walks the cells."""
+    from tmp_sph_gb300 import api
+    st, p = small()
+    for skin in (0, 100):
+        a = run(st, p, 3, 8, opts={api.SPH_OPT_SKIN_PERMILLE: skin, api.SPH_OPT_NEIGHBOR_CAP: 16})
+        b = run(st, p, 3, 8, opts={api.SPH_OPT_SKIN_PERMILLE: skin})
+        assert a["flags"] & api.SPH_FLAG_NEIGHBOR_OVERFLOW and b["flags"] == 0
+        fl = st["type"] == 1
+        e = rel_l2(a["vel"][fl], b["vel"][fl], floor=1e-3 * np.sqrt(fl.sum()))
+        report(f"lanes 8 overflow walk vs list, skin {skin}, vel", e, 1e-5)
+        assert e < 1e-5
+
+
+def test_lanes_batch_equals_solo(sphlib, cuda):
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    states, p = cases.batch(2, dx=0.02, seed=9)
+    n = sum(len(st["rho"]) for st in states)
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
+        sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, 8)
+        off = sol.upload_instances(states, stream=s)
+        sol.step(3, stream=s)
+        out = sol.download(stream=s)
+        assert sol.error_flags(stream=s) == 0
+    for b, st in enumerate(states):
+        ref = run(st, p, 3, 8, opts={api.SPH_OPT_SKIN_PERMILLE: 0})
+        sl = slice(int(off[b]), int(off[b + 1]))
+        for k in ("pos", "vel", "rho", "p"):
+            assert np.array_equal(out[k][sl], ref[k]), (b, k)
+
+
+def test_lanes_option_checked(sphlib):
+    from tmp_sph_gb300 import api, cases, solver as S
+    st, p = small()
+    with S.Solver(p, len(st["rho"])) as sol:
+        for bad in (0, 3, 32, -1):
+            with pytest.raises(api.SphError):
+                sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, bad)
+        for good in (1, 2, 4, 8, 16):
+            sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, good)

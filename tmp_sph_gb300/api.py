@@ -44,6 +44,7 @@ SPH_OPT_PRECISION = 8
 SPH_OPT_BLOCK_THREADS = 9
 SPH_OPT_PARTICLES_PER_THREAD = 10
 SPH_OPT_PAIRS = 11
+SPH_OPT_LANES_PER_PARTICLE = 12
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
               "mixed_comp": SPH_PREC_MIXED_COMP}

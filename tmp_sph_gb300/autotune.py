@@ -1,7 +1,8 @@
 """Autotuner for the resident solver's launch shape and cell size.
 
-Picks, for one workload on the GPU at hand, the threads per block and particles per thread of
-the neighbour kernels and the neighbour-list skin (which sets the cell size, kh (1 + skin)).
+Picks, for one workload on the GPU at hand, the threads per block, particles per thread and
+lanes per particle of the neighbour kernels and the neighbour-list skin (which sets the cell
+size, kh (1 + skin)).
 It loads the workload once; for every candidate it forces one list rebuild, runs two profiled
 steps and reads the per-phase device time (SPH_OPT_PROFILE): the cost of a rebuild (sort,
 gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The step
@@ -28,6 +29,7 @@ from . import solver as S
 
 THREADS = (64, 128, 256)
 PPT = (1, 2, 4)
+LANES = (1, 4, 8)
 SKINS = (0, 50, 100, 150, 200, 300)
 
 # profile phases: 0 sort, 1 gather + cell starts, 2 list build, 3 pass 1, 4 pass 2
@@ -53,11 +55,12 @@ def _upload(sol, states, stream):
         sol.upload_instances(states, stream=stream)
 
 
-def measure(sol, stream, threads: int, ppt: int, skin: int) -> dict:
+def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> dict:
     """Rebuild and pass costs (ms) of one candidate on the loaded state, from two profiled
     steps (setting the skin forces the next half step to rebuild; the state advances)."""
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
+    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, lanes)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
     sol.step(1, stream=stream)  # warm: first launches of this shape
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
@@ -71,7 +74,7 @@ def measure(sol, stream, threads: int, ppt: int, skin: int) -> dict:
     t_re = sum(prof[k]["ms"] for k in _REBUILD)
     t_pass = sum(prof[k]["ms"] for k in _PASSES) / 4.0  # per half step
     # with every half step rebuilding (skin 0) the rebuild time covers four rebuilds
-    return {"threads": threads, "ppt": ppt, "skin_permille": skin,
+    return {"threads": threads, "ppt": ppt, "lanes": lanes, "skin_permille": skin,
             "rebuild_ms": t_re / max(1, rebuilds), "pass_ms_per_half_step": t_pass,
             "rebuilds_seen": rebuilds, "flags": sol.error_flags(stream=stream)}
 
@@ -82,10 +85,20 @@ def step_cost(m: dict, p, v: float) -> float:
     return 2.0 * m["pass_ms_per_half_step"] + rate * m["rebuild_ms"]
 
 
+def candidates(threads=THREADS, ppt=PPT, skins=SKINS, lanes=LANES) -> list[tuple]:
+    """(threads, ppt, lanes, skin) to measure: particles per thread only vary with one lane per
+    particle (the lane-group kernels take one particle per group)."""
+    out = []
+    for t, g, s in itertools.product(threads, lanes, skins):
+        for k in (ppt if g == 1 else (1,)):
+            out.append((t, k, g, s))
+    return out
+
+
 def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=SKINS,
-         speed: float | None = None) -> dict:
-    """Best (threads, ppt, skin) for this workload; `states` is one state dict or a list of
-    them (batched instances).  Returns the choice with the measured table."""
+         lanes=LANES, speed: float | None = None) -> dict:
+    """Best (threads, ppt, lanes, skin) for this workload; `states` is one state dict or a list
+    of them (batched instances).  Returns the choice with the measured table."""
     import torch
     states = states if isinstance(states, list) else [states]
     n = sum(len(st["rho"]) for st in states)
@@ -94,13 +107,13 @@ def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=
     table = []
     with S.Solver(p, n, precision=precision) as sol:
         _upload(sol, states, stream)
-        for t, k, s in itertools.product(threads, ppt, skins):
-            m = measure(sol, stream, t, k, s)
+        for t, k, g, s in candidates(threads, ppt, skins, lanes):
+            m = measure(sol, stream, t, k, s, g)
             m["step_ms_estimate"] = step_cost(m, p, v)
             table.append(m)
     ok = [m for m in table if m["flags"] == 0] or table
     best = min(ok, key=lambda m: m["step_ms_estimate"])
-    return {"threads": best["threads"], "ppt": best["ppt"],
+    return {"threads": best["threads"], "ppt": best["ppt"], "lanes": best["lanes"],
             "skin_permille": best["skin_permille"], "speed_m_s": v,
             "step_ms_estimate": best["step_ms_estimate"], "table": table}
 
@@ -109,14 +122,16 @@ def apply(sol, best: dict) -> None:
     """Set a tuned choice on a solver (before its upload)."""
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, best["threads"])
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, best["ppt"])
+    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, best.get("lanes", 1))
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, best["skin_permille"])
 
 
 def summary(best: dict) -> dict:
-    """The choice without the table, plus the estimate of the default (128, 1, 100)."""
+    """The choice without the table, plus the estimate of the default (128 threads, one
+    particle per thread and lane, skin 0.1 kh)."""
     out = {k: v for k, v in best.items() if k != "table"}
     for m in best["table"]:
-        if (m["threads"], m["ppt"], m["skin_permille"]) == (128, 1, 100):
+        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == (128, 1, 1, 100):
             out["default_step_ms_estimate"] = m["step_ms_estimate"]
     return out
 

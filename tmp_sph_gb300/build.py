@@ -26,6 +26,7 @@ SOURCES = [
     "lib/mesh.cu",
     "lib/sort_noalloc.cu",
     "equation/ns.cu",
+    "equation/ns_groups.cu",
     "sph/integrator.cu",
     "sph/solver.cu",
     "sph/params.cpp",
@@ -34,7 +35,7 @@ SOURCES = [
     "io/probes.cu",
     "io/vtk.cpp",
 ]
-HEADERS = ["header/sph_device.cuh", "header/sph_internal.h"]
+HEADERS = ["header/sph_device.cuh", "header/sph_internal.h", "equation/ns_pair.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -1,0 +1,518 @@
+// ns_pair.cuh — pair arithmetic and per-particle accumulators of the two neighbour passes,
+// shared by the one-thread-per-particle kernels (ns.cu) and the lane-group kernels
+// (ns_groups.cu).  Internal to those two translation units: everything is in an unnamed
+// namespace, so each gets its own copy.  The kernel algebra and the record layout are
+// described at the top of ns.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sph_internal.h"
+
+namespace sph {
+
+namespace {
+
+// Block size of the neighbour kernels is a launch parameter (KParams::threads, a multiple of
+// 32 up to NS_MAX_THREADS), as is the number of particles a thread handles (KParams::ppt); both
+// are picked by the autotuner.  ppt > 1 runs the grid-stride instantiation (GS), which holds
+// its loop state in registers (pass 2: 64 instead of 48), so ppt = 1 has its own.
+constexpr int NS_MAX_THREADS = 256;
+// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^26).
+constexpr int CODE_SHIFT = 26;
+constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
+
+// Squared distance with an explicit rounding sequence, so the in-range test gives the same
+// answer in the list build, in the walking passes and in the list passes.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+__device__ __forceinline__ double dist2(double dx, double dy, double dz) {
+    return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+}
+// Pair arithmetic: in FP32 the distance and the reciprocal of a pair come from the hardware's
+// approximate instructions (sqrt.approx, rcp.approx: within about one ulp, one instruction each
+// instead of the correctly rounded sequences); FP64 keeps correctly rounded sqrt and division.
+__device__ __forceinline__ float pair_sqrt(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double pair_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float pair_rcp(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double pair_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float dabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double dabs(double x) { return fabs(x); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// A neighbour sum: plain, or compensated (Neumaier) when COMP.  The compensated form uses
+// explicitly rounded adds so no contraction folds the error terms away.
+template <class T, bool COMP>
+struct Sum {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T v) {
+        if constexpr (COMP) {
+            const T t = add_rn(s, v);
+            c = add_rn(c, dabs(s) >= dabs(v) ? add_rn(sub_rn(s, t), v) : add_rn(sub_rn(v, t), s));
+            s = t;
+        } else {
+            s += v;
+        }
+    }
+    __device__ __forceinline__ T get() const {
+        if constexpr (COMP) return add_rn(s, c);
+        return s;
+    }
+};
+
+// Visit every candidate slot j of the 27 cells around (cx, cy, cz): f(j, code).  Without CODES
+// each x-strip is one range and code is 0; with CODES the strip's three cells are visited one
+// by one and code = (dz+1) << 4 | (dy+1) << 2 | (dx+1) is j's cell relative to (cx, cy, cz).
+// Both visit the same slots in the same order.
+template <bool CODES, class KP, class F>
+__device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
+                                                   int cx, int cy, int cz, F&& f) {
+    const int xl = cx > 0 ? cx - 1 : 0;
+    const int xh = cx < k.gx - 1 ? cx + 1 : k.gx - 1;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = cz + dz;
+        if ((unsigned)z >= (unsigned)k.gz) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = cy + dy;
+            if ((unsigned)y >= (unsigned)k.gy) continue;
+            const int row = (z * k.gy + y) * k.gx;
+            if constexpr (CODES) {
+#pragma unroll 1
+                for (int xc = xl; xc <= xh; xc++) {
+                    const unsigned code =
+                        (unsigned)(((dz + 1) << 4) | ((dy + 1) << 2) | (xc - cx + 1));
+                    const int j0 = max(__ldg(cs + row + xc), 0);
+                    const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
+                    for (int j = j0; j < j1; j++) f(j, code);
+                }
+            } else {
+                const int j0 = max(__ldg(cs + row + xl), 0);
+                const int j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
+#pragma unroll 4
+                for (int j = j0; j < j1; j++) f(j, 0u);
+            }
+        }
+    }
+}
+
+// One record (two vec4) in single 256-bit read-only loads: a neighbour gather touches one L1
+// sector per 32 bytes with one request.  R is 32-byte aligned (cudaMalloc'd).
+__device__ __forceinline__ void ld_rec(const float4* __restrict__ R, int j, float4& a,
+                                       float4& b) {
+    const float4* p = R + 2 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void ld_rec(const dvec4* __restrict__ R, int j, dvec4& a, dvec4& b) {
+    const dvec4* p = R + 2 * (size_t)j;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(a.x), "=d"(a.y), "=d"(a.z), "=d"(a.w)
+        : "l"(p));
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(b.x), "=d"(b.y), "=d"(b.z), "=d"(b.w)
+        : "l"(p + 1));
+}
+__device__ __forceinline__ float4 ld_pos(const float4* __restrict__ X, size_t j) {
+    return __ldg(X + j);
+}
+__device__ __forceinline__ dvec4 ld_pos(const dvec4* __restrict__ X, size_t j) {
+    const dvec4* p = X + j;
+    dvec4 a;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(a.x), "=d"(a.y), "=d"(a.z), "=d"(a.w)
+        : "l"(p));
+    return a;
+}
+
+// Relative position r = x_i - x_j of a pair: from absolute positions, or (mixed precision)
+// from cell-local offsets and j's cell relative to i's.
+template <class P, class V>
+__device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const V& pi,
+                                        const V& pj, unsigned code, typename P::T& dx,
+                                        typename P::T& dy, typename P::T& dz) {
+    using T = typename P::T;
+    if constexpr (P::kMixed) {
+        const int rz = (int)(code >> 4) - 1;
+        const int ry = (int)((code >> 2) & 3u) - 1;
+        const int rx = (int)(code & 3u) - 1;
+        dx = (pi.x - pj.x) - (T)rx * k.cell;
+        dy = (pi.y - pj.y) - (T)ry * k.cell;
+        dz = (pi.z - pj.z) - (T)rz * k.cell;
+    } else {
+        (void)k;
+        (void)code;
+        dx = pi.x - pj.x;
+        dy = pi.y - pj.y;
+        dz = pi.z - pj.z;
+    }
+}
+
+// Walk the cells of particle i over the positions X[STRIDE * j] and call
+// f(j, code, pj, dx, dy, dz, r2) for every j != i with r2 < cut2.  X is the dense
+// (x, y, z, ±1) array (STRIDE 1) or a record array (STRIDE 2).
+template <class P, int STRIDE, class F>
+__device__ __forceinline__ void walk_pairs(const KParamsT<typename P::T>& k,
+                                           const int* __restrict__ cs,
+                                           const unsigned* __restrict__ keys,
+                                           const vec4_t<typename P::T>* __restrict__ X, int i,
+                                           const vec4_t<typename P::T>& pi, typename P::T cut2,
+                                           F&& f) {
+    using T = typename P::T;
+    const unsigned key = keys[i];
+    if (inactive_key(k, key)) return;  // outside the neighbour search (park_inactive)
+    int cx, cy, cz;
+    cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+    for_each_candidate<P::kMixed>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
+        const vec4_t<T> pj = ld_pos(X, (size_t)STRIDE * (size_t)j);
+        T dx, dy, dz;
+        rel_pos<P>(k, pi, pj, code, dx, dy, dz);
+        const T r2 = dist2(dx, dy, dz);
+        if (r2 < cut2 && j != i) f(j, code, pj, dx, dy, dz, r2);
+    });
+}
+
+
+template <class T>
+__device__ __forceinline__ bool fluid_rec(T signed_rho) { return signed_rho > T(0); }
+
+// Position the list build records for the displacement test (offsets in mixed precision).
+__device__ __forceinline__ float4 as_float4(const float4& v) { return v; }
+__device__ __forceinline__ float4 as_float4(const dvec4& v) {
+    return make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+}
+
+// Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
+// particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
+// neighbour record and the particle's own (p', rho', dofv).
+// Pass-1 state of one particle: its own record and the three neighbour sums.
+template <class P>
+struct Pass1Acc {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    V pi, vi;  // x, y, z, p / vx, vy, vz, ±rho
+    bool fi;
+    Sum<T, P::kComp> dofv, rs, ws;
+
+    __device__ __forceinline__ void load(const V* __restrict__ R, int i) {
+        pi = R[2 * (size_t)i];
+        vi = R[2 * (size_t)i + 1];
+        fi = fluid_rec(vi.w);
+    }
+    // One neighbour inside the support radius.
+    __device__ __forceinline__ void pair(const KParamsT<T>& k, const V& aj, const V& vj, T dx,
+                                         T dy, T dz, T r2) {
+        if (!fluid_rec(vj.w)) return;
+        const T rr = pair_sqrt(r2);
+        const T q = rr * k.inv_h;
+        const T t = T(1) - T(0.5) * q;
+        const T t2 = t * t;
+        if (!fi) {
+            const T w = k.adh * t2 * t2 * (T(2) * q + T(1));
+            rs.add((aj.w + vj.w * k.g * dz) * w);
+            ws.add(w);
+        } else {
+            const T fr = k.c_fr * t2 * t;
+            const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            dofv.add(-(fr * vdotr * (k.mass * pair_rcp(vj.w))));
+        }
+    }
+    template <bool WRITE_SUMS>
+    __device__ __forceinline__ void finish(const KParamsT<T>& k, const Pass1OutT<T>& out,
+                                           float* __restrict__ rhop_sum,
+                                           float* __restrict__ w_sum, int i) {
+        T p, rho;
+        const T dv = dofv.get(), rsum = rs.get(), wsum = ws.get();
+        if (fi) {
+            p = pi.w;
+            rho = vi.w;
+        } else {
+            p = dabs(wsum) > T(1.0e-8) ? rsum / wsum : T(0);
+            if (p < T(0)) p = T(0);
+            rho = eos_density(k, p);
+        }
+        const T qv = fi ? p - k.damper * dv : p;
+        out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
+        out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
+        out.self[i] = make4<T>(p, rho, dv, T(0));
+        if constexpr (WRITE_SUMS) {
+            rhop_sum[i] = (float)rsum;
+            w_sum[i] = (float)wsum;
+        }
+    }
+};
+
+
+enum { MODE_RATES = 0, MODE_PRED = 1, MODE_CORR = 2 };
+
+// Pass 2: continuity + delta density diffusion, momentum (pressure, acoustic damper,
+// artificial viscosity, gravity); then either the rates are stored (MODE_RATES) or the
+// midpoint predictor / corrector of src/sph/sph_run.cu:425-519 is applied and the updated
+// particle written to `out` with its next cell hash.
+//
+// `out` may alias `in`: the update touches only particle i's own rows, and neighbours (also
+// the positions of a cell walk) come from the pass-1 records.  Returns the squared distance
+// of particle i from its position when the neighbour list was built (0 without a list).
+// Pass-2 state of one particle: its pass-1 record, own side and the four neighbour sums.
+template <class P, int MODE>
+struct Pass2Acc {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    V pi, vi;  // x, y, z, q / vx, vy, vz, ±rho
+    T rhoi, presi, damp_i;
+    bool fi, active;
+    Sum<T, P::kComp> sd, sx, sy, sz;
+
+    __device__ __forceinline__ void load(const KParamsT<T>& k, const Pass1OutT<T>& p1, int i,
+                                         int wall_rates) {
+        pi = p1.nrec[2 * (size_t)i];
+        vi = p1.nrec[2 * (size_t)i + 1];
+        const V si = p1.self[i];  // p_i, rho_i, dofv_i
+        fi = fluid_rec(vi.w);
+        rhoi = si.y;
+        presi = si.x;
+        damp_i = k.damper * si.z;
+        active = fi || (MODE == MODE_RATES && wall_rates);
+    }
+    // One neighbour inside the support radius.  aj = (x, y, z, q), vj = (vx, vy, vz, ±rho).
+    // rho_i - rho_j stays an exact difference of two close floats; writing the
+    // density-diffusion term with the volume m / rho_j instead (rho_i V_j - m) cancels and lost
+    // three digits of rho_dt.
+    __device__ __forceinline__ void pair(const KParamsT<T>& k, const Pass1OutT<T>& p1, int j,
+                                         const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
+        const bool fj = fluid_rec(vj.w);
+        const T rhoj = dabs(vj.w);
+        const T rr = pair_sqrt(r2);
+        const T q = rr * k.inv_h;
+        const T t = T(1) - T(0.5) * q;
+        const T fr = k.c_fr * t * t * t;
+        const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+        const T volj = k.mass * pair_rcp(rhoj);
+        const T inv_r2e = pair_rcp(r2 + k.eta2);
+        sd.add(volj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
+        T S;
+        if (fi) {
+            S = -presi - aj.w;
+            if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
+        } else {
+            S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
+        }
+        const T c = fr * S * volj;
+        sx.add(c * dx);
+        sy.add(c * dy);
+        sz.add(c * dz);
+    }
+};
+
+
+// Rates, or the predictor / corrector update and the next key of particle i; returns its
+// squared distance from its list-build position (0 without a list).
+template <class P, int MODE>
+__device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, int i,
+                                              const Pass2Acc<P, MODE>& acc,
+                                              const ParticleSetT<typename P::T>& in,
+                                              const unsigned* __restrict__ keys,
+                                              const NbrList& nl, float* __restrict__ rho_dt,
+                                              float* __restrict__ vel_dt, int wall_rates,
+                                              const ParticleSetT<typename P::T>& out,
+                                              unsigned* __restrict__ out_hash, unsigned* err) {
+    using T = typename P::T;
+    using V = vec4_t<T>;
+    const V& pi = acc.pi;
+    const V& vi = acc.vi;
+    const bool fi = acc.fi;
+    const T rhoi = acc.rhoi, presi = acc.presi;
+    T drho = T(0), ax = T(0), ay = T(0), az = T(0);
+    if (acc.active) {
+        drho = acc.sd.get();
+        const T inv_rhoi = T(1) / rhoi;
+        ax = acc.sx.get() * inv_rhoi;
+        ay = acc.sy.get() * inv_rhoi;
+        az = acc.sz.get() * inv_rhoi;
+    }
+    az += k.g;
+
+    if constexpr (MODE == MODE_RATES) {
+        const bool have = fi || wall_rates;
+        rho_dt[i] = have ? (float)drho : 0.f;
+        vel_dt[3 * i] = have ? (float)ax : 0.f;
+        vel_dt[3 * i + 1] = have ? (float)ay : 0.f;
+        vel_dt[3 * i + 2] = have ? (float)az : 0.f;
+        return 0.f;
+    } else if constexpr (P::kMixed) {
+        // FP64 position and density perturbation; FP32 velocity
+        const dvec4 xm = in.xm[i];
+        dvec4 nxm = xm, txm = xm;
+        float4 nv, tv;
+        float npres, nrho;
+        const double hdt = (double)k.half_dt;
+        if (fi) {
+            if (escaped(k, xm.x, xm.y, xm.z)) {
+                nxm = dvec4{(double)k.park_x, (double)k.park_y, (double)k.park_z, 0.0};
+                nv = make_float4(0.f, 0.f, 0.f, 0.f);
+                txm = nxm;
+                tv = nv;
+            } else if (MODE == MODE_PRED) {
+                tv = make_float4(vi.x, vi.y, vi.z, 0.f);
+                double d = xm.w + (double)drho * hdt;
+                if (k.clamp_density && d < 0.0) d = 0.0;
+                nxm.x = xm.x + (double)vi.x * hdt;
+                nxm.y = xm.y + (double)vi.y * hdt;
+                nxm.z = xm.z + (double)vi.z * hdt;
+                nxm.w = d;
+                nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
+                                 0.f);
+            } else {
+                txm = in.txm[i];
+                tv = in.tvel[i];
+                double ds = txm.w + (double)drho * hdt;
+                if (k.clamp_density && ds < 0.0) ds = 0.0;
+                double d = 2.0 * ds - txm.w;
+                if (k.clamp_density && d < 0.0) d = 0.0;
+                nxm.x = 2.0 * (txm.x + (double)vi.x * hdt) - txm.x;
+                nxm.y = 2.0 * (txm.y + (double)vi.y * hdt) - txm.y;
+                nxm.z = 2.0 * (txm.z + (double)vi.z * hdt) - txm.z;
+                nxm.w = d;
+                const float uxs = tv.x + ax * k.half_dt;
+                const float uys = tv.y + ay * k.half_dt;
+                const float uzs = tv.z + az * k.half_dt;
+                nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, 0.f);
+            }
+            nrho = k.rho0 + (float)nxm.w;
+            npres = eos_pressure_d(k, (float)nxm.w);
+        } else {
+            // boundary particles do not move; they keep the extrapolated pressure and density
+            nv = make_float4(vi.x, vi.y, vi.z, 0.f);
+            npres = presi;
+            nrho = rhoi;
+            tv = nv;
+        }
+        double ox, oy, oz;
+        cell_origin(k, keys[i], ox, oy, oz);
+        const float px = (float)(nxm.x - ox), py = (float)(nxm.y - oy), pz = (float)(nxm.z - oz);
+        out.rec[2 * (size_t)i] = make_float4(px, py, pz, npres);
+        out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+        if (out.xyz) out.xyz[i] = make_float4(px, py, pz, fi ? 1.f : -1.f);
+        out.type[i] = in.type[i];
+        out.id[i] = in.id[i];
+        out.xm[i] = nxm;
+        if (MODE == MODE_PRED) {
+            out.txm[i] = txm;
+            out.tvel[i] = tv;
+        }
+        // instance ids only move with the particles when instances are batched
+        const int inst = k.inst_cells ? in.inst[i] : 0;
+        if (k.inst_cells) out.inst[i] = inst;
+        unsigned f = 0;
+        const unsigned nk = slot_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f);
+        out_hash[i] = nk;
+        raise_flags(err, f);
+        if (k.park_inactive) {
+            // a particle that leaves (or rejoins) the neighbour search needs new lists; one
+            // outside it is in no list, so its moves do not count
+            const bool now = inactive_key(k, nk);
+            if (now != inactive_key(k, keys[i])) return 3.0e38f;
+            if (now) return 0.f;
+        }
+        if (!fi || !nl.xb) return 0.f;
+        const float4 xb = nl.xb[i];
+        return dist2(px - xb.x, py - xb.y, pz - xb.z);
+    } else {
+        V np = pi, nv;
+        T npres, nrho;
+        V tp, tv;
+        if (fi) {
+            if (escaped(k, pi.x, pi.y, pi.z)) {
+                np = make4<T>(k.park_x, k.park_y, k.park_z, T(0));
+                nv = make4<T>(T(0), T(0), T(0), T(0));
+                npres = T(0);
+                nrho = k.rho0;
+                tp = make4<T>(np.x, np.y, np.z, k.rho0);
+                tv = make4<T>(T(0), T(0), T(0), T(0));
+            } else if (MODE == MODE_PRED) {
+                tp = make4<T>(pi.x, pi.y, pi.z, rhoi);
+                tv = make4<T>(vi.x, vi.y, vi.z, T(0));
+                T rho = rhoi + drho * k.half_dt;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                np.x = pi.x + vi.x * k.half_dt;
+                np.y = pi.y + vi.y * k.half_dt;
+                np.z = pi.z + vi.z * k.half_dt;
+                nv = make4<T>(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
+                              T(0));
+                nrho = rho;
+                npres = eos_pressure(k, rho);
+            } else {
+                tp = in.tpos[i];
+                tv = in.tvel[i];
+                T rho = tp.w + drho * k.half_dt;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                const T xs = tp.x + vi.x * k.half_dt;
+                const T ys = tp.y + vi.y * k.half_dt;
+                const T zs = tp.z + vi.z * k.half_dt;
+                const T uxs = tv.x + ax * k.half_dt;
+                const T uys = tv.y + ay * k.half_dt;
+                const T uzs = tv.z + az * k.half_dt;
+                rho = T(2) * rho - tp.w;
+                if (k.clamp_density && rho < k.rho0) rho = k.rho0;
+                np.x = T(2) * xs - tp.x;
+                np.y = T(2) * ys - tp.y;
+                np.z = T(2) * zs - tp.z;
+                nv = make4<T>(T(2) * uxs - tv.x, T(2) * uys - tv.y, T(2) * uzs - tv.z, T(0));
+                nrho = rho;
+                npres = eos_pressure(k, rho);
+            }
+        } else {
+            // boundary particles do not move; they keep the extrapolated pressure and density
+            nv = make4<T>(vi.x, vi.y, vi.z, T(0));
+            npres = presi;
+            nrho = rhoi;
+            tp = make4<T>(pi.x, pi.y, pi.z, rhoi);
+            tv = make4<T>(vi.x, vi.y, vi.z, T(0));
+        }
+        out.rec[2 * (size_t)i] = make4<T>(np.x, np.y, np.z, npres);
+        out.rec[2 * (size_t)i + 1] = make4<T>(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
+        if (out.xyz) out.xyz[i] = make4<T>(np.x, np.y, np.z, fi ? T(1) : T(-1));
+        out.type[i] = in.type[i];
+        out.id[i] = in.id[i];
+        if (MODE == MODE_PRED) {
+            out.tpos[i] = tp;
+            out.tvel[i] = tv;
+        }
+        // instance ids only move with the particles when instances are batched
+        const int inst = k.inst_cells ? in.inst[i] : 0;
+        if (k.inst_cells) out.inst[i] = inst;
+        unsigned f = 0;
+        const unsigned nk = slot_key(k, inst, fi, np.x, np.y, np.z, &f);
+        out_hash[i] = nk;
+        raise_flags(err, f);
+        if (k.park_inactive) {
+            // a particle that leaves (or rejoins) the neighbour search needs new lists; one
+            // outside it is in no list, so its moves do not count
+            const bool now = inactive_key(k, nk);
+            if (now != inactive_key(k, keys[i])) return 3.0e38f;
+            if (now) return 0.f;
+        }
+        if (!fi || !nl.xb) return 0.f;
+        const float4 xb = nl.xb[i];
+        return (float)dist2(np.x - (T)xb.x, np.y - (T)xb.y, np.z - (T)xb.z);
+    }
+}
+
+
+}  // namespace
+
+}  // namespace sph

@@ -51,6 +51,7 @@ struct KParamsT {
     int threads;
     int ppt;
     int pairs;  // two consecutive particles per thread over the union of their lists
+    int lanes;  // lanes per particle in the list kernels (1, or 2 .. 16: ns_groups.cu)
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
     T h, inv_h, kh, kh2;

@@ -176,6 +176,27 @@ cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float*
                                   const int* type, const int* inst_off, int n_inst,
                                   ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
                                   cudaStream_t s);
+// Lane-group variants of the list kernels (equation/ns_groups.cu): k.lanes in {2, 4, 8, 16}
+// lanes per particle over a list in the group layout; launch_nbr_build / launch_pass1 /
+// launch_pass2_step dispatch to them when k.lanes > 1.
+template <class P>
+cudaError_t launch_nbr_build_groups(const KParamsT<typename P::T>& k,
+                                    const ParticleSetT<typename P::T>& in, const unsigned* keys,
+                                    const int* cs, const NbrList& nl, int walls_all,
+                                    unsigned* err, cudaStream_t s, const unsigned* gate);
+template <class P>
+cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
+                                const ParticleSetT<typename P::T>& in, const unsigned* keys,
+                                const int* cs, const NbrList& nl,
+                                const Pass1OutT<typename P::T>& out, cudaStream_t s);
+template <class P>
+cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
+                                const ParticleSetT<typename P::T>& in, const unsigned* keys,
+                                const int* cs, const NbrList& nl,
+                                const Pass1OutT<typename P::T>& p1,
+                                ParticleSetT<typename P::T> out, unsigned* out_hash,
+                                unsigned* err, unsigned* disp, cudaStream_t s);
+
 // Upload original-order arrays into the current sorted order (slot k takes particle id[k]),
 // measuring displacements from the list-build positions xb into *disp; a changed particle
 // kind sets *force.
@@ -274,6 +295,7 @@ struct sph_ctx {
     int opt_threads = 128;   // neighbour kernels: threads per block
     int opt_ppt = 1;         // neighbour kernels: particles per thread
     int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
+    int opt_lanes = 1;       // neighbour-list kernels: lanes per particle
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

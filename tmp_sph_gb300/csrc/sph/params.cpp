@@ -37,6 +37,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.threads = 128;
     k.ppt = 1;
     k.pairs = 0;
+    k.lanes = 1;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
@@ -97,6 +98,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.threads = 128;
     k.ppt = 1;
     k.pairs = 0;
+    k.lanes = 1;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];

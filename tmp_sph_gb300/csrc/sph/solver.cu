@@ -245,6 +245,8 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.threads = c->opt_threads;
     k.ppt = c->opt_ppt;
     k.pairs = c->opt_pairs;
+    // lane groups need the list (and are not combined with pair mode)
+    k.lanes = (c->opt_nbr_list && c->nl.idx && !c->opt_pairs) ? c->opt_lanes : 1;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
@@ -555,6 +557,13 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             c->opt_ppt = value;
             drop_graph(c);
             return SPH_OK;
+        case SPH_OPT_LANES_PER_PARTICLE:
+            if (value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
+                return SPH_ERR_ARG;
+            if (value == c->opt_lanes) return SPH_OK;
+            c->opt_lanes = value;
+            drop_graph(c);
+            break;  // the list layout changed: rebuild
         case SPH_OPT_PAIRS:
             c->opt_pairs = value != 0;
             drop_graph(c);

@@ -406,3 +406,33 @@ def test_pair_mode_matches_oracle(sphlib, oracle, cuda, report):
     for k, v in e.items():
         report(f"pairs 20 steps vs oracle {k}", v, 2e-4)
     assert all(v < 2e-4 for v in e.values()), e
+
+
+def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):
+    """The lists are rebuilt when the box of all displacements since the last build has a
+    half-diagonal beyond skin/2: a block carried at 1 m/s past static walls keeps them for
+    about skin/v (twice as long as a test on the largest displacement would), the results match
+    the oracle, and with every list overflowed (cell walks from the cells of the last build)
+    they are the same bits."""
+    from tmp_sph_gb300 import api, cases
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    fl = st["type"] == 1
+    st["vel"][fl] = np.array([1.0, 0.0, 0.0], np.float32)
+    steps = 60
+    out, flags = run_opts(st, p, steps, {api.SPH_OPT_SKIN_PERMILLE: 100})
+    skin = 0.1 * float(p.kh)
+    per_build = skin / (1.0 * float(p.dt))  # steps a uniform 1 m/s carry takes to reach skin
+    report("uniform carry: list rebuilds in 60 steps", out["rebuilds"], 1 + steps / per_build)
+    assert flags == 0
+    assert out["rebuilds"] <= 2 + steps / per_build
+    ref = oracle.run(oracle.params_like(p), st, steps)
+    e = field_errors(out, ref, st)
+    for k, v in e.items():
+        report(f"uniform carry 60 steps {k}", v, 2e-4)
+    assert all(v < 2e-4 for v in e.values()), e
+    walk, wflags = run_opts(st, p, steps, {api.SPH_OPT_SKIN_PERMILLE: 100,
+                                           api.SPH_OPT_NEIGHBOR_CAP: 8})
+    assert wflags & api.SPH_FLAG_NEIGHBOR_OVERFLOW
+    assert walk["rebuilds"] == out["rebuilds"]
+    for k in ("pos", "vel", "rho", "p"):
+        assert np.array_equal(walk[k], out[k]), k

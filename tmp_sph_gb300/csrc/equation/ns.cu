@@ -225,14 +225,15 @@ k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     }
 }
 template <class P, int MODE, bool LIST>
-__device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int i,
-                                           const ParticleSetT<typename P::T>& in,
-                                           const unsigned* __restrict__ keys,
-                                           const int* __restrict__ cs, const NbrList& nl,
-                                           const Pass1OutT<typename P::T>& p1,
-                                           float* __restrict__ rho_dt, float* __restrict__ vel_dt,
-                                           int wall_rates, const ParticleSetT<typename P::T>& out,
-                                           unsigned* __restrict__ out_hash, unsigned* err) {
+__device__ __forceinline__ void pass2_one(const KParamsT<typename P::T>& k, int i,
+                                          const ParticleSetT<typename P::T>& in,
+                                          const unsigned* __restrict__ keys,
+                                          const int* __restrict__ cs, const NbrList& nl,
+                                          const Pass1OutT<typename P::T>& p1,
+                                          float* __restrict__ rho_dt, float* __restrict__ vel_dt,
+                                          int wall_rates, const ParticleSetT<typename P::T>& out,
+                                          unsigned* __restrict__ out_hash, unsigned* err,
+                                          DispBox& box) {
     using T = typename P::T;
     using V = vec4_t<T>;
     Pass2Acc<P, MODE> acc;
@@ -242,8 +243,8 @@ __device__ __forceinline__ float pass2_one(const KParamsT<typename P::T>& k, int
                                   [&](int j, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
             acc.pair(k, p1, j, aj, vj, dx, dy, dz, r2);
         });
-    return pass2_finish<P, MODE>(k, i, acc, in, keys, nl, rho_dt, vel_dt, wall_rates, out,
-                                 out_hash, err);
+    pass2_finish<P, MODE>(k, i, acc, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
+                          err, box);
 }
 
 
@@ -254,28 +255,20 @@ k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
         int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
         unsigned* err, unsigned* disp) {
-    float d2 = 0.f;
+    DispBox box;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
-            d2 = fmaxf(d2, pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt,
-                                                    wall_rates, out, out_hash, err));
+            pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                     out_hash, err, box);
     } else if (i0 < k.n) {
-        d2 = pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
-                                      out, out_hash, err);
+        pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                 out_hash, err, box);
     }
     if (MODE == MODE_RATES || disp == nullptr) return;
-    // block maximum of the squared displacement, one atomic per block (non-negative floats
-    // order like their bit patterns); blockDim is a multiple of 32, every thread gets here
-    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
-    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned m = s_max[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
-        if (m) atomicMax(disp, m);
-    }
+    // the block's displacement box; blockDim is a multiple of 32, every thread gets here
+    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
+    reduce_disp_box(box, disp, s_box);
 }
 
 // The same kernel held to CAP registers (one particle per thread): the FP32 step kernel fits
@@ -288,28 +281,20 @@ k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt, float* __restrict__ vel_dt,
         int wall_rates, ParticleSetT<typename P::T> out, unsigned* __restrict__ out_hash,
         unsigned* err, unsigned* disp) {
-    float d2 = 0.f;
+    DispBox box;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
-            d2 = fmaxf(d2, pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt,
-                                                    wall_rates, out, out_hash, err));
+            pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                     out_hash, err, box);
     } else if (i0 < k.n) {
-        d2 = pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates,
-                                      out, out_hash, err);
+        pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
+                                 out_hash, err, box);
     }
     if (MODE == MODE_RATES || disp == nullptr) return;
-    // block maximum of the squared displacement, one atomic per block (non-negative floats
-    // order like their bit patterns); blockDim is a multiple of 32, every thread gets here
-    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
-    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned m = s_max[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
-        if (m) atomicMax(disp, m);
-    }
+    // the block's displacement box; blockDim is a multiple of 32, every thread gets here
+    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
+    reduce_disp_box(box, disp, s_box);
 }
 
 // ---------------------------------------------------------------- particle pairs
@@ -457,15 +442,16 @@ __device__ __forceinline__ void pass1_pair(const KParamsT<typename P::T>& k,
 }
 
 template <class P, int MODE>
-__device__ __forceinline__ float pass2_pair(const KParamsT<typename P::T>& k, int c,
-                                            const ParticleSetT<typename P::T>& in,
-                                            const unsigned* __restrict__ keys,
-                                            const int* __restrict__ cs, const NbrList& nl,
-                                            const Pass1OutT<typename P::T>& p1,
-                                            float* __restrict__ rho_dt,
-                                            float* __restrict__ vel_dt, int wall_rates,
-                                            const ParticleSetT<typename P::T>& out,
-                                            unsigned* __restrict__ out_hash, unsigned* err) {
+__device__ __forceinline__ void pass2_pair(const KParamsT<typename P::T>& k, int c,
+                                           const ParticleSetT<typename P::T>& in,
+                                           const unsigned* __restrict__ keys,
+                                           const int* __restrict__ cs, const NbrList& nl,
+                                           const Pass1OutT<typename P::T>& p1,
+                                           float* __restrict__ rho_dt,
+                                           float* __restrict__ vel_dt, int wall_rates,
+                                           const ParticleSetT<typename P::T>& out,
+                                           unsigned* __restrict__ out_hash, unsigned* err,
+                                           DispBox& box) {
     using T = typename P::T;
     using V = vec4_t<T>;
     const int i0 = 2 * c, i1 = 2 * c + 1;
@@ -497,12 +483,11 @@ __device__ __forceinline__ float pass2_pair(const KParamsT<typename P::T>& k, in
                                                T r2) { a1.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
         }
     }
-    float d2 = pass2_finish<P, MODE>(k, i0, a0, in, keys, nl, rho_dt, vel_dt, wall_rates, out,
-                                     out_hash, err);
+    pass2_finish<P, MODE>(k, i0, a0, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
+                          err, box);
     if (has1)
-        d2 = fmaxf(d2, pass2_finish<P, MODE>(k, i1, a1, in, keys, nl, rho_dt, vel_dt, wall_rates,
-                                             out, out_hash, err));
-    return d2;
+        pass2_finish<P, MODE>(k, i1, a1, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
+                              err, box);
 }
 
 template <class P>
@@ -536,20 +521,13 @@ k_pass2_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
               float* __restrict__ vel_dt, int wall_rates, ParticleSetT<typename P::T> out,
               unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    float d2 = 0.f;
+    DispBox box;
     if (c < (k.n + 1) / 2)
-        d2 = pass2_pair<P, MODE>(k, c, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                 out_hash, err);
+        pass2_pair<P, MODE>(k, c, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash,
+                            err, box);
     if (MODE == MODE_RATES || disp == nullptr) return;
-    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
-    const unsigned wmax = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned m = s_max[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
-        if (m) atomicMax(disp, m);
-    }
+    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
+    reduce_disp_box(box, disp, s_box);
 }
 
 // Pair mode applies to the FP32 and FP64 policies (mixed-precision slots carry each

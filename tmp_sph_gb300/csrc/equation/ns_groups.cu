@@ -301,7 +301,7 @@ k_pass2_g(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     using T = typename P::T;
     using V = vec4_t<T>;
     __shared__ T s_sum[4][NS_MAX_THREADS];
-    __shared__ unsigned s_max[NS_MAX_THREADS / 32];
+    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
     const int nt = (int)blockDim.x, base = (int)blockIdx.x * nt, s = sub_lane<G>();
 #pragma unroll 1
     for (int r = 0; r < G; r++) {
@@ -328,7 +328,7 @@ k_pass2_g(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     }
     __syncthreads();
     const int i = base + (int)threadIdx.x;
-    float d2 = 0.f;
+    DispBox box;
     if (i < k.n) {
         Pass2Acc<P, MODE> acc;
         acc.load(k, p1, i, 0);
@@ -336,19 +336,11 @@ k_pass2_g(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         acc.sx = sum_of<T, P::kComp>(s_sum[1][threadIdx.x]);
         acc.sy = sum_of<T, P::kComp>(s_sum[2][threadIdx.x]);
         acc.sz = sum_of<T, P::kComp>(s_sum[3][threadIdx.x]);
-        d2 = pass2_finish<P, MODE>(k, i, acc, in, keys, nl, nullptr, nullptr, 0, out, out_hash,
-                                   err);
+        pass2_finish<P, MODE>(k, i, acc, in, keys, nl, nullptr, nullptr, 0, out, out_hash, err,
+                              box);
     }
-    // block maximum of the squared displacement, one atomic per block (non-negative floats
-    // order like their bit patterns); blockDim is a multiple of 32, every thread gets here
-    const unsigned wmax = __reduce_max_sync(FULL_MASK, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = wmax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned m = s_max[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = max(m, s_max[w]);
-        if (m) atomicMax(disp, m);
-    }
+    // the block's displacement box; blockDim is a multiple of 32, every thread gets here
+    reduce_disp_box(box, disp, s_box);
 }
 
 inline int group_blocks(int n, int threads) { return (n + threads - 1) / threads; }

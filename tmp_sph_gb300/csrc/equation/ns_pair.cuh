@@ -319,17 +319,19 @@ struct Pass2Acc {
 };
 
 
-// Rates, or the predictor / corrector update and the next key of particle i; returns its
-// squared distance from its list-build position (0 without a list).
+// Rates, or the predictor / corrector update and the next key of particle i; adds its
+// displacement from its list-build position to `box` (nothing without a list or for a particle
+// outside the search; a huge one when it leaves or rejoins the search).
 template <class P, int MODE>
-__device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, int i,
+__device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, int i,
                                               const Pass2Acc<P, MODE>& acc,
                                               const ParticleSetT<typename P::T>& in,
                                               const unsigned* __restrict__ keys,
                                               const NbrList& nl, float* __restrict__ rho_dt,
                                               float* __restrict__ vel_dt, int wall_rates,
                                               const ParticleSetT<typename P::T>& out,
-                                              unsigned* __restrict__ out_hash, unsigned* err) {
+                                              unsigned* __restrict__ out_hash, unsigned* err,
+                                              DispBox& box) {
     using T = typename P::T;
     using V = vec4_t<T>;
     const V& pi = acc.pi;
@@ -352,7 +354,7 @@ __device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, 
         vel_dt[3 * i] = have ? (float)ax : 0.f;
         vel_dt[3 * i + 1] = have ? (float)ay : 0.f;
         vel_dt[3 * i + 2] = have ? (float)az : 0.f;
-        return 0.f;
+        return;
     } else if constexpr (P::kMixed) {
         // FP64 position and density perturbation; FP32 velocity
         const dvec4 xm = in.xm[i];
@@ -425,12 +427,16 @@ __device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, 
             // a particle that leaves (or rejoins) the neighbour search needs new lists; one
             // outside it is in no list, so its moves do not count
             const bool now = inactive_key(k, nk);
-            if (now != inactive_key(k, keys[i])) return 3.0e38f;
-            if (now) return 0.f;
+            if (now != inactive_key(k, keys[i])) {
+                box.add(3.0e38f, 3.0e38f, 3.0e38f);
+                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+                return;
+            }
+            if (now) return;
         }
-        if (!fi || !nl.xb) return 0.f;
+        if (!nl.xb) return;
         const float4 xb = nl.xb[i];
-        return dist2(px - xb.x, py - xb.y, pz - xb.z);
+        box.add(px - xb.x, py - xb.y, pz - xb.z);
     } else {
         V np = pi, nv;
         T npres, nrho;
@@ -503,12 +509,16 @@ __device__ __forceinline__ float pass2_finish(const KParamsT<typename P::T>& k, 
             // a particle that leaves (or rejoins) the neighbour search needs new lists; one
             // outside it is in no list, so its moves do not count
             const bool now = inactive_key(k, nk);
-            if (now != inactive_key(k, keys[i])) return 3.0e38f;
-            if (now) return 0.f;
+            if (now != inactive_key(k, keys[i])) {
+                box.add(3.0e38f, 3.0e38f, 3.0e38f);
+                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+                return;
+            }
+            if (now) return;
         }
-        if (!fi || !nl.xb) return 0.f;
+        if (!nl.xb) return;
         const float4 xb = nl.xb[i];
-        return (float)dist2(np.x - (T)xb.x, np.y - (T)xb.y, np.z - (T)xb.z);
+        box.add((float)(np.x - (T)xb.x), (float)(np.y - (T)xb.y), (float)(np.z - (T)xb.z));
     }
 }
 

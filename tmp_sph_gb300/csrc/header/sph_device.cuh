@@ -221,4 +221,74 @@ __device__ __forceinline__ void raise_flags(unsigned* err, unsigned f) {
     if (f && err) atomicOr(err, f);
 }
 
+// ---------------------------------------------------------------- list rebuild test
+// The neighbour lists hold every pair closer than kh + s at the last build (s = skin kh).  A
+// pair missing from them can only come within kh once the two particles' displacements since
+// the build differ by more than s, and |d_i - d_j| <= |d_i - D| + |d_j - D| for any vector D.
+// Taking D as the centre of the bounding box of all displacements, the lists stay complete
+// while that box's half-diagonal is below s/2: a flow that carries many particles the same
+// way (a surge) keeps its lists roughly twice as long as with the largest displacement
+// itself.  The cell walk of a particle whose list overflowed uses the cells of the last build,
+// which the same bound keeps within reach.
+//
+// The box is kept as order-preserving integer keys of its low and high corners in
+// DISP_WORDS words of the rebuild block, each in its own 128-byte line so the atomics of
+// different corners do not queue on one L2 slice.
+constexpr int DISP_STRIDE = 32;  // words between corner words
+constexpr int DISP_WORDS = 6 * DISP_STRIDE;
+
+__device__ __forceinline__ unsigned ord_key(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord_value(unsigned key) {
+    return __uint_as_float((key & 0x80000000u) ? (key & 0x7fffffffu) : ~key);
+}
+
+// A thread's box of displacements (empty until the first add).
+struct DispBox {
+    unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
+    unsigned hi[3] = {0u, 0u, 0u};
+    // a displacement that is not a number counts as a huge one (the lists are rebuilt)
+    __device__ __forceinline__ void add(float x, float y, float z) {
+        const float v[3] = {x == x ? x : 3.0e38f, y == y ? y : 3.0e38f, z == z ? z : 3.0e38f};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const unsigned kc = ord_key(v[c]);
+            lo[c] = min(lo[c], kc);
+            hi[c] = max(hi[c], kc);
+        }
+    }
+};
+
+// Fold the boxes of a block into the rebuild words (lo x, y, z, hi x, y, z, DISP_STRIDE apart).
+// Every thread of the block must call it (it synchronises); s_box holds 6 * (blockDim / 32)
+// words.  A corner is only written when the block improves on the value already there.
+__device__ __forceinline__ void reduce_disp_box(const DispBox& b, unsigned* disp,
+                                                unsigned* s_box) {
+    const int warps = (int)(blockDim.x >> 5), w = (int)(threadIdx.x >> 5);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const unsigned l = __reduce_min_sync(0xffffffffu, b.lo[c]);
+        const unsigned h = __reduce_max_sync(0xffffffffu, b.hi[c]);
+        if ((threadIdx.x & 31) == 0) {
+            s_box[c * warps + w] = l;
+            s_box[(3 + c) * warps + w] = h;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6 && disp) {
+        const int c = (int)threadIdx.x;
+        unsigned v = s_box[c * warps];
+        for (int q = 1; q < warps; q++)
+            v = c < 3 ? min(v, s_box[c * warps + q]) : max(v, s_box[c * warps + q]);
+        unsigned* word = disp + c * DISP_STRIDE;
+        if (c < 3) {
+            if (v < *(volatile unsigned*)word) atomicMin(word, v);
+        } else {
+            if (v > *(volatile unsigned*)word) atomicMax(word, v);
+        }
+    }
+}
+
 }  // namespace sph

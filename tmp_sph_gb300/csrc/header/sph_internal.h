@@ -230,6 +230,11 @@ cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float*
 cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* self,
                                 float* s_rho, float* s_p, float* dofv, cudaStream_t s);
 
+// Layout of the rebuild block: four control words, then the displacement box (DISP_WORDS,
+// 128-byte aligned).
+constexpr int RB_DISP = 32;
+constexpr int RB_WORDS = RB_DISP + DISP_WORDS;
+
 // Per-phase device timing of sph_step (SPH_OPT_PROFILE).
 enum Phase { PH_SORT = 0, PH_GATHER, PH_NBR, PH_PASS1, PH_PASS2, PH_COUNT };
 
@@ -282,8 +287,9 @@ struct sph_ctx {
     int gz_inst = 0;                 // grid height of one instance
     int* inst_off = nullptr;         // [SPH_MAX_INSTANCES + 1] instance particle offsets
     double skin = 0.1;               // list skin as a fraction of the support radius kh
-    unsigned* rb = nullptr;          // [0] rebuild gate, [1] max squared displacement (float
-                                     // bits), [2] forced rebuild, [3] rebuild count
+    unsigned* rb = nullptr;          // [0] rebuild gate, [1] last half-diagonal^2 of the
+                                     // displacement box (float bits), [2] forced rebuild,
+                                     // [3] rebuild count, [RB_DISP ..] the displacement box
 
     // graph replay of one full step
     int opt_use_graph = 1;

@@ -473,9 +473,10 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
 
 // Upload into the current cell order.  Slot k of the sorted live set takes particle id[k] of
 // the original-order arrays, so the cell starts and neighbour lists built for that order stay
-// in use.  Every slot measures its squared displacement from the position its list was built
-// at (xb) into *disp (the half step's rebuild test then decides, as after a pass-2 update), and
-// a particle whose kind changed (boundary lists hold fluid neighbours only) sets *force.
+// in use.  Every slot adds its displacement from the position its list was built at (xb) to
+// the displacement box `disp` (the half step's rebuild test then decides, as after a pass-2
+// update), and a particle whose kind changed (boundary lists hold fluid neighbours only) sets
+// *force.
 // Mixed precision: positions become offsets in the slot's sorted cell, as pass 2 writes them.
 template <class P>
 __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restrict__ pos,
@@ -486,7 +487,7 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
                                 unsigned* err, unsigned* disp, unsigned* force) {
     using T = typename P::T;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    float d2 = 0.f;
+    DispBox box;
     if (k < kp.n) {
         const int r = dst.id[k];
         if ((unsigned)r < (unsigned)kp.n) {
@@ -524,17 +525,15 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
             raise_flags(err, f);
             if (xb && !out_now) {
                 const float4 b = xb[k];
-                const float dx = (float)a.x - b.x, dy = (float)a.y - b.y, dz = (float)a.z - b.z;
-                d2 = dx * dx + dy * dy + dz * dz;
-                if (!(d2 <= 3.0e38f)) d2 = 3.0e38f;  // NaN or overflow: rebuild
+                box.add((float)a.x - b.x, (float)a.y - b.y, (float)a.z - b.z);
             }
         } else {
             atomicOr(force, 1u);  // a consistent permutation never takes this
         }
     }
-    // non-negative floats order like their bit patterns; blockDim is 256, every thread gets here
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(disp, m);
+    // blockDim is 256, every thread gets here
+    __shared__ unsigned s_box[6 * 8];
+    reduce_disp_box(box, disp, s_box);
 }
 
 // Cell keys of a resident set on the current grid (after the grid changed under it).

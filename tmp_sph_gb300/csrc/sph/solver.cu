@@ -255,20 +255,38 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
 }
 
 // Rebuild decision, one thread: rebuild when forced, when the cells are walked every half
-// step (no list), or when some fluid particle has moved farther than skin/2 from where it was
-// at the last build (rb[1] holds the largest squared displacement as float bits).
-// In a graph built with conditional nodes it also sets the condition of the node that holds
-// the rebuild kernels, so a half step without a rebuild launches none of them.
-__global__ void k_decide(unsigned* rb, unsigned threshold_bits, int always,
+// step (no list), or when the box of all displacements since the last build (written by the
+// previous pass 2 or upload, sph_device.cuh) has a half-diagonal beyond skin/2, its square
+// compared with `threshold`.  The box is emptied for the next half step.  In a graph built
+// with conditional nodes it also sets the condition of the node that holds the rebuild
+// kernels, so a half step without a rebuild launches none of them.
+__global__ void k_decide(unsigned* rb, float threshold, int always,
                          cudaGraphConditionalHandle cond, int set_cond) {
-    const bool rebuild = always || rb[2] != 0u || rb[1] > threshold_bits;
+    unsigned* box = rb + RB_DISP;
+    float hd2 = 0.f;
+    for (int c = 0; c < 3; c++) {
+        const unsigned lo = box[c * DISP_STRIDE], hi = box[(3 + c) * DISP_STRIDE];
+        if (lo <= hi) {  // else no particle counted
+            const float r = 0.5f * (ord_value(hi) - ord_value(lo));
+            hd2 += r * r;
+        }
+        box[c * DISP_STRIDE] = 0xffffffffu;
+        box[(3 + c) * DISP_STRIDE] = 0u;
+    }
+    const bool rebuild = always || rb[2] != 0u || !(hd2 <= threshold);
     rb[0] = rebuild ? 1u : 0u;
+    rb[1] = __float_as_uint(hd2);
     if (rebuild) {
-        rb[1] = 0u;
         rb[2] = 0u;
         rb[3] += 1u;
     }
     if (set_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
+}
+
+// Empty displacement box (before an upload fills it, and at allocation).
+__global__ void k_disp_reset(unsigned* rb) {
+    const int c = (int)threadIdx.x;
+    if (c < 6) rb[RB_DISP + c * DISP_STRIDE] = c < 3 ? 0xffffffffu : 0u;
 }
 
 // Conditional-node capture of a half step: the rebuild kernels go into the body of an IF node
@@ -350,11 +368,9 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     const NbrList* nl = list_for(c);
     const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
     const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
-    unsigned thr_bits;
-    memcpy(&thr_bits, &thr, sizeof(thr_bits));
     cudaError_t e;
     if (ev) cudaEventRecord(ev[PH_SORT], s);
-    k_decide<<<1, 1, 0, s>>>(c->rb, thr_bits, nl ? 0 : 1, cc ? cc->handle : 0, cc ? 1 : 0);
+    k_decide<<<1, 1, 0, s>>>(c->rb, thr, nl ? 0 : 1, cc ? cc->handle : 0, cc ? 1 : 0);
     e = cc ? capture_conditional_rebuild<P>(c, k, s, *cc) : rebuild_lists<P>(c, k, s, ev);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
@@ -364,7 +380,7 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     if (ev) cudaEventRecord(ev[PH_PASS2], s);
     // in place: pass 2 reads its neighbours from the pass-1 records
     e = launch_pass2_step<P>(k, half, y, c->keys_sorted, c->cell_start, nl, p1, y, c->hash_x,
-                             c->err, c->rb + 1, s);
+                             c->err, c->rb + RB_DISP, s);
     if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
 }
@@ -474,8 +490,12 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->snap_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = dalloc(&c->rb, 4);
-    if (e == cudaSuccess) e = cudaMemset(c->rb, 0, 4 * sizeof(unsigned));
+    if (e == cudaSuccess) e = dalloc(&c->rb, RB_WORDS);
+    if (e == cudaSuccess) e = cudaMemset(c->rb, 0, RB_WORDS * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        k_disp_reset<<<1, 32>>>(c->rb);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = alloc_list(c);
     for (auto& ev : c->ev)
@@ -693,15 +713,17 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
         dpos = spos; dvel = svel; drho = srho; dp = sp; dtype = stype;
     }
     if (into_order) {
-        // rb[1] restarts from the uploaded positions; a pending forced rebuild (rb[2]) stays
-        if (cudaMemsetAsync(c->rb + 1, 0, sizeof(unsigned), s) != cudaSuccess) return SPH_ERR_CUDA;
+        // the displacement box restarts from the uploaded positions; a pending forced rebuild
+        // (rb[2]) stays
+        k_disp_reset<<<1, 32, 0, s>>>(c->rb);
+        if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
         const NbrList* nl = list_for(c);
         return to_status(with_prec(c, [&](auto tag) {
             using P = decltype(tag);
             return launch_upload_sorted<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho,
                                            dp, dtype, c->keys_sorted, nl ? nl->xb : nullptr,
-                                           State<P>::y(c), c->hash_x, c->err, c->rb + 1,
-                                           c->rb + 2, s);
+                                           State<P>::y(c), c->hash_x, c->err,
+                                           c->rb + RB_DISP, c->rb + 2, s);
         }));
     }
     // the state goes straight into the live set, hashed on the solver's grid; the first half

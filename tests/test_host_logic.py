@@ -37,8 +37,8 @@ def test_autotune_cost_model():
     m1 = {"skin_permille": 100, "pass_ms_per_half_step": 1.1, "rebuild_ms": 3.5}
     # skin 0 rebuilds every half step: 2 passes + 2 rebuilds
     assert math.isclose(autotune.step_cost(m0, P, 2.0), 2.0 + 6.0)
-    # skin 0.1 kh at 2 m/s: a rebuild every 0.1*0.01/(2*1e-4) = 5 steps -> 0.4 per step
-    assert math.isclose(autotune.step_cost(m1, P, 2.0), 2.2 + 0.4 * 3.5)
+    # skin 0.1 kh carried at 2 m/s: a rebuild every 0.1*0.01/(2*1e-4) = 5 steps -> 0.2 per step
+    assert math.isclose(autotune.step_cost(m1, P, 2.0), 2.2 + 0.2 * 3.5)
     # never more than two rebuilds per step
     assert math.isclose(autotune.step_cost(m1, P, 1e3), 2.2 + 2 * 3.5)
     st = {"type": np.array([1, 1, 0]), "pos": np.array([[0, 0, 0.1], [0, 0, 0.3], [0, 0, 0.9]])}

@@ -8,10 +8,11 @@ steps and reads the per-phase device time (SPH_OPT_PROFILE): the cost of a rebui
 gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The step
 cost it ranks by is
 
-    2 t_pass + r t_rebuild,    r = 2 v dt / (skin kh)   (r = 2 with skin 0),
+    2 t_pass + r t_rebuild,    r = v dt / (skin kh)   (r = 2 with skin 0),
 
-with r the rebuilds per step a flow whose fastest particle moves at v needs (the list is
-rebuilt once some particle has moved skin kh / 2).  v defaults to the dam-break surge-front
+with r the rebuilds per step a flow carried at v past static walls needs (the list is rebuilt
+once the box of all displacements has a half-diagonal of skin kh / 2, which such a flow reaches
+after moving skin kh).  v defaults to the dam-break surge-front
 speed 2 sqrt(g H) of the tallest water column H, so a short tuning run from rest does not
 reward a large skin for rebuilds the flow has not needed yet.
 
@@ -81,7 +82,7 @@ def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> d
 
 def step_cost(m: dict, p, v: float) -> float:
     skin = m["skin_permille"] / 1000.0
-    rate = 2.0 if skin <= 0.0 else min(2.0, 2.0 * v * float(p.dt) / (skin * float(p.kh)))
+    rate = 2.0 if skin <= 0.0 else min(2.0, v * float(p.dt) / (skin * float(p.kh)))
     return 2.0 * m["pass_ms_per_half_step"] + rate * m["rebuild_ms"]
 
 

@@ -54,6 +54,7 @@ struct KParamsT {
     int lanes;  // lanes per particle in the list kernels (1, or 2 .. 16: ns_groups.cu)
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
+    T inv_cell;          // 1 / cell (the FP64 and mixed solvers' hash scales by it)
     T h, inv_h, kh, kh2;
     T kh2_list;          // squared list cutoff (support radius + skin); kh2 without a skin
     T eta2;
@@ -85,9 +86,19 @@ template <class T> KParamsT<T> make_kparams_t(const sph_params& p, int n);
 __device__ __forceinline__ int cell_coord(float p, float gmin, float cell) {
     return (int)floorf(__fdiv_rn(__fsub_rn(p, gmin), cell));
 }
-// The FP64 solver's cell of a double position.
-__device__ __forceinline__ int cell_coord(double p, double gmin, double cell) {
-    return (int)floor(__ddiv_rn(__dsub_rn(p, gmin), cell));
+// Cell of a double position (FP64 and mixed-precision solvers, no reference counterpart):
+// the offset from the grid origin in double, scaled by the reciprocal of the cell edge — in
+// float for the mixed solver, whose constants are float — instead of a double division per
+// axis (GB300's FP64 rate is a small fraction of FP32, and three divisions per particle and
+// half step kept the FP64 pipe of the mixed predictor half busy).  Next to a cell face the
+// scaled value can land in the neighbouring cell, by at most its rounding (about 1e-7 of the
+// grid extent); every hash of a double position goes through this one function, so the keys
+// stay consistent, and the neighbour search and the cell offsets absorb such a particle.
+__device__ __forceinline__ int cell_coord_scaled(double p, double gmin, float inv_cell) {
+    return (int)floorf((float)(p - gmin) * inv_cell);
+}
+__device__ __forceinline__ int cell_coord_scaled(double p, double gmin, double inv_cell) {
+    return (int)floor((p - gmin) * inv_cell);
 }
 
 // Reference hash without clamping (src/lib/mesh.cu:20-23).
@@ -135,9 +146,16 @@ __device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT
         y = isfinite(y) ? y : (PT)k.gmin_y;
         z = isfinite(z) ? z : (PT)k.gmin_z;
     }
-    int cx = cell_coord(x, (PT)k.gmin_x, (PT)k.cell);
-    int cy = cell_coord(y, (PT)k.gmin_y, (PT)k.cell);
-    int cz = cell_coord(z, (PT)k.gmin_z, (PT)k.cell);
+    int cx, cy, cz;
+    if constexpr (sizeof(PT) == sizeof(double)) {
+        cx = cell_coord_scaled(x, (double)k.gmin_x, k.inv_cell);
+        cy = cell_coord_scaled(y, (double)k.gmin_y, k.inv_cell);
+        cz = cell_coord_scaled(z, (double)k.gmin_z, k.inv_cell);
+    } else {
+        cx = cell_coord(x, k.gmin_x, k.cell);
+        cy = cell_coord(y, k.gmin_y, k.cell);
+        cz = cell_coord(z, k.gmin_z, k.cell);
+    }
     if ((unsigned)cx >= (unsigned)k.gx || (unsigned)cy >= (unsigned)k.gy ||
         (unsigned)cz >= (unsigned)k.gz_local) {
         *flag |= SPH_FLAG_OUT_OF_GRID;

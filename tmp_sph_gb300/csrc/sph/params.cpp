@@ -42,6 +42,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
     k.cell = p.cell_size;
+    k.inv_cell = 1.0 / (double)p.cell_size;
     k.h = p.h;
     k.inv_h = (float)(1.0 / (double)p.h);
     k.kh = p.kh;
@@ -103,6 +104,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
     k.cell = p.cell_size;
+    k.inv_cell = 1.0 / (double)p.cell_size;
     const double h = p.h, kh = p.kh, cs = p.cs, rho0 = p.rho0;
     k.h = h;
     k.inv_h = 1.0 / h;

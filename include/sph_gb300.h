@@ -238,11 +238,13 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_NEIGHBOR_CAP  5  /* list slots per particle; 0 (default) = 1.5x the lattice
                                     neighbours of the list sphere (reallocates the list) */
 #define SPH_OPT_SKIN_PERMILLE 6  /* neighbour-list skin in thousandths of the support radius kh
-                                    (default 100).  The list keeps every pair closer than
-                                    kh (1 + skin) and is rebuilt, cell list included, only when
-                                    some particle has moved more than skin/2 since the last
-                                    build (decided on the GPU each half step); 0 rebuilds every
-                                    half step as the reference does */
+                                    (default 100; the cells are kh (1 + skin) wide).  The list
+                                    keeps every pair closer than kh (1 + skin) and is rebuilt,
+                                    cell list included, only when the bounding box of all
+                                    displacements since the last build has a half-diagonal over
+                                    skin/2 (decided on the GPU each half step); 0 rebuilds every
+                                    half step as the reference does.  With
+                                    SPH_OPT_ADAPTIVE_SKIN the lists use a skin up to this one */
 #define SPH_OPT_CONDITIONAL_GRAPH 7  /* 1 (default): the replayed step graph holds the rebuild
                                     kernels under conditional nodes, so a half step that keeps
                                     its lists launches none of them; 0: they are launched and
@@ -257,6 +259,10 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_PAIRS 11  /* 1: the neighbour kernels take two consecutive particles per thread
                              over the union of their neighbour lists, gathering each neighbour
                              record once for both (FP32 and FP64; ignored in mixed precision) */
+#define SPH_OPT_ADAPTIVE_SKIN 13  /* 1 (default): each list rebuild picks the skin of the next
+                             lists, between 0.02 and SPH_OPT_SKIN_PERMILLE, from how long the
+                             last lists lasted (tight lists for slow flow, wide for fast); 0: the
+                             lists always use SPH_OPT_SKIN_PERMILLE */
 #define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in the list kernels:
                              1 (one thread per particle), 2, 4, 8 or 16 (a group of lanes shares a
                              particle's list and reduces its sums; not with SPH_OPT_PAIRS) */
@@ -346,6 +352,8 @@ int sph_steps_taken(const sph_ctx* ctx, long long* steps);
 int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
 /* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream). */
 int sph_read_rebuild_count(sph_ctx* ctx, unsigned* count, void* stream);
+/* Skin of the current neighbour lists as a fraction of kh (synchronises the stream). */
+int sph_read_list_skin(sph_ctx* ctx, float* skin, void* stream);
 
 /* ---------------------------------------------------------------- probes and reductions */
 /* Measurements of the resident state computed on the GPU (no reference counterpart: the

@@ -419,7 +419,8 @@ def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):
     fl = st["type"] == 1
     st["vel"][fl] = np.array([1.0, 0.0, 0.0], np.float32)
     steps = 60
-    out, flags = run_opts(st, p, steps, {api.SPH_OPT_SKIN_PERMILLE: 100})
+    fixed = {api.SPH_OPT_SKIN_PERMILLE: 100, api.SPH_OPT_ADAPTIVE_SKIN: 0}
+    out, flags = run_opts(st, p, steps, fixed)
     skin = 0.1 * float(p.kh)
     per_build = skin / (1.0 * float(p.dt))  # steps a uniform 1 m/s carry takes to reach skin
     report("uniform carry: list rebuilds in 60 steps", out["rebuilds"], 1 + steps / per_build)
@@ -430,9 +431,44 @@ def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):
     for k, v in e.items():
         report(f"uniform carry 60 steps {k}", v, 2e-4)
     assert all(v < 2e-4 for v in e.values()), e
-    walk, wflags = run_opts(st, p, steps, {api.SPH_OPT_SKIN_PERMILLE: 100,
-                                           api.SPH_OPT_NEIGHBOR_CAP: 8})
+    walk, wflags = run_opts(st, p, steps, {**fixed, api.SPH_OPT_NEIGHBOR_CAP: 8})
     assert wflags & api.SPH_FLAG_NEIGHBOR_OVERFLOW
     assert walk["rebuilds"] == out["rebuilds"]
     for k in ("pos", "vel", "rho", "p"):
         assert np.array_equal(walk[k], out[k]), k
+
+
+def test_adaptive_skin(sphlib, oracle, cuda, report):
+    """The lists start tight (skin 0.02 kh) and stay near that while the flow is slow; fast flow
+    widens them towards the skin option; with the option off they use it throughout.  The
+    fields match the oracle either way."""
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    from gpu_util import perturbed
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    P = oracle.params_like(p)
+    for name, state, steps in (("rest", st, 20), ("fast", perturbed(st, vamp=2.0, ramp=0.0), 30)):
+        s = torch.cuda.Stream()
+        with S.Solver(p, len(state["rho"])) as sol:
+            sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 100)
+            sol.upload(state["pos"], state["vel"], state["rho"], state["p"], state["type"],
+                       stream=s)
+            assert abs(sol.list_skin(stream=s) - 0.02) < 1e-6
+            sol.step(steps, stream=s)
+            skin = sol.list_skin(stream=s)
+            rebuilds = sol.rebuild_count(stream=s)
+            out = sol.download(stream=s)
+            assert sol.error_flags(stream=s) == 0
+            sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, 0)
+            assert abs(sol.list_skin(stream=s) - 0.1) < 1e-6
+        report(f"adaptive skin, {name}: skin after {steps} steps", skin)
+        report(f"adaptive skin, {name}: rebuilds", rebuilds)
+        if name == "rest":
+            assert 0.02 - 1e-6 <= skin <= 0.03
+        else:
+            assert skin > 0.04 and rebuilds >= 3
+        ref = oracle.run(P, state, steps)
+        e = field_errors(out, ref, state)
+        for k, v in e.items():
+            report(f"adaptive skin, {name}, {steps} steps {k}", v, 2e-4)
+        assert all(v < 2e-4 for v in e.values()), (name, e)

@@ -79,6 +79,7 @@ def test_moved_particles_rebuild(sphlib, oracle, cuda, report):
     s = torch.cuda.Stream()
     with S.Solver(p, len(st["rho"])) as sol:
         sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 100)
+        sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, 0)  # the shifts are measured in this skin
         hst = _pinned(st)
         sol.step_host(hst, 1, stream=s)
         base = sol.rebuild_count(stream=s)

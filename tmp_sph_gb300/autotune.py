@@ -107,6 +107,8 @@ def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=
     stream = torch.cuda.Stream()
     table = []
     with S.Solver(p, n, precision=precision) as sol:
+        # every candidate's lists at its own skin (no adaptive skin while measuring)
+        sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, 0)
         _upload(sol, states, stream)
         for t, k, g, s in candidates(threads, ppt, skins, lanes):
             m = measure(sol, stream, t, k, s, g)

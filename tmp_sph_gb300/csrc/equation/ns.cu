@@ -165,7 +165,8 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     SlotWriter w{nl.idx + nbr_col(nl, i), nl.cap, stage};
-    walk_pairs<P, 1>(k, cs, keys, X, i, pi, k.kh2_list,
+    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
+    walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
         if (keep_all || fluid_rec(pj.w))
             w.put(P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j);
@@ -332,13 +333,14 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
     const bool keep0 = fluid_rec(p0.w) || walls_all;
     const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
     SlotWriter w{nl.idx + nbr_col(nl, c), nl.cap, stage};
+    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     auto visit = [&](int j) {
         const V pj = ld_pos(X, (size_t)j);
         const bool fj = fluid_rec(pj.w);
-        bool in = dist2(p0.x - pj.x, p0.y - pj.y, p0.z - pj.z) < k.kh2_list && j != i0 &&
+        bool in = dist2(p0.x - pj.x, p0.y - pj.y, p0.z - pj.z) < cut2 && j != i0 &&
                   (keep0 || fj);
         if (has1)
-            in = in || (dist2(p1.x - pj.x, p1.y - pj.y, p1.z - pj.z) < k.kh2_list && j != i1 &&
+            in = in || (dist2(p1.x - pj.x, p1.y - pj.y, p1.z - pj.z) < cut2 && j != i1 &&
                         (keep1 || fj));
         if (in) w.put(j);
     };

@@ -141,6 +141,7 @@ __device__ __forceinline__ void build_group(const KParamsT<typename P::T>& k,
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     int cx = 0, cy = 0, cz = 0;
     if (live) cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     int cnt = 0;
 #pragma unroll 1
     for (int t = 0; t < 9; t++) {
@@ -156,7 +157,7 @@ __device__ __forceinline__ void build_group(const KParamsT<typename P::T>& k,
                 if constexpr (P::kMixed) code = strip_code(st, t, cx, j);
                 T dx, dy, dz;
                 rel_pos<P>(k, pi, pj, code, dx, dy, dz);
-                hit = dist2(dx, dy, dz) < k.kh2_list && j != i && (keep_all || fluid_rec(pj.w));
+                hit = dist2(dx, dy, dz) < cut2 && j != i && (keep_all || fluid_rec(pj.w));
             }
             const unsigned m = group_bits<G>(__ballot_sync(FULL_MASK, hit));
             if (hit) {

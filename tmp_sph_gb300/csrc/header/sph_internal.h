@@ -117,6 +117,9 @@ struct NbrList {
     int* count = nullptr;
     int cap = 0;
     float4* xb = nullptr;
+    // squared list cutoff chosen on the device at each rebuild (adaptive skin); NULL: the
+    // constant block's kh2_list
+    const float* cut2 = nullptr;
 };
 // List slots per particle (per pair of particles with pairs): 1.5x the lattice particles within
 // kh (1 + skin), rounded up to 16.
@@ -230,8 +233,12 @@ cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float*
 cudaError_t launch_ns_writeback(const KParams& k, const int* s_type, const float4* self,
                                 float* s_rho, float* s_p, float* dofv, cudaStream_t s);
 
-// Layout of the rebuild block: four control words, then the displacement box (DISP_WORDS,
-// 128-byte aligned).
+// Layout of the rebuild block: four control words, the list skin control, then the
+// displacement box (DISP_WORDS, 128-byte aligned).
+constexpr int RB_SKIN = 4;  // skin of the current lists, as a fraction of kh (float bits)
+constexpr int RB_HS = 5;    // half steps since the last build
+constexpr int RB_CUT2 = 6;  // squared list cutoff kh^2 (1 + skin)^2 (float bits)
+constexpr int RB_THR = 7;   // rebuild threshold (skin kh / 2)^2 on the box (float bits)
 constexpr int RB_DISP = 32;
 constexpr int RB_WORDS = RB_DISP + DISP_WORDS;
 
@@ -302,6 +309,7 @@ struct sph_ctx {
     int opt_ppt = 1;         // neighbour kernels: particles per thread
     int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
     int opt_lanes = 1;       // neighbour-list kernels: lanes per particle
+    int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

@@ -254,13 +254,65 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     return k;
 }
 
+// Skin of the neighbour lists.  The cells are sized for the largest skin s_max (the option);
+// with `adapt`, each rebuild picks the skin s <= s_max of the next lists from how long the last
+// ones lasted.  A list of skin s costs passes over about (1 + s)^3 times the pairs within kh
+// and lasts until the displacement box has grown to s kh / 2; with the box growing at the rate
+// just seen, a list of skin s lasts n s / s_cur half steps.  Balancing the extra pass work of
+// a larger skin against the rebuilds it saves (a rebuild costs about as much as three passes'
+// share of skin pairs at s = 0.1: `ratio`) gives s ~ sqrt(ratio s_cur / n); the new skin is
+// the geometric mean of that and the current one, within [s_min, s_max].  A flow at rest keeps
+// tight lists (a dam break's first hundreds of steps); a surge widens them to s_max.
+struct SkinControl {
+    float kh, s_min, s_max, ratio;
+    int adapt;
+};
+
+__device__ __forceinline__ void set_skin(unsigned* rb, const SkinControl& sc, float s) {
+    const float cut = sc.kh * (1.f + s), half = 0.5f * s * sc.kh;
+    rb[RB_SKIN] = __float_as_uint(s);
+    rb[RB_CUT2] = __float_as_uint(cut * cut);
+    rb[RB_THR] = __float_as_uint(half * half);
+    rb[RB_HS] = 0u;
+}
+
+// Skin of the first lists after an upload or a change of parameters.
+__global__ void k_skin_init(unsigned* rb, SkinControl sc) {
+    if (threadIdx.x == 0) set_skin(rb, sc, sc.adapt ? sc.s_min : sc.s_max);
+}
+
+SkinControl skin_control(const sph_ctx* c) {
+    SkinControl sc;
+    sc.kh = c->P.kh;
+    sc.s_max = c->skin > 0.0 ? (float)c->skin : 0.f;
+    sc.s_min = std::min(sc.s_max, 0.02f);
+    sc.ratio = 1.f;
+    sc.adapt = (c->opt_adaptive_skin && sc.s_max > 0.f) ? 1 : 0;
+    return sc;
+}
+
+cudaError_t reset_skin(sph_ctx* c, cudaStream_t s) {
+    k_skin_init<<<1, 32, 0, s>>>(c->rb, skin_control(c));
+    return cudaGetLastError();
+}
+
+// The same, between calls on any stream: the device is idle first, so no half step in flight
+// reads the skin words while they change.
+cudaError_t reset_skin_sync(sph_ctx* c) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = reset_skin(c, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e;
+}
+
 // Rebuild decision, one thread: rebuild when forced, when the cells are walked every half
 // step (no list), or when the box of all displacements since the last build (written by the
 // previous pass 2 or upload, sph_device.cuh) has a half-diagonal beyond skin/2, its square
-// compared with `threshold`.  The box is emptied for the next half step.  In a graph built
-// with conditional nodes it also sets the condition of the node that holds the rebuild
-// kernels, so a half step without a rebuild launches none of them.
-__global__ void k_decide(unsigned* rb, float threshold, int always,
+// compared with the threshold of the current lists.  A rebuild picks the next skin (above).
+// The box is emptied for the next half step.  In a graph built with conditional nodes it also
+// sets the condition of the node that holds the rebuild kernels, so a half step without a
+// rebuild launches none of them.
+__global__ void k_decide(unsigned* rb, SkinControl sc, int always,
                          cudaGraphConditionalHandle cond, int set_cond) {
     unsigned* box = rb + RB_DISP;
     float hd2 = 0.f;
@@ -273,12 +325,22 @@ __global__ void k_decide(unsigned* rb, float threshold, int always,
         box[c * DISP_STRIDE] = 0xffffffffu;
         box[(3 + c) * DISP_STRIDE] = 0u;
     }
-    const bool rebuild = always || rb[2] != 0u || !(hd2 <= threshold);
+    const bool forced = rb[2] != 0u;
+    const bool rebuild = always || forced || !(hd2 <= __uint_as_float(rb[RB_THR]));
+    const unsigned hs = rb[RB_HS] + 1u;
     rb[0] = rebuild ? 1u : 0u;
     rb[1] = __float_as_uint(hd2);
     if (rebuild) {
+        float s = __uint_as_float(rb[RB_SKIN]);
+        if (sc.adapt && !always && !forced && s > 0.f) {
+            const float want = sqrtf(sc.ratio * s / (float)hs);
+            s = fminf(fmaxf(sqrtf(s * want), sc.s_min), sc.s_max);
+        }
+        set_skin(rb, sc, s);
         rb[2] = 0u;
         rb[3] += 1u;
+    } else {
+        rb[RB_HS] = hs;
     }
     if (set_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
 }
@@ -366,11 +428,10 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     auto& y = State<P>::y(c);
     auto& p1 = State<P>::p1(c);
     const NbrList* nl = list_for(c);
-    const float half_skin = (float)(0.5 * c->skin * (double)c->P.kh);
-    const float thr = c->skin > 0.0 ? half_skin * half_skin : 0.0f;
     cudaError_t e;
     if (ev) cudaEventRecord(ev[PH_SORT], s);
-    k_decide<<<1, 1, 0, s>>>(c->rb, thr, nl ? 0 : 1, cc ? cc->handle : 0, cc ? 1 : 0);
+    k_decide<<<1, 1, 0, s>>>(c->rb, skin_control(c), nl ? 0 : 1, cc ? cc->handle : 0,
+                             cc ? 1 : 0);
     e = cc ? capture_conditional_rebuild<P>(c, k, s, *cc) : rebuild_lists<P>(c, k, s, ev);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
@@ -456,6 +517,7 @@ cudaError_t alloc_list(sph_ctx* c) {
         return e;
     }
     c->nl.cap = cap;
+    c->nl.cut2 = reinterpret_cast<const float*>(c->rb + RB_CUT2);
     return cudaSuccess;
 }
 
@@ -496,6 +558,8 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
         k_disp_reset<<<1, 32>>>(c->rb);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess) e = reset_skin(c, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = alloc_list(c);
     for (auto& ev : c->ev)
@@ -550,6 +614,7 @@ extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
         cudaGetLastError();
         return SPH_ERR_NOMEM;
     }
+    if (reset_skin_sync(c) != cudaSuccess) return SPH_ERR_CUDA;  // kh may have changed
     return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }
 
@@ -577,6 +642,10 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             c->opt_ppt = value;
             drop_graph(c);
             return SPH_OK;
+        case SPH_OPT_ADAPTIVE_SKIN:
+            c->opt_adaptive_skin = value != 0;
+            if (reset_skin_sync(c) != cudaSuccess) return SPH_ERR_CUDA;
+            break;  // the next lists take the first skin of the new mode
         case SPH_OPT_LANES_PER_PARTICLE:
             if (value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
                 return SPH_ERR_ARG;
@@ -634,6 +703,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
                 c->Pi = pi;
                 c->gz_inst = gz_local;
                 c->rehash = c->loaded;
+                if (reset_skin_sync(c) != cudaSuccess) return SPH_ERR_CUDA;
             }
             drop_graph(c);
             if (alloc_list(c) != cudaSuccess) {
@@ -729,7 +799,7 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
     // the state goes straight into the live set, hashed on the solver's grid; the first half
     // step sorts it
     if (cudaMemsetAsync(c->rb, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
-        force_rebuild(c, s) != cudaSuccess)
+        reset_skin(c, s) != cudaSuccess || force_rebuild(c, s) != cudaSuccess)
         return SPH_ERR_CUDA;
     return to_status(with_prec(c, [&](auto tag) {
         using P = decltype(tag);
@@ -1073,7 +1143,10 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
         return SPH_ERR_CUDA;
     if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
-    const NbrList* nl = list_for(c);
+    // the drop-in builds and uses its list within this call, with the constant cutoff
+    NbrList dl = c->nl;
+    dl.cut2 = nullptr;
+    const NbrList* nl = list_for(c) ? &dl : nullptr;
     if (nl && (e = launch_nbr_build<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, *nl,
                                     c->opt_wall_rates, c->err, s)) != cudaSuccess)
         return SPH_ERR_CUDA;
@@ -1088,6 +1161,18 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     // the resident state (y) is untouched, but the cell and neighbour lists now describe these
     // arrays: a later sph_step rebuilds them first
     return force_rebuild(c, s) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
+extern "C" int sph_read_list_skin(sph_ctx* c, float* skin, void* stream) {
+    if (!c || !skin) return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, c->rb + RB_SKIN, sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SPH_ERR_CUDA;
+    std::memcpy(skin, &h, sizeof(float));
+    return SPH_OK;
 }
 
 extern "C" int sph_read_rebuild_count(sph_ctx* c, unsigned* count, void* stream) {

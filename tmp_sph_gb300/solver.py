@@ -153,6 +153,12 @@ class Solver:
         call("sph_read_rebuild_count", self.handle, C.byref(v), _stream(stream))
         return v.value
 
+    def list_skin(self, stream=None) -> float:
+        """Skin of the current neighbour lists, as a fraction of kh."""
+        v = C.c_float(0)
+        call("sph_read_list_skin", self.handle, C.byref(v), _stream(stream))
+        return v.value
+
     def probe(self, probes=(), cfl: float = 0.25, stream=None) -> tuple[list, dict]:
         """Probe values (one per (kind, x, y, z, radius, zmax) tuple or api.SphProbe) and the
         FP64 fluid statistics, computed on the GPU (synchronises)."""

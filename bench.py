@@ -232,7 +232,7 @@ def config_block(args, p, n):
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
             "graph_mode": args.graph_mode, "pairs": args.pairs,
-            "lanes_per_particle": args.lanes}
+            "lanes_per_particle": args.lanes, "adaptive_skin": args.adaptive_skin}
 
 
 def run_batch(args):
@@ -262,6 +262,7 @@ def run_batch(args):
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+    sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload_instances(states, stream=stream)
@@ -340,6 +341,8 @@ def main():
                     help="two particles per thread over a union neighbour list (FP32, FP64)")
     ap.add_argument("--lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
                     help="lanes per particle in the neighbour-list kernels")
+    ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
+                    help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -371,6 +374,7 @@ def main():
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+    sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
@@ -421,6 +425,7 @@ def main():
         v = S.Solver(p, n, precision=precision)
         v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
         v.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+        v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
         v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         v.step(3, stream=stream)
         torch.cuda.synchronize()

@@ -31,10 +31,11 @@
 // and step.  A particle with more hits than
 // the list capacity is marked and walks the cells itself (same order again).
 //
-// With a Verlet skin the list is built with the cutoff kh(1 + skin) (kh2_list) on cells that
-// wide and kept while every particle stays within skin*kh/2 of its build position; both
-// passes still test r < kh on the current positions, and k_nbr_build keeps the build
-// positions (xb) that pass 2 measures each particle's displacement against.
+// With a Verlet skin the list is built with the cutoff kh(1 + s) (NbrList::cut2, else
+// kh2_list) on cells kh(1 + skin) wide, s <= skin, and kept while the displacements since the
+// build stay within the bound the solver's rebuild test checks; both passes still test r < kh
+// on the current positions, and k_nbr_build keeps the build positions (xb) that pass 2
+// measures each particle's displacement against.
 //
 // Precision.  Every kernel is instantiated for the three policies of sph_internal.h: FP32
 // (records of float4), FP64 (records of two 32-byte double vectors) and mixed.  The mixed

@@ -6,7 +6,7 @@
 //
 //   rebuild decision  ->  [radix sort (cell key, slot)  ->  gather y -> x -> y in cell order
 //   + dense cell starts  ->  neighbour-list build (y)]  ->  pass 1 (y -> records p1)
-//   ->  pass 2 + integrator (p1 -> y in place, next cell keys, largest displacement)
+//   ->  pass 2 + integrator (p1 -> y in place, next cell keys, displacement box)
 //
 // so the state never returns to original order inside a step (the original particle id
 // travels with it and is used only by sph_download), there is no separate hash kernel
@@ -14,13 +14,14 @@
 // of launches, captured once as a CUDA graph and replayed.
 //
 // Verlet skin.  The cells are kh(1 + skin) wide and the list holds every pair closer than
-// kh(1 + skin) at build time.  While no particle has moved more than skin*kh/2 since the
-// build, every pair now closer than kh is in the list, so the bracketed kernels are skipped:
-// k_decide (one thread, on the GPU) compares the largest displacement pass 2 recorded with
-// that bound and writes a gate word the gated kernels read before doing any work.  The
-// passes test r < kh themselves, so they evaluate the same pairs as a rebuild every half
-// step; only the order of the sums within a particle can differ.  skin = 0 rebuilds every
-// half step on the reference's cell size.
+// kh(1 + s) at build time, s <= skin (the adaptive skin below picks s at each rebuild).
+// While the bounding box of all displacements since the build has a half-diagonal below
+// s kh / 2, no two particles have closed in by more than s kh, so every pair now closer than
+// kh is in the list and the bracketed kernels are skipped: k_decide (one thread, on the GPU)
+// compares the box pass 2 recorded with that bound and writes a gate word the gated kernels
+// read before doing any work.  The passes test r < kh themselves, so they evaluate the same
+// pairs as a rebuild every half step; only the order of the sums within a particle can
+// differ.  skin = 0 rebuilds every half step on the reference's cell size.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -165,6 +165,22 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     const vec4_t<T> pi = X[i];
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
+    if (!keep_all && nl.fluid_cells && !inactive_key(k, keys[i])) {
+        // a boundary particle with no fluid in its 27 cells has an empty list
+        int cx, cy, cz;
+        cell_of_key(k.gx, k.gy, keys[i], cx, cy, cz);
+        bool any = false;
+        for (int z = max(cz - 1, 0); z <= min(cz + 1, k.gz - 1); z++)
+            for (int y = max(cy - 1, 0); y <= min(cy + 1, k.gy - 1); y++) {
+                const int row = (z * k.gy + y) * k.gx;
+                for (int x = max(cx - 1, 0); x <= min(cx + 1, k.gx - 1); x++)
+                    any = any || __ldg(nl.fluid_cells + row + x) != 0;
+            }
+        if (!any) {
+            nl.count[i] = 0;
+            return;
+        }
+    }
     SlotWriter w{nl.idx + nbr_col(nl, i), nl.cap, stage};
     const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,

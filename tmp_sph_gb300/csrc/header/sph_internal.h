@@ -29,9 +29,11 @@ int key_bits_for(int num_cells);
 
 // ---------------------------------------------------------------- cell list (lib/mesh.cu)
 // Dense cell starts: cell_start[c] = first sorted slot whose key >= c, for c in [0, C];
-// cell_start[C] = n.  Keys must be sorted and < C.
+// cell_start[C] = n.  Keys must be sorted and < C.  With `type` and `fluid_cells` (C + 4 bytes),
+// also marks the cells that hold a fluid particle.
 cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
-                              int* cell_start, cudaStream_t s, const unsigned* gate = nullptr);
+                              int* cell_start, cudaStream_t s, const unsigned* gate = nullptr,
+                              const int* type = nullptr, unsigned char* fluid_cells = nullptr);
 
 // ---------------------------------------------------------------- precision policies
 // The resident solver in three precisions sharing one code path:
@@ -120,6 +122,10 @@ struct NbrList {
     // squared list cutoff chosen on the device at each rebuild (adaptive skin); NULL: the
     // constant block's kh2_list
     const float* cut2 = nullptr;
+    // cells holding a fluid particle (marked with the cell starts); NULL: not known.  A
+    // boundary particle keeps fluid neighbours only, so one with no such cell among its 27
+    // has an empty list without walking them.
+    const unsigned char* fluid_cells = nullptr;
 };
 // List slots per particle (per pair of particles with pairs): 1.5x the lattice particles within
 // kh (1 + skin), rounded up to 16.
@@ -268,6 +274,7 @@ struct sph_ctx {
     unsigned* hash_x = nullptr;      // next cell of every slot of x
     unsigned* keys_sorted = nullptr; // sorted cell keys of y
     int* perm = nullptr;             // y slot k came from x slot perm[k]
+    unsigned char* fluid_cells = nullptr;  // cells holding fluid, per list build
     sph::Pass1Out p1;                // pass-1 output
     sph::ParticleSetT<double> xd, yd;
     sph::Pass1OutT<double> p1d;

@@ -243,11 +243,13 @@ cudaError_t fill_u32(unsigned* p, unsigned value, long count, const unsigned* ga
 
 // ---------------------------------------------------------------- dense cell starts
 __global__ void k_cell_mark(const unsigned* __restrict__ keys, int n, int num_cells,
-                            int* __restrict__ cs, const unsigned* gate) {
+                            int* __restrict__ cs, const unsigned* gate,
+                            const int* __restrict__ type, unsigned char* __restrict__ fluid) {
     if (gated_off(gate)) return;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     unsigned key = keys[k];
+    if (fluid && key < (unsigned)num_cells && type[k] == SPH_TYPE_FLUID) fluid[key] = 1;
     // key num_cells starts the tail of slots outside every cell (park_inactive)
     if ((k == 0 || keys[k - 1] != key) && key <= (unsigned)num_cells) cs[key] = k;
 }
@@ -727,11 +729,21 @@ cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsign
 }
 
 cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells, int* cs,
-                              cudaStream_t s, const unsigned* gate) {
+                              cudaStream_t s, const unsigned* gate, const int* type,
+                              unsigned char* fluid_cells) {
     cudaError_t e = fill_u32(reinterpret_cast<unsigned*>(cs), 0x7f7f7f7fu, (long)num_cells + 1,
                              gate, s);
     if (e != cudaSuccess) return e;
-    if (n > 0) k_cell_mark<<<blocks_for(n, 256), 256, 0, s>>>(sorted_keys, n, num_cells, cs, gate);
+    if (fluid_cells && type) {
+        e = fill_u32(reinterpret_cast<unsigned*>(fluid_cells), 0u, ((long)num_cells + 4) / 4,
+                     gate, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        fluid_cells = nullptr;
+    }
+    if (n > 0)
+        k_cell_mark<<<blocks_for(n, 256), 256, 0, s>>>(sorted_keys, n, num_cells, cs, gate, type,
+                                                       fluid_cells);
     k_cell_fill<<<blocks_for((long)num_cells + 1, FILL_CHUNK), FILL_THREADS, 0, s>>>(
         cs, num_cells, sorted_keys, n, gate);
     return cudaGetLastError();

@@ -140,6 +140,8 @@ void release(sph_ctx* c) {
     free_state(c);
     cudaFree(c->hash_x); cudaFree(c->keys_sorted); cudaFree(c->perm);
     cudaFree(c->cell_start); cudaFree(c->sort_scratch); cudaFree(c->err);
+    cudaFree(c->fluid_cells);
+    c->fluid_cells = nullptr;
     cudaFree(c->nl.idx); cudaFree(c->nl.count); cudaFree(c->nl.xb);
     c->nl = NbrList{};
     cudaFree(c->rb);
@@ -201,7 +203,10 @@ bool params_ok(const sph_params* p) {
 constexpr int EV_PER_HALF = PH_COUNT + 1;
 
 // The neighbour list to use this half step, or NULL to walk the cells in every pass.
-const NbrList* list_for(sph_ctx* c) { return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr; }
+const NbrList* list_for(sph_ctx* c) {
+    c->nl.fluid_cells = c->fluid_cells;
+    return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr;
+}
 
 // The resident solver's own grid: the caller's grid box with cells of kh (1 + skin), so a walk
 // of the 27 cells around a particle's cell at the last rebuild still finds every particle
@@ -378,7 +383,8 @@ cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStre
     if ((e = launch_gather<P>(k, c->perm, y, x, 1, c->keys_sorted, s, gate)) != cudaSuccess)
         return e;
     if ((e = launch_gather<P>(k, nullptr, x, y, 1, nullptr, s, gate)) != cudaSuccess) return e;
-    if ((e = build_cell_starts(c->keys_sorted, c->n, c->Pi.num_cells, c->cell_start, s, gate)) !=
+    if ((e = build_cell_starts(c->keys_sorted, c->n, c->Pi.num_cells, c->cell_start, s, gate,
+                               y.type, c->fluid_cells)) !=
         cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[PH_NBR], s);
@@ -542,6 +548,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = dalloc(&c->perm, cap);
     c->cell_capacity = std::max(p->num_cells, c->Pi.num_cells);
     if (e == cudaSuccess) e = dalloc(&c->cell_start, (size_t)c->cell_capacity + 1);
+    if (e == cudaSuccess) e = cudaMalloc(&c->fluid_cells, (size_t)c->cell_capacity + 4);
     c->sort_scratch_bytes = sort_scratch_bytes(cap);
     if (e == cudaSuccess) e = cudaMalloc(&c->sort_scratch, c->sort_scratch_bytes);
     if (e == cudaSuccess) e = dalloc(&c->err, 1);
@@ -587,13 +594,18 @@ extern "C" int sph_destroy(sph_ctx* c) {
 static cudaError_t ensure_cells(sph_ctx* c, int cells) {
     if (cells <= c->cell_capacity) return cudaSuccess;
     int* cs = nullptr;
+    unsigned char* fc = nullptr;
     cudaError_t e = dalloc(&cs, (size_t)cells + 1);
+    if (e == cudaSuccess) e = cudaMalloc(&fc, (size_t)cells + 4);
     if (e != cudaSuccess) {
+        cudaFree(cs);
         cudaGetLastError();
         return e;
     }
     cudaFree(c->cell_start);
+    cudaFree(c->fluid_cells);
     c->cell_start = cs;
+    c->fluid_cells = fc;
     c->cell_capacity = cells;
     return cudaSuccess;
 }
@@ -1147,6 +1159,7 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     // the drop-in builds and uses its list within this call, with the constant cutoff
     NbrList dl = c->nl;
     dl.cut2 = nullptr;
+    dl.fluid_cells = nullptr;
     const NbrList* nl = list_for(c) ? &dl : nullptr;
     if (nl && (e = launch_nbr_build<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, *nl,
                                     c->opt_wall_rates, c->err, s)) != cudaSuccess)

@@ -297,21 +297,20 @@ struct Pass2Acc {
         const bool fj = fluid_rec(vj.w);
         const T rhoj = dabs(vj.w);
         const T rr = pair_sqrt(r2);
-        const T q = rr * k.inv_h;
-        const T t = T(1) - T(0.5) * q;
-        const T fr = k.c_fr * t * t * t;
+        const T t = T(1) - T(0.5) * k.inv_h * rr;
+        // m / rho_j grad W / r in one factor: c_fr m t^3 / rho_j
+        const T w = k.c_fr_mass * (t * t) * t * pair_rcp(rhoj);
         const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-        const T volj = k.mass * pair_rcp(rhoj);
         const T inv_r2e = pair_rcp(r2 + k.eta2);
-        sd.add(volj * fr * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
+        sd.add(w * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
         T S;
-        if (fi) {
+        if (MODE != MODE_RATES || fi) {  // the integrating passes only visit fluid rows
             S = -presi - aj.w;
             if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
         } else {
             S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
         }
-        const T c = fr * S * volj;
+        const T c = w * S;
         sx.add(c * dx);
         sy.add(c * dy);
         sz.add(c * dz);

@@ -60,6 +60,7 @@ struct KParamsT {
     T eta2;
     T adh;               // 21/(16 pi h^3)
     T c_fr;              // -5 adh / h^2: grad W = c_fr (1 - q/2)^3 r
+    T c_fr_mass;         // c_fr * mass
     T mass, rho0, cs, g, half_dt;
     T delta_h_cs;        // delta h cs
     T damper;            // rho0 cs h

@@ -52,6 +52,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.adh = p.adh;
     k.c_fr = (float)(-5.0 * (double)p.adh / ((double)p.h * (double)p.h));
     k.mass = p.mass;
+    k.c_fr_mass = (float)(-5.0 * (double)p.adh / ((double)p.h * (double)p.h) * (double)p.mass);
     k.rho0 = p.rho0;
     k.cs = p.cs;
     k.g = p.gravity;
@@ -115,6 +116,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.adh = p.adh;
     k.c_fr = -5.0 * (double)p.adh / (h * h);
     k.mass = p.mass;
+    k.c_fr_mass = -5.0 * (double)p.adh / (h * h) * (double)p.mass;
     k.rho0 = rho0;
     k.cs = cs;
     k.g = p.gravity;

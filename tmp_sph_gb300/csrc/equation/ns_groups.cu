@@ -16,8 +16,8 @@
 // bit-equal to one lane per particle (the sums associate differently).
 //
 // List layout.  The 32/G particles a warp handles together share a block of cap * 32/G slots
-// in which step t (entries tG .. tG + G - 1 of each of them) is 32 consecutive ints: one line
-// per warp and step.  The build walks the cells with the whole group, G candidates per step,
+// in which each lane's entries come four to an int4 (gslot): a warp reads four entries of
+// every lane with one 16-byte load per lane.  The build walks the cells with the whole group, G candidates per step,
 // and compacts the hits with a ballot, so the list holds the same entries in the same (walk)
 // order as the one-lane build.
 //
@@ -52,19 +52,26 @@ __device__ __forceinline__ unsigned group_bits(unsigned ballot) {
     }
 }
 
-// Entry c of particle i in the group layout.
+// Entry c of particle i in the group layout.  The 32/G particles a warp handles together
+// share a block of cap * 32/G slots; lane L = (i mod 32/G) G + c mod G of the warp holds
+// entries c = s, s + G, s + 2G, ... of its particle, and its entries 4m .. 4m+3 (in that
+// order) are one int4 at block + 128 m + 4 L: a warp reads four entries of every lane with
+// one 16-byte load per lane, as the one-lane layout does.
 template <int G>
 __device__ __forceinline__ size_t gslot(const NbrList& nl, int i, int c) {
     constexpr unsigned PPW = 32 / G;
     const unsigned ui = (unsigned)i, uc = (unsigned)c;
-    return (size_t)(ui / PPW) * ((size_t)nl.cap * PPW) + (size_t)(uc / G) * 32u +
-           (size_t)((ui % PPW) * G + uc % G);
+    const unsigned lane = (ui % PPW) * G + uc % G, t = uc / G;
+    return (size_t)(ui / PPW) * ((size_t)nl.cap * PPW) + (size_t)(t >> 2) * 128u +
+           (size_t)(lane * 4u + (t & 3u));
 }
 
-// One list slot, read past L1 (the slots stream through once per pass).
-__device__ __forceinline__ int ld_slot(const int* p) {
-    int v;
-    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+// Four list slots, read past L1 (the slots stream through once per pass).
+__device__ __forceinline__ int4 ld_slots4(const int* p) {
+    int4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
     return v;
 }
 
@@ -215,15 +222,20 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
             const T r2 = dist2(dx, dy, dz);
             if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
         };
-        int c = s;
+        // this lane's entries s, s + G, ...: n of them, four per int4, the next int4 loaded
+        // one group ahead (four record gathers in flight per lane)
+        const int n = cnt > s ? (cnt - s + G - 1) / G : 0;
+        const int* __restrict__ col = nl.idx + gslot<G>(nl, i, s);
+        int4 q = n > 0 ? ld_slots4(col) : make_int4(0, 0, 0, 0);
 #pragma unroll 1
-        for (; c + G < cnt; c += 2 * G) {
-            const int e0 = ld_slot(nl.idx + gslot<G>(nl, i, c));
-            const int e1 = ld_slot(nl.idx + gslot<G>(nl, i, c + G));
-            one(e0);
-            one(e1);
+        for (int t = 0; t < n; t += 4) {
+            const int4 qn = t + 4 < n ? ld_slots4(col + ((size_t)(t + 4) << 5)) : q;
+            one(q.x);
+            if (t + 1 < n) one(q.y);
+            if (t + 2 < n) one(q.z);
+            if (t + 3 < n) one(q.w);
+            q = qn;
         }
-        if (c < cnt) one(ld_slot(nl.idx + gslot<G>(nl, i, c)));
         return;
     }
     const unsigned key = keys[i];
@@ -372,7 +384,7 @@ cudaError_t launch_nbr_build_groups(const KParamsT<typename P::T>& k,
                                     unsigned* err, cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
     // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % k.lanes != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
+    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
     return with_group(k.lanes, [&](auto tag) {
         constexpr int G = decltype(tag)::value;
         k_nbr_build_g<P, G><<<group_blocks(k.n, k.threads), k.threads, 0, s>>>(
@@ -388,7 +400,7 @@ cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
                                 const Pass1OutT<typename P::T>& out, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % k.lanes != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
+    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
     return with_group(k.lanes, [&](auto tag) {
         constexpr int G = decltype(tag)::value;
         k_pass1_g<P, G><<<group_blocks(k.n, k.threads), k.threads, 0, s>>>(k, in, keys, cs, nl,
@@ -406,7 +418,7 @@ cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
                                 unsigned* err, unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
     // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % k.lanes != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
+    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
     return with_group(k.lanes, [&](auto tag) {
         constexpr int G = decltype(tag)::value;
         const int blocks = group_blocks(k.n, k.threads);

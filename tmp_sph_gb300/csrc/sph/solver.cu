@@ -510,8 +510,11 @@ cudaError_t alloc_list(sph_ctx* c) {
     // pair mode keeps one union list per two particles (also used per particle by sph_ns, so
     // the rows still cover every particle)
     const bool pairs = c->opt_pairs != 0;
-    const int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
-                                       : nbr_capacity_for(c->P, c->skin, pairs);
+    int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
+                                 : nbr_capacity_for(c->P, c->skin, pairs);
+    // lane groups keep each lane's entries four to an int4: whole int4 rows per lane
+    const int unit = std::max(16, 4 * c->opt_lanes);
+    cap = (cap + unit - 1) / unit * unit;
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
     free_list(c->nl);
     // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
@@ -665,6 +668,10 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             if (value == c->opt_lanes) return SPH_OK;
             c->opt_lanes = value;
             drop_graph(c);
+            if (alloc_list(c) != cudaSuccess) {
+                cudaGetLastError();
+                return SPH_ERR_NOMEM;
+            }
             break;  // the list layout changed: rebuild
         case SPH_OPT_PAIRS:
             c->opt_pairs = value != 0;

@@ -224,7 +224,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def config_block(args, p, n):
+def set_lanes(sol, args) -> None:
+    """Lanes per particle of the two list passes: --lanes for both, else --pass1-lanes (0: the
+    precision's default) and --pass2-lanes."""
+    from tmp_sph_gb300 import api
+    if args.lanes is not None:
+        sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+    else:
+        sol.set_option(api.SPH_OPT_PASS1_LANES, args.pass1_lanes)
+        sol.set_option(api.SPH_OPT_PASS2_LANES, args.pass2_lanes)
+
+
+def lanes_in_effect(sol) -> list:
+    from tmp_sph_gb300 import api
+    return [sol.get_option(api.SPH_OPT_PASS1_LANES), sol.get_option(api.SPH_OPT_PASS2_LANES)]
+
+
+def config_block(args, p, n, lanes=None):
     return {"workload": f"dam_break_{args.case}_{getattr(args, 'precision', 'fp32')}", "particles": n,
             "fluid_particles": n - p.num_boundary, "dx_m": p.dx, "h_over_dx": 1.3,
             "cells": p.num_cells, "eos": "tait", "dt_s": p.dt,
@@ -232,7 +248,8 @@ def config_block(args, p, n):
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
             "graph_mode": args.graph_mode, "pairs": args.pairs,
-            "lanes_per_particle": args.lanes, "adaptive_skin": args.adaptive_skin}
+            "lanes_per_particle_pass1_pass2": lanes,
+            "adaptive_skin": args.adaptive_skin}
 
 
 def run_batch(args):
@@ -261,7 +278,7 @@ def run_batch(args):
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
-    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+    set_lanes(sol, args)
     sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
@@ -297,7 +314,8 @@ def run_batch(args):
                    "parallelism": f"instances x{ws} (independent batches, no collective)",
                    "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
                    "neighbour_list_skin_over_kh": args.skin / 1000.0,
-                   "graph_mode": args.graph_mode},
+                   "graph_mode": args.graph_mode,
+                   "lanes_per_particle_pass1_pass2": lanes_in_effect(sol)},
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps},
         "autotune": autotune.summary(tuned) if tuned else None,
         "gpu_launches": count_launches(sol_cells_batch(p, n_inst, args.skin), 2 * args.steps,
@@ -339,8 +357,12 @@ def main():
                          "autotuner first (overrides --skin)")
     ap.add_argument("--pairs", type=int, default=0, choices=[0, 1],
                     help="two particles per thread over a union neighbour list (FP32, FP64)")
-    ap.add_argument("--lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
-                    help="lanes per particle in the neighbour-list kernels")
+    ap.add_argument("--lanes", type=int, default=None, choices=[1, 2, 4, 8, 16],
+                    help="lanes per particle in both neighbour-list passes")
+    ap.add_argument("--pass1-lanes", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
+                    help="lanes per particle in list pass 1 (0: 2 in FP32, 1 otherwise)")
+    ap.add_argument("--pass2-lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
+                    help="lanes per particle in list pass 2")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
     ap.add_argument("--skin", type=int, default=100,
@@ -373,10 +395,11 @@ def main():
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
-    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+    set_lanes(sol, args)
     sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
+    lanes = lanes_in_effect(sol)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
 
     def barrier():
@@ -424,7 +447,7 @@ def main():
     def time_precision(precision: str, steps: int) -> dict:
         v = S.Solver(p, n, precision=precision)
         v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
-        v.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
+        set_lanes(v, args)
         v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
         v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         v.step(3, stream=stream)
@@ -505,7 +528,7 @@ def main():
         "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
                   "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
-        "config": config_block(args, p, n),
+        "config": config_block(args, p, n, lanes),
         "hbm_gbs_algorithmic": value / ws * b_alg / 1e9,
         "hbm_frac_step_algorithmic": value / ws * b_alg / 1e9 / hbm_peak,
         "bytes_per_particle_step": b_alg,

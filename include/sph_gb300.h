@@ -263,9 +263,15 @@ typedef struct sph_ctx sph_ctx;
                              lists, between 0.02 and SPH_OPT_SKIN_PERMILLE, from how long the
                              last lists lasted (tight lists for slow flow, wide for fast); 0: the
                              lists always use SPH_OPT_SKIN_PERMILLE */
-#define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in the list kernels:
+#define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in both list passes:
                              1 (one thread per particle), 2, 4, 8 or 16 (a group of lanes shares a
-                             particle's list and reduces its sums; not with SPH_OPT_PAIRS) */
+                             particle's list and reduces its sums; not with SPH_OPT_PAIRS); 0:
+                             the defaults below.  With groups in either pass the lists store
+                             their 16-entry windows transposed (a change rebuilds them) */
+#define SPH_OPT_PASS1_LANES 14  /* the same for list pass 1 (density sums) alone; default (0):
+                             2 in FP32 and mixed precision with a list skin, else 1 */
+#define SPH_OPT_PASS2_LANES 15  /* the same for list pass 2 (forces + integrator) alone;
+                             default 1 */
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */
@@ -288,6 +294,10 @@ int sph_destroy(sph_ctx* ctx);
 int sph_set_params(sph_ctx* ctx, const sph_params* p);
 int sph_get_params(const sph_ctx* ctx, sph_params* out);
 int sph_ctx_set_option(sph_ctx* ctx, int option, int value);
+/* The value an option has in effect (a default resolved: SPH_OPT_PASS1_LANES and
+ * SPH_OPT_LANES_PER_PARTICLE give pass 1's lanes for the context's precision;
+ * SPH_OPT_SKIN_PERMILLE the largest skin). */
+int sph_ctx_get_option(const sph_ctx* ctx, int option, int* value);
 
 /* SPH_NS_simpleversion (src/header/ns.cuh:4, src/equation/ns.cu:5-131 and :134-249): both
  * neighbour passes on sorted AoS arrays.  Writes dofv, rho_dt, vel_dt (AoS) and, for boundary

@@ -11,9 +11,9 @@ def test_autotune_small_case(sphlib, cuda, report):
     import torch
     from tmp_sph_gb300 import autotune, cases, solver as S
     st, p = cases.build("small", physics="config", dx=0.02)
-    best = autotune.tune(p, st, threads=(64, 128), ppt=(1, 2), skins=(0, 100), lanes=(1, 8))
-    # ppt varies with one lane per particle only: 2 x 2 x 2 + 2 x 2 candidates
-    assert len(best["table"]) == 12
+    best = autotune.tune(p, st, threads=(64, 128), ppt=(1, 2), skins=(0, 100), lanes=(1, 2))
+    # every combination: 2 x 2 x 2 x 2 candidates
+    assert len(best["table"]) == 16
     assert all(m["flags"] == 0 for m in best["table"])
     assert all(m["pass_ms_per_half_step"] > 0 and m["rebuild_ms"] > 0 for m in best["table"])
     # skin 0 rebuilds every half step of the profiled steps

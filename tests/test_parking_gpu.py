@@ -92,7 +92,8 @@ def test_escaped_particles_other_precisions(sphlib, oracle, cuda, report, precis
 
 def test_inactive_particles_without_skin_or_list(sphlib, cuda):
     """Rebuilding every half step, and walking the cells without a list, give the same bits
-    as each other with particles outside the search (the list and the walk skip them alike)."""
+    as each other with particles outside the search (the one-lane list passes and the walk
+    skip them alike)."""
     from tmp_sph_gb300 import api
     import torch
     from tmp_sph_gb300 import solver as S
@@ -103,6 +104,7 @@ def test_inactive_particles_without_skin_or_list(sphlib, cuda):
         with S.Solver(p, len(st["rho"])) as sol:
             sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
             sol.set_option(api.SPH_OPT_NEIGHBOR_LIST, use_list)
+            sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, 1)
             sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
             sol.step(3, stream=s)
             outs.append(sol.download(stream=s))

@@ -88,14 +88,16 @@ def test_fp32_and_mixed_against_fp64(sphlib, cuda, report):
 
 
 def test_mixed_list_matches_cell_walk(sphlib, cuda):
-    """Mixed precision: list passes and walking passes (cell codes from the walk) agree bit
-    for bit; an overflowing list falls back to the same walk."""
+    """Mixed precision: one-lane list passes and walking passes (cell codes from the walk)
+    agree bit for bit; an overflowing list falls back to the same walk."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    a = run_prec(st, p, 5, "mixed", {api.SPH_OPT_SKIN_PERMILLE: 0})
-    b = run_prec(st, p, 5, "mixed", {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 0})
-    c = run_prec(st, p, 5, "mixed", {api.SPH_OPT_NEIGHBOR_CAP: 8})
-    d = run_prec(st, p, 5, "mixed")
+    one = {api.SPH_OPT_LANES_PER_PARTICLE: 1}
+    a = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_SKIN_PERMILLE: 0})
+    b = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_SKIN_PERMILLE: 0,
+                                     api.SPH_OPT_NEIGHBOR_LIST: 0})
+    c = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_NEIGHBOR_CAP: 8})
+    d = run_prec(st, p, 5, "mixed", one)
     assert a["flags"] == 0 and b["flags"] == 0 and d["flags"] == 0
     assert c["flags"] & api.SPH_FLAG_NEIGHBOR_OVERFLOW
     for k in ("pos", "vel", "rho", "p"):

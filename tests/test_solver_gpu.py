@@ -106,11 +106,13 @@ def run_opts(st, p, nsteps, opts):
 
 
 def test_neighbor_list_matches_cell_walk(sphlib, cuda):
-    """Without a skin the list is rebuilt every half step and the list passes visit the same
-    pairs in the same order as passes that walk the cells themselves: bit-identical steps."""
+    """Without a skin the list is rebuilt every half step and the one-lane list passes visit
+    the same pairs in the same order as passes that walk the cells themselves: bit-identical
+    steps."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    a, fa = run_opts(st, p, 5, {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 1})
+    a, fa = run_opts(st, p, 5, {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 1,
+                                api.SPH_OPT_LANES_PER_PARTICLE: 1})
     b, fb = run_opts(st, p, 5, {api.SPH_OPT_SKIN_PERMILLE: 0, api.SPH_OPT_NEIGHBOR_LIST: 0})
     assert fa == 0 and fb == 0
     for k in ("pos", "vel", "rho", "p"):
@@ -119,12 +121,14 @@ def test_neighbor_list_matches_cell_walk(sphlib, cuda):
 
 def test_neighbor_list_overflow_falls_back(sphlib, cuda):
     """With a 16-slot list every fluid particle overflows: it is flagged and walks its cells,
-    giving the same result."""
+    giving the same result as the one-lane list passes."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    one = {api.SPH_OPT_LANES_PER_PARTICLE: 1}
     for skin in (0, 100):
-        a, fa = run_opts(st, p, 3, {api.SPH_OPT_SKIN_PERMILLE: skin, api.SPH_OPT_NEIGHBOR_CAP: 8})
-        b, fb = run_opts(st, p, 3, {api.SPH_OPT_SKIN_PERMILLE: skin})
+        a, fa = run_opts(st, p, 3, {**one, api.SPH_OPT_SKIN_PERMILLE: skin,
+                                    api.SPH_OPT_NEIGHBOR_CAP: 8})
+        b, fb = run_opts(st, p, 3, {**one, api.SPH_OPT_SKIN_PERMILLE: skin})
         assert fa & api.SPH_FLAG_NEIGHBOR_OVERFLOW and fb == 0
         for k in ("pos", "vel", "rho", "p"):
             assert np.array_equal(a[k], b[k]), (skin, k)
@@ -419,7 +423,8 @@ def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):
     fl = st["type"] == 1
     st["vel"][fl] = np.array([1.0, 0.0, 0.0], np.float32)
     steps = 60
-    fixed = {api.SPH_OPT_SKIN_PERMILLE: 100, api.SPH_OPT_ADAPTIVE_SKIN: 0}
+    fixed = {api.SPH_OPT_SKIN_PERMILLE: 100, api.SPH_OPT_ADAPTIVE_SKIN: 0,
+             api.SPH_OPT_LANES_PER_PARTICLE: 1}  # list passes in walk order
     out, flags = run_opts(st, p, steps, fixed)
     skin = 0.1 * float(p.kh)
     per_build = skin / (1.0 * float(p.dt))  # steps a uniform 1 m/s carry takes to reach skin

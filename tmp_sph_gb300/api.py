@@ -45,6 +45,8 @@ SPH_OPT_BLOCK_THREADS = 9
 SPH_OPT_PARTICLES_PER_THREAD = 10
 SPH_OPT_PAIRS = 11
 SPH_OPT_LANES_PER_PARTICLE = 12
+SPH_OPT_PASS1_LANES = 14
+SPH_OPT_PASS2_LANES = 15
 SPH_OPT_ADAPTIVE_SKIN = 13
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
@@ -166,6 +168,7 @@ _PROTOS = {
     "sph_set_params": (_I, [_P, _PP]),
     "sph_get_params": (_I, [_P, _PP]),
     "sph_ctx_set_option": (_I, [_P, _I, _I]),
+    "sph_ctx_get_option": (_I, [_P, _I, _P]),
     "sph_ns": (_I, [_P] + [_P] * 9 + [_I] + [_P] * 4 + [_P]),
     "sph_upload": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_upload_instances": (_I, [_P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _P]),

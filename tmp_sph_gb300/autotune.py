@@ -1,8 +1,9 @@
 """Autotuner for the resident solver's launch shape and cell size.
 
-Picks, for one workload on the GPU at hand, the threads per block, particles per thread and
-lanes per particle of the neighbour kernels and the neighbour-list skin (which sets the cell
-size, kh (1 + skin)).
+Picks, for one workload on the GPU at hand, the threads per block and particles per thread of
+the neighbour kernels, the lanes per particle of list pass 1 (pass 2 keeps one: lane groups
+made it slower at every G measured) and the neighbour-list skin (which sets the cell size,
+kh (1 + skin)).
 It loads the workload once; for every candidate it forces one list rebuild, runs two profiled
 steps and reads the per-phase device time (SPH_OPT_PROFILE): the cost of a rebuild (sort,
 gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The step
@@ -30,7 +31,7 @@ from . import solver as S
 
 THREADS = (64, 128, 256)
 PPT = (1, 2, 4)
-LANES = (1, 4, 8)
+LANES = (1, 2, 4)
 SKINS = (0, 50, 100, 150, 200, 300)
 
 # profile phases: 0 sort, 1 gather + cell starts, 2 list build, 3 pass 1, 4 pass 2
@@ -61,7 +62,8 @@ def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> d
     steps (setting the skin forces the next half step to rebuild; the state advances)."""
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
-    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, lanes)
+    sol.set_option(api.SPH_OPT_PASS1_LANES, lanes)
+    sol.set_option(api.SPH_OPT_PASS2_LANES, 1)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
     sol.step(1, stream=stream)  # warm: first launches of this shape
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
@@ -87,13 +89,9 @@ def step_cost(m: dict, p, v: float) -> float:
 
 
 def candidates(threads=THREADS, ppt=PPT, skins=SKINS, lanes=LANES) -> list[tuple]:
-    """(threads, ppt, lanes, skin) to measure: particles per thread only vary with one lane per
-    particle (the lane-group kernels take one particle per group)."""
-    out = []
-    for t, g, s in itertools.product(threads, lanes, skins):
-        for k in (ppt if g == 1 else (1,)):
-            out.append((t, k, g, s))
-    return out
+    """(threads, ppt, pass-1 lanes, skin) to measure: every combination (particles per thread
+    apply to pass 2 and the list build whatever pass 1's lanes)."""
+    return [(t, k, g, s) for t, k, g, s in itertools.product(threads, ppt, lanes, skins)]
 
 
 def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=SKINS,
@@ -117,7 +115,7 @@ def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=
     ok = [m for m in table if m["flags"] == 0] or table
     best = min(ok, key=lambda m: m["step_ms_estimate"])
     return {"threads": best["threads"], "ppt": best["ppt"], "lanes": best["lanes"],
-            "skin_permille": best["skin_permille"], "speed_m_s": v,
+            "skin_permille": best["skin_permille"], "speed_m_s": v, "precision": precision,
             "step_ms_estimate": best["step_ms_estimate"], "table": table}
 
 
@@ -125,16 +123,18 @@ def apply(sol, best: dict) -> None:
     """Set a tuned choice on a solver (before its upload)."""
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, best["threads"])
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, best["ppt"])
-    sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, best.get("lanes", 1))
+    sol.set_option(api.SPH_OPT_PASS1_LANES, best.get("lanes", 0))
+    sol.set_option(api.SPH_OPT_PASS2_LANES, 1)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, best["skin_permille"])
 
 
 def summary(best: dict) -> dict:
     """The choice without the table, plus the estimate of the default (128 threads, one
-    particle per thread and lane, skin 0.1 kh)."""
+    particle per thread, pass-1 lanes 2 in FP32 and 1 otherwise, skin 0.1 kh)."""
     out = {k: v for k, v in best.items() if k != "table"}
+    lanes = 2 if best.get("precision", "fp32") == "fp32" else 1
     for m in best["table"]:
-        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == (128, 1, 1, 100):
+        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == (128, 1, lanes, 100):
             out["default_step_ms_estimate"] = m["step_ms_estimate"]
     return out
 

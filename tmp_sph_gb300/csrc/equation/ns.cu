@@ -53,39 +53,32 @@
 // adh(-2 t^3 (2q+1) + 2 t^4) r/(h|r|) after factoring.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "ns_pair.cuh"
 #include "sph_internal.h"
 
 namespace sph {
 
 namespace {
-// Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
-// col + 32 * 4g (col = the warp's block + 4 * lane).  The 32 particles of a warp share one block
-// of cap x 32 slots, so a warp reading slot group g of all its lanes touches four consecutive
-// lines (512 bytes) with one 16-byte load per lane, and the build stores four slots at a time.
-__device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
-    return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + ((size_t)(i & 31) << 2);
-}
+// Appends slots to a list column.  Plain windows: four slots at a time (one 16-byte store per
+// four), the group being filled staged in the thread's 16 bytes of shared memory — one store
+// per slot at a computed address, where keeping it in registers took a select per register per
+// slot, and the walk's divergent hit path runs for nearly every candidate a warp tests (build
+// −6%).  Transposed windows: each slot stored at its place directly (4-byte stores; staging
+// the window's 16 slots in shared memory took L1 from the build's position reads and was no
+// faster).
+template <bool WIN>
+struct SlotWriter;
 
-// Four list slots.  The slots stream past once per pass, so they are read without allocating
-// in L1, which keeps L1 for the neighbour records (measured: passes 0.6% faster).
-__device__ __forceinline__ int4 ld_slots(const int* p) {
-    int4 v;
-    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
-        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-        : "l"(p));
-    return v;
-}
-
-// Appends slots to a list column four at a time (one 16-byte store per four slots).  The group
-// being filled is staged in the thread's 16 bytes of shared memory: one store per slot at a
-// computed address, where keeping it in registers took a select per register per slot — and
-// the walk's divergent hit path runs for nearly every candidate a warp tests (build −6%).
-struct SlotWriter {
+template <>
+struct SlotWriter<false> {
     int* __restrict__ col;
     int cap;
     int* buf;  // the thread's four staging slots (shared memory, 16-byte aligned)
     int cnt = 0;
+    __device__ __forceinline__ SlotWriter(int* c, int cp, int* stage)
+        : col(c), cap(cp), buf(stage) {}
     __device__ __forceinline__ void put(int v) {
         buf[cnt & 3] = v;
         cnt++;
@@ -101,12 +94,33 @@ struct SlotWriter {
     }
 };
 
+template <>
+struct SlotWriter<true> {
+    int* __restrict__ col;
+    int cap;
+    int cnt = 0;
+    __device__ __forceinline__ SlotWriter(int* c, int cp, int*) : col(c), cap(cp) {}
+    // entry e of window u goes to chunk 4u + (e mod 4), component (e / 4) mod 4; cap is a
+    // multiple of 16, so every window below cap fits
+    __device__ __forceinline__ void put(int v) {
+        if (cnt < cap)
+            col[((size_t)(((cnt >> 4) << 2) | (cnt & 3)) << 7) | (size_t)((cnt >> 2) & 3)] = v;
+        cnt++;
+    }
+    __device__ __forceinline__ void flush() {}
+};
+
+// List modes of the one-lane passes (template LIST): no list (cell walks), a list of plain
+// windows, or one of transposed windows (KParams::list_win).  The mode is a template
+// parameter: a runtime choice between the two loops cost pass 2 1%.
+enum { LIST_NONE = 0, LIST_PLAIN = 1, LIST_WIN = 2 };
+
 // Neighbours of i (r2 < kh2) with their records R[2j], R[2j+1]: from the list (one record
 // load per listed pair, the next slot loaded one pair ahead; pairs in the skin beyond the
 // support radius are skipped), or by walking the cells over X[XSTRIDE * j] when i overflowed
 // the list.  f(j, a, b, dx, dy, dz, r2).  (Skipping the gathers of slots in the skin with a
 // pass-1 hit mask cost pass 2 more in instructions than it saved in sectors.)
-template <class P, bool LIST, int XSTRIDE, class F>
+template <class P, int LIST, int XSTRIDE, class F>
 __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
                                               const int* __restrict__ cs,
                                               const unsigned* __restrict__ keys,
@@ -116,10 +130,9 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
                                               const vec4_t<typename P::T>& pi, F&& f) {
     using T = typename P::T;
     using V = vec4_t<T>;
-    if (LIST) {
+    if constexpr (LIST != LIST_NONE) {
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
-            const int* __restrict__ col = nl.idx + nbr_col(nl, i);
             auto one = [&](int e) {
                 const int j = P::kMixed ? (int)((unsigned)e & IDX_MASK) : e;
                 V a, b;
@@ -129,17 +142,7 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
                 const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
             };
-            int4 q = cnt > 0 ? ld_slots(col) : make_int4(0, 0, 0, 0);
-#pragma unroll 1
-            for (int c = 0; c < cnt; c += 4) {
-                // the next group is loaded one group ahead
-                const int4 qn = c + 4 < cnt ? ld_slots(col + ((size_t)(c + 4) << 5)) : q;
-                one(q.x);
-                if (c + 1 < cnt) one(q.y);
-                if (c + 2 < cnt) one(q.z);
-                if (c + 3 < cnt) one(q.w);
-                q = qn;
-            }
+            for_each_slot<LIST == LIST_WIN>(nl.idx + nbr_col(nl, i), cnt, 0, 1, one);
             return;
         }
     }
@@ -155,7 +158,7 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
 // needs), every fluid particle all of them; with walls_all, boundary particles keep all.
 // Slots are warp-interleaved (nbr_col): the passes read them coalesced, the build writes them
 // scattered within its warp's block, which L2 merges before they reach HBM.
-template <class P>
+template <class P, bool WIN>
 __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
                                               const vec4_t<typename P::T>* __restrict__ X,
                                               const unsigned* __restrict__ keys,
@@ -181,7 +184,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
             return;
         }
     }
-    SlotWriter w{nl.idx + nbr_col(nl, i), nl.cap, stage};
+    SlotWriter<WIN> w(nl.idx + nbr_col(nl, i), nl.cap, stage);
     const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
@@ -193,24 +196,24 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     raise_flags(err, w.cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
 }
 
-template <class P, bool GS>
+template <class P, bool GS, bool WIN>
 __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
             const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
             int walls_all, unsigned* err, const unsigned* gate) {
-    __shared__ int4 s_stage[NS_MAX_THREADS];
+    __shared__ int4 s_stage[WIN ? 1 : NS_MAX_THREADS];
     if (gated_off(gate)) return;
-    int* stage = reinterpret_cast<int*>(&s_stage[threadIdx.x]);
+    int* stage = reinterpret_cast<int*>(&s_stage[WIN ? 0 : threadIdx.x]);
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
-            nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, stage, i);
+            nbr_build_one<P, WIN>(k, X, keys, cs, nl, walls_all, err, stage, i);
     } else if (i0 < k.n) {
-        nbr_build_one<P>(k, X, keys, cs, nl, walls_all, err, stage, i0);
+        nbr_build_one<P, WIN>(k, X, keys, cs, nl, walls_all, err, stage, i0);
     }
 }
 
-template <class P, bool WRITE_SUMS, bool LIST>
+template <class P, bool WRITE_SUMS, int LIST>
 __device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
                                           const ParticleSetT<typename P::T>& in,
                                           const unsigned* __restrict__ keys,
@@ -229,7 +232,7 @@ __device__ __forceinline__ void pass1_one(const KParamsT<typename P::T>& k,
     acc.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i);
 }
 
-template <class P, bool WRITE_SUMS, bool LIST, bool GS>
+template <class P, bool WRITE_SUMS, int LIST, bool GS>
 __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
@@ -242,7 +245,7 @@ k_pass1(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         pass1_one<P, WRITE_SUMS, LIST>(k, in, keys, cs, nl, out, rhop_sum, w_sum, i0);
     }
 }
-template <class P, int MODE, bool LIST>
+template <class P, int MODE, int LIST>
 __device__ __forceinline__ void pass2_one(const KParamsT<typename P::T>& k, int i,
                                           const ParticleSetT<typename P::T>& in,
                                           const unsigned* __restrict__ keys,
@@ -266,7 +269,7 @@ __device__ __forceinline__ void pass2_one(const KParamsT<typename P::T>& k, int 
 }
 
 
-template <class P, int MODE, bool LIST, bool GS>
+template <class P, int MODE, int LIST, bool GS>
 __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
@@ -292,7 +295,7 @@ k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
 // The same kernel held to CAP registers (one particle per thread): the FP32 step kernel fits
 // in 48 with an 8-byte stack frame, keeping ten 128-thread blocks resident per SM where the
 // unconstrained 53 keeps nine; the mixed-precision one in 56 (nine blocks instead of eight).
-template <class P, int MODE, bool LIST, bool GS, int CAP>
+template <class P, int MODE, int LIST, bool GS, int CAP>
 __global__ void __maxnreg__(CAP)
 k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
         const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
@@ -349,7 +352,7 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
     }
     const bool keep0 = fluid_rec(p0.w) || walls_all;
     const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
-    SlotWriter w{nl.idx + nbr_col(nl, c), nl.cap, stage};
+    SlotWriter<false> w(nl.idx + nbr_col(nl, c), nl.cap, stage);
     const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     auto visit = [&](int j) {
         const V pj = ld_pos(X, (size_t)j);
@@ -400,22 +403,11 @@ __device__ __forceinline__ bool visit_union(const NbrList& nl,
     using V = vec4_t<typename P::T>;
     const int cnt = __ldg(nl.count + c);
     if (cnt > nl.cap) return false;
-    const int* __restrict__ col = nl.idx + nbr_col(nl, c);
-    auto one = [&](int j) {
+    for_each_slot<false>(nl.idx + nbr_col(nl, c), cnt, 0, 1, [&](int j) {
         V a, b;
         ld_rec(R, j, a, b);
         f(j, a, b);
-    };
-    int4 q = cnt > 0 ? ld_slots(col) : make_int4(0, 0, 0, 0);
-#pragma unroll 1
-    for (int e = 0; e < cnt; e += 4) {
-        const int4 qn = e + 4 < cnt ? ld_slots(col + ((size_t)(e + 4) << 5)) : q;
-        one(q.x);
-        if (e + 1 < cnt) one(q.y);
-        if (e + 2 < cnt) one(q.z);
-        if (e + 3 < cnt) one(q.w);
-        q = qn;
-    }
+    });
     return true;
 }
 
@@ -447,12 +439,12 @@ __device__ __forceinline__ void pass1_pair(const KParamsT<typename P::T>& k,
         if (use1) one(a1, i1, j, a, b);
     });
     if (!listed) {
-        visit_records<P, false, 1>(k, cs, keys, nl, in.xyz, in.rec, i0, a0.pi,
+        visit_records<P, LIST_NONE, 1>(k, cs, keys, nl, in.xyz, in.rec, i0, a0.pi,
                                    [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
             a0.pair(k, aj, vj, dx, dy, dz, r2);
         });
         if (has1)
-            visit_records<P, false, 1>(k, cs, keys, nl, in.xyz, in.rec, i1, a1.pi,
+            visit_records<P, LIST_NONE, 1>(k, cs, keys, nl, in.xyz, in.rec, i1, a1.pi,
                                        [&](int, const V& aj, const V& vj, T dx, T dy, T dz,
                                            T r2) { a1.pair(k, aj, vj, dx, dy, dz, r2); });
     }
@@ -493,11 +485,11 @@ __device__ __forceinline__ void pass2_pair(const KParamsT<typename P::T>& k, int
         });
         if (!listed) {
             if (a0.active)
-                visit_records<P, false, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i0, a0.pi,
+                visit_records<P, LIST_NONE, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i0, a0.pi,
                                            [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
                                                T r2) { a0.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
             if (act1)
-                visit_records<P, false, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i1, a1.pi,
+                visit_records<P, LIST_NONE, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i1, a1.pi,
                                            [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
                                                T r2) { a1.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
         }
@@ -567,7 +559,7 @@ inline dim3 ns_grid(const KP& k) {
     return dim3((unsigned)(b > 0 ? b : 1));
 }
 
-template <class P, bool LIST, bool GS>
+template <class P, int LIST, bool GS>
 void pass1_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
                      const unsigned* keys, const int* cs, const NbrList& nl,
                      const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
@@ -584,12 +576,12 @@ void pass1_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typena
                                                         nullptr);
 }
 
-template <class P, bool LIST>
+template <class P, int LIST>
 void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename P::T>& in,
                   const unsigned* keys, const int* cs, const NbrList& nl,
                   const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
-    if constexpr (LIST && !P::kMixed) {
+    if constexpr (LIST == LIST_PLAIN && !P::kMixed) {  // pair lists keep plain windows
         if (k.pairs) {
             if (rhop_sum && w_sum && P::kId == SPH_PREC_FP32)
                 k_pass1_pairs<P, true><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
@@ -613,22 +605,32 @@ void pass2_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typena
                      int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                      unsigned* err, unsigned* disp, cudaStream_t s) {
     const dim3 b = ns_grid(k);
-    if constexpr (MODE != MODE_RATES && !GS && (P::kId == SPH_PREC_FP32 || P::kMixed)) {
-        constexpr int cap = P::kId == SPH_PREC_FP32 ? 48 : 56;
-        if (nl) {
-            k_pass2_cap<P, MODE, true, GS, cap><<<b, k.threads, 0, s>>>(
+    if (!nl) {
+        k_pass2<P, MODE, LIST_NONE, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, NbrList{}, p1,
+                                                                 rho_dt, vel_dt, wall_rates, out,
+                                                                 out_hash, err, nullptr);
+        return;
+    }
+    auto with_list = [&](auto mode) {
+        constexpr int L = decltype(mode)::value;
+        if constexpr (MODE != MODE_RATES && !GS && (P::kId == SPH_PREC_FP32 || P::kMixed)) {
+            constexpr int cap = P::kId == SPH_PREC_FP32 ? 48 : 56;
+            k_pass2_cap<P, MODE, L, GS, cap><<<b, k.threads, 0, s>>>(
                 k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
+        } else {
+            k_pass2<P, MODE, L, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt,
+                                                             vel_dt, wall_rates, out, out_hash,
+                                                             err, disp);
+        }
+    };
+    // the rates (sph_ns) run on the drop-in's own list, which has plain windows
+    if constexpr (MODE != MODE_RATES) {
+        if (k.list_win) {
+            with_list(std::integral_constant<int, LIST_WIN>{});
             return;
         }
     }
-    if (nl)
-        k_pass2<P, MODE, true, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, *nl, p1, rho_dt,
-                                                            vel_dt, wall_rates, out, out_hash,
-                                                            err, disp);
-    else
-        k_pass2<P, MODE, false, GS><<<b, k.threads, 0, s>>>(k, in, keys, cs, NbrList{}, p1,
-                                                             rho_dt, vel_dt, wall_rates, out,
-                                                             out_hash, err, nullptr);
+    with_list(std::integral_constant<int, LIST_PLAIN>{});
 }
 
 template <class P, int MODE>
@@ -670,7 +672,6 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    if (k.lanes > 1) return launch_nbr_build_groups<P>(k, in, keys, cs, nl, walls_all, err, s, gate);
     if constexpr (!P::kMixed) {
         if (k.pairs) {
             k_nbr_build_pairs<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
@@ -678,12 +679,22 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
             return cudaGetLastError();
         }
     }
-    if (k.ppt > 1)
-        k_nbr_build<P, true><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl, walls_all,
-                                                              err, gate);
-    else
-        k_nbr_build<P, false><<<ns_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                               walls_all, err, gate);
+    const dim3 g = ns_grid(k);
+    if (k.ppt > 1) {
+        if (k.list_win)
+            k_nbr_build<P, true, true><<<g, k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                walls_all, err, gate);
+        else
+            k_nbr_build<P, true, false><<<g, k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                 walls_all, err, gate);
+    } else {
+        if (k.list_win)
+            k_nbr_build<P, false, true><<<g, k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                 walls_all, err, gate);
+        else
+            k_nbr_build<P, false, false><<<g, k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
+                                                                  walls_all, err, gate);
+    }
     return cudaGetLastError();
 }
 
@@ -695,10 +706,12 @@ cudaError_t launch_pass1(const KParamsT<typename P::T>& k, const ParticleSetT<ty
     if (k.n <= 0) return cudaSuccess;
     if (nl && k.lanes > 1 && !rhop_sum && !w_sum)
         return launch_pass1_groups<P>(k, in, keys, cs, *nl, out, s);
-    if (nl)
-        pass1_launch<P, true>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
+    if (nl && k.list_win)
+        pass1_launch<P, LIST_WIN>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
+    else if (nl)
+        pass1_launch<P, LIST_PLAIN>(k, in, keys, cs, *nl, out, rhop_sum, w_sum, s);
     else
-        pass1_launch<P, false>(k, in, keys, cs, NbrList{}, out, rhop_sum, w_sum, s);
+        pass1_launch<P, LIST_NONE>(k, in, keys, cs, NbrList{}, out, rhop_sum, w_sum, s);
     return cudaGetLastError();
 }
 
@@ -719,7 +732,7 @@ cudaError_t launch_pass2_step(const KParamsT<typename P::T>& k, HalfStep half,
                               ParticleSetT<typename P::T> out, unsigned* out_hash, unsigned* err,
                               unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    if (nl && k.lanes > 1)
+    if (nl && k.lanes2 > 1)
         return launch_pass2_groups<P>(k, half, in, keys, cs, *nl, p1, out, out_hash, err, disp, s);
     if (half == HALF_PREDICT)
         pass2_launch<P, MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash,

@@ -4,22 +4,22 @@
 // computeGovering_equationD, src/equation/ns.cu:30-249), same list contents, different
 // assignment of work to lanes.  With one thread per particle every lane of a warp gathers a
 // different neighbour record, and a warp-level gather touches about twenty distinct 128-byte
-// lines: the passes are limited by L1 data-stage wavefronts.  With G lanes per particle, lane s
-// of particle i handles its list entries s, s + G, s + 2G, ...: the G records a group gathers
-// in one step are consecutive entries of one list — runs of nearby slots of a few cell strips —
-// and the 32/G particles of a warp are neighbours in the sorted order with largely the same
-// lists.  A model of the 765,828-particle case on the host counts 0.70 distinct lines per
-// gathered pair with one lane per particle and 0.34 with eight.
+// lines: the passes are limited by L1 data-stage wavefronts.  With G lanes per particle the G
+// records a group gathers in one step are entries of one list a few slots apart — nearby slots
+// of a few cell strips — and the 32/G particles of a warp are neighbours in the sorted order
+// with largely the same lists; a warp also runs its loop for the longest list of 32/G
+// particles rather than of 32.
 //
 // Sums.  Each lane accumulates its share of the pairs; a group reduces them with xor shuffles
 // in a fixed tree, so results are deterministic and independent of the launch shape, but not
 // bit-equal to one lane per particle (the sums associate differently).
 //
-// List layout.  The 32/G particles a warp handles together share a block of cap * 32/G slots
-// in which each lane's entries come four to an int4 (gslot): a warp reads four entries of
-// every lane with one 16-byte load per lane.  The build walks the cells with the whole group, G candidates per step,
-// and compacts the hits with a ballot, so the list holds the same entries in the same (walk)
-// order as the one-lane build.
+// List layout.  The groups read the one-lane list with transposed windows (ns_pair.cuh):
+// lane s of a group takes int4 chunks s, s + G, s + 2G, ... of its particle's column, so at
+// every step the group gathers G consecutive entries.  With G = 4 the 8 particles of a warp read
+// 8 consecutive int4s of each of four chunk rows — four whole lines per request, as the
+// one-lane passes do.  The list build is the one-lane build with another slot order, and each
+// pass picks its own G.
 //
 // Blocks.  A block of T threads owns T consecutive particles and visits them in G rounds of T/G
 // particles (one group each), parking the reduced sums in shared memory; then every thread
@@ -40,39 +40,6 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 template <int G>
 __device__ __forceinline__ int sub_lane() {
     return (int)(threadIdx.x & (unsigned)(G - 1));
-}
-
-// This group's bits of a warp ballot, in sub-lane order.
-template <int G>
-__device__ __forceinline__ unsigned group_bits(unsigned ballot) {
-    if constexpr (G == 32) {
-        return ballot;
-    } else {
-        return (ballot >> ((threadIdx.x & 31u) & ~(unsigned)(G - 1))) & ((1u << G) - 1u);
-    }
-}
-
-// Entry c of particle i in the group layout.  The 32/G particles a warp handles together
-// share a block of cap * 32/G slots; lane L = (i mod 32/G) G + c mod G of the warp holds
-// entries c = s, s + G, s + 2G, ... of its particle, and its entries 4m .. 4m+3 (in that
-// order) are one int4 at block + 128 m + 4 L: a warp reads four entries of every lane with
-// one 16-byte load per lane, as the one-lane layout does.
-template <int G>
-__device__ __forceinline__ size_t gslot(const NbrList& nl, int i, int c) {
-    constexpr unsigned PPW = 32 / G;
-    const unsigned ui = (unsigned)i, uc = (unsigned)c;
-    const unsigned lane = (ui % PPW) * G + uc % G, t = uc / G;
-    return (size_t)(ui / PPW) * ((size_t)nl.cap * PPW) + (size_t)(t >> 2) * 128u +
-           (size_t)(lane * 4u + (t & 3u));
-}
-
-// Four list slots, read past L1 (the slots stream through once per pass).
-__device__ __forceinline__ int4 ld_slots4(const int* p) {
-    int4 v;
-    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
-        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-        : "l"(p));
-    return v;
 }
 
 // Sum a Sum<> over the G lanes of the group (all lanes of the warp take part).
@@ -129,76 +96,9 @@ __device__ __forceinline__ unsigned strip_code(const Strip& st, int t, int cx, i
     return (unsigned)(((t / 3) << 4) | ((t % 3) << 2) | (xc - cx + 1));
 }
 
-// ---------------------------------------------------------------- list build
-template <class P, int G>
-__device__ __forceinline__ void build_group(const KParamsT<typename P::T>& k,
-                                            const vec4_t<typename P::T>* __restrict__ X,
-                                            const unsigned* __restrict__ keys,
-                                            const int* __restrict__ cs, const NbrList& nl,
-                                            int walls_all, unsigned* err, int i) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    const int s = sub_lane<G>();
-    const bool valid = i < k.n;
-    const V pi = valid ? X[i] : make4<T>(T(0), T(0), T(0), T(0));
-    const unsigned key = valid ? keys[i] : (unsigned)k.num_cells;
-    // particles outside the neighbour search (park_inactive) take no candidates
-    const bool live = valid && !inactive_key(k, key);
-    if (valid && s == 0 && nl.xb) nl.xb[i] = as_float4(pi);
-    const bool keep_all = fluid_rec(pi.w) || walls_all;
-    int cx = 0, cy = 0, cz = 0;
-    if (live) cell_of_key(k.gx, k.gy, key, cx, cy, cz);
-    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
-    int cnt = 0;
-#pragma unroll 1
-    for (int t = 0; t < 9; t++) {
-        const Strip st = live ? strip_of<P::kMixed>(k, cs, cx, cy, cz, t) : Strip{};
-        // every lane of the warp runs the loop while any group has candidates left
-#pragma unroll 1
-        for (int jb = st.j0; __any_sync(FULL_MASK, jb < st.j1); jb += G) {
-            const int j = jb + s;
-            bool hit = false;
-            unsigned code = 0;
-            if (j < st.j1) {
-                const V pj = ld_pos(X, (size_t)j);
-                if constexpr (P::kMixed) code = strip_code(st, t, cx, j);
-                T dx, dy, dz;
-                rel_pos<P>(k, pi, pj, code, dx, dy, dz);
-                hit = dist2(dx, dy, dz) < cut2 && j != i && (keep_all || fluid_rec(pj.w));
-            }
-            const unsigned m = group_bits<G>(__ballot_sync(FULL_MASK, hit));
-            if (hit) {
-                const int c = cnt + __popc(m & ((1u << s) - 1u));
-                if (c < nl.cap)
-                    nl.idx[gslot<G>(nl, i, c)] =
-                        P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j;
-            }
-            cnt += __popc(m);
-        }
-    }
-    if (valid && s == 0) {
-        nl.count[i] = cnt;
-        raise_flags(err, cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
-    }
-}
-
-// A block of T threads builds the lists of T particles in G rounds of T/G groups.
-template <class P, int G>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_nbr_build_g(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
-              const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-              int walls_all, unsigned* err, const unsigned* gate) {
-    if (gated_off(gate)) return;
-    const int nt = (int)blockDim.x, base = (int)blockIdx.x * nt;
-#pragma unroll 1
-    for (int r = 0; r < G; r++)
-        build_group<P, G>(k, X, keys, cs, nl, walls_all, err,
-                          base + r * (nt / G) + (int)threadIdx.x / G);
-}
-
 // ---------------------------------------------------------------- neighbour visits
 // The group's share of particle i's neighbours (r2 < kh2) with their records: from the list,
-// lane s taking entries s, s + G, ... two at a time; or, when i overflowed the list, by walking
+// lane s taking chunks s, s + G, ... of four entries; or, when i overflowed the list, by walking
 // the cells over X[XSTRIDE * j], G candidates per step.  f(j, a, b, dx, dy, dz, r2).
 template <class P, int G, int XSTRIDE, class F>
 __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
@@ -222,20 +122,11 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
             const T r2 = dist2(dx, dy, dz);
             if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
         };
-        // this lane's entries s, s + G, ...: n of them, four per int4, the next int4 loaded
-        // one group ahead (four record gathers in flight per lane)
-        const int n = cnt > s ? (cnt - s + G - 1) / G : 0;
-        const int* __restrict__ col = nl.idx + gslot<G>(nl, i, s);
-        int4 q = n > 0 ? ld_slots4(col) : make_int4(0, 0, 0, 0);
-#pragma unroll 1
-        for (int t = 0; t < n; t += 4) {
-            const int4 qn = t + 4 < n ? ld_slots4(col + ((size_t)(t + 4) << 5)) : q;
-            one(q.x);
-            if (t + 1 < n) one(q.y);
-            if (t + 2 < n) one(q.z);
-            if (t + 3 < n) one(q.w);
-            q = qn;
-        }
+        // this lane's chunks s, s + G, ... (the group gathers G consecutive entries per step)
+        if (k.list_win)
+            for_each_slot<true>(nl.idx + nbr_col(nl, i), cnt, s, G, one);
+        else
+            for_each_slot<false>(nl.idx + nbr_col(nl, i), cnt, s, G, one);
         return;
     }
     const unsigned key = keys[i];
@@ -378,29 +269,13 @@ cudaError_t with_group(int lanes, F&& f) {
 }  // namespace
 
 template <class P>
-cudaError_t launch_nbr_build_groups(const KParamsT<typename P::T>& k,
-                                    const ParticleSetT<typename P::T>& in, const unsigned* keys,
-                                    const int* cs, const NbrList& nl, int walls_all,
-                                    unsigned* err, cudaStream_t s, const unsigned* gate) {
-    if (k.n <= 0) return cudaSuccess;
-    // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
-    return with_group(k.lanes, [&](auto tag) {
-        constexpr int G = decltype(tag)::value;
-        k_nbr_build_g<P, G><<<group_blocks(k.n, k.threads), k.threads, 0, s>>>(
-            k, in.xyz, keys, cs, nl, walls_all, err, gate);
-        return cudaGetLastError();
-    });
-}
-
-template <class P>
 cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
                                 const ParticleSetT<typename P::T>& in, const unsigned* keys,
                                 const int* cs, const NbrList& nl,
                                 const Pass1OutT<typename P::T>& out, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
+    // whole warps per block (each block's rounds split its warps into groups)
+    if (k.threads % 32 != 0) return cudaErrorInvalidValue;
     return with_group(k.lanes, [&](auto tag) {
         constexpr int G = decltype(tag)::value;
         k_pass1_g<P, G><<<group_blocks(k.n, k.threads), k.threads, 0, s>>>(k, in, keys, cs, nl,
@@ -417,9 +292,9 @@ cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
                                 ParticleSetT<typename P::T> out, unsigned* out_hash,
                                 unsigned* err, unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    // the layout needs whole steps of G entries and whole warps per block
-    if (nl.cap % (4 * k.lanes) != 0 || k.threads % 32 != 0) return cudaErrorInvalidValue;
-    return with_group(k.lanes, [&](auto tag) {
+    // whole warps per block (each block's rounds split its warps into groups)
+    if (k.threads % 32 != 0) return cudaErrorInvalidValue;
+    return with_group(k.lanes2, [&](auto tag) {
         constexpr int G = decltype(tag)::value;
         const int blocks = group_blocks(k.n, k.threads);
         if (half == HALF_PREDICT)
@@ -433,9 +308,6 @@ cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
 }
 
 #define SPH_NS_GROUPS_INSTANTIATE(P)                                                          \
-    template cudaError_t launch_nbr_build_groups<P>(                                          \
-        const KParamsT<P::T>&, const ParticleSetT<P::T>&, const unsigned*, const int*,        \
-        const NbrList&, int, unsigned*, cudaStream_t, const unsigned*);                       \
     template cudaError_t launch_pass1_groups<P>(const KParamsT<P::T>&,                        \
                                                 const ParticleSetT<P::T>&, const unsigned*,   \
                                                 const int*, const NbrList&,                   \

@@ -22,6 +22,62 @@ constexpr int NS_MAX_THREADS = 256;
 constexpr int CODE_SHIFT = 26;
 constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
 
+// Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
+// col + 32 * 4g (col = the warp's block + 4 * lane).  The 32 particles of a warp share one block
+// of cap x 32 slots, so a warp reading slot group g of all its lanes touches four consecutive
+// lines (512 bytes) with one 16-byte load per lane, and the build stores four slots at a time.
+__device__ __forceinline__ size_t nbr_col(const NbrList& nl, int i) {
+    return (size_t)(i >> 5) * ((size_t)nl.cap << 5) + ((size_t)(i & 31) << 2);
+}
+
+// Four list slots.  The slots stream past once per pass, so they are read without allocating
+// in L1, which keeps L1 for the neighbour records (measured: passes 0.6% faster).
+__device__ __forceinline__ int4 ld_slots(const int* p) {
+    int4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p));
+    return v;
+}
+
+// List windows.  A column is written in windows of 16 entries, four int4 chunks.  A plain
+// window keeps walk order (chunk a holds entries 4a .. 4a+3), so the one-lane passes sum in
+// the order a cell walk visits.  A transposed window (KParams::list_win, set while a pass runs
+// lane groups) holds entries a, a+4, a+8, a+12 in chunk a: the G lanes of a group, reading
+// chunks s, s + G, ..., then gather G consecutive entries — neighbouring records, a line or
+// two — side by side at every step.  (Reading plain windows that way had a group gathering
+// entries four apart: pass 1 at G = 4 took 1.03 ms against 0.79 with one lane; swapping
+// entries between the lanes of a pair with shuffles cost more than it saved, 0.83 at G = 2.)
+// First entry of chunk c; its four entries are st = 4 (transposed) or 1 (plain) apart.
+template <bool WIN>
+__device__ __forceinline__ int chunk_first(int c) {
+    return WIN ? c + 12 * (c >> 2) : c << 2;
+}
+
+// one(slot) for the entries of a column (cnt <= cap of them) in chunks c0, c0 + dc, ... (the
+// one-lane passes: c0 = 0, dc = 1; lane s of a group of G: c0 = s, dc = G), four to an int4,
+// the next chunk loaded one chunk ahead (four record gathers in flight per thread).  Chunk
+// firsts grow with c, so the first chunk past the count ends the column.
+template <bool WIN, class F>
+__device__ __forceinline__ void for_each_slot(const int* __restrict__ col, int cnt, int c0,
+                                              int dc, F&& one) {
+    constexpr int st = WIN ? 4 : 1;
+    int c = c0, e = chunk_first<WIN>(c0);
+    int4 q = e < cnt ? ld_slots(col + ((size_t)c << 7)) : make_int4(0, 0, 0, 0);
+#pragma unroll 1
+    while (e < cnt) {
+        const int cn = c + dc, en = chunk_first<WIN>(cn);
+        const int4 qn = en < cnt ? ld_slots(col + ((size_t)cn << 7)) : q;
+        one(q.x);
+        if (e + st < cnt) one(q.y);
+        if (e + 2 * st < cnt) one(q.z);
+        if (e + 3 * st < cnt) one(q.w);
+        q = qn;
+        c = cn;
+        e = en;
+    }
+}
+
 // Squared distance with an explicit rounding sequence, so the in-range test gives the same
 // answer in the list build, in the walking passes and in the list passes.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {

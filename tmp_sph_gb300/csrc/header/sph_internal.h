@@ -106,8 +106,9 @@ using Pass1Out = Pass1OutT<float>;
 
 enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 
-// Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + c * 32 + i % 32] (each warp
-// of 32 consecutive particles owns a block of cap x 32 slots), count[i] entries, and xb[i]
+// Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + (c / 4) * 128 + (i % 32) * 4
+// + c % 4] (each warp of 32 consecutive particles owns a block of cap x 32 slots, its particles'
+// slots four to an int4, side by side), count[i] entries, and xb[i]
 // the position i had when the list was built (cell-local offset in mixed precision).  The list
 // holds every pair closer than the list cutoff (KParams::kh2_list, the support radius plus a
 // skin), in candidate-walk order; count[i] > cap means the list overflowed for i and the
@@ -185,14 +186,9 @@ cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float*
                                   const int* type, const int* inst_off, int n_inst,
                                   ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
                                   cudaStream_t s);
-// Lane-group variants of the list kernels (equation/ns_groups.cu): k.lanes in {2, 4, 8, 16}
-// lanes per particle over a list in the group layout; launch_nbr_build / launch_pass1 /
-// launch_pass2_step dispatch to them when k.lanes > 1.
-template <class P>
-cudaError_t launch_nbr_build_groups(const KParamsT<typename P::T>& k,
-                                    const ParticleSetT<typename P::T>& in, const unsigned* keys,
-                                    const int* cs, const NbrList& nl, int walls_all,
-                                    unsigned* err, cudaStream_t s, const unsigned* gate);
+// Lane-group variants of the list passes (equation/ns_groups.cu): k.lanes (pass 1) and
+// k.lanes2 (pass 2) in {2, 4, 8, 16} lanes per particle over the one-lane list; launch_pass1 /
+// launch_pass2_step dispatch to them when the pass's G > 1.
 template <class P>
 cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
                                 const ParticleSetT<typename P::T>& in, const unsigned* keys,
@@ -315,7 +311,8 @@ struct sph_ctx {
     int opt_threads = 128;   // neighbour kernels: threads per block
     int opt_ppt = 1;         // neighbour kernels: particles per thread
     int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
-    int opt_lanes = 1;       // neighbour-list kernels: lanes per particle
+    int opt_lanes = 0;       // list pass 1: lanes per particle (0: the precision's default)
+    int opt_lanes2 = 1;      // list pass 2: lanes per particle
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;

@@ -519,13 +519,19 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
             }
             hash[k] = nk;
             // a particle entering or leaving the neighbour search (park_inactive) needs new
-            // lists; one that stays outside it is in no list
+            // lists; one that stays outside it is in no list.  Marked as pass 2 marks it (a
+            // box no skin covers, not a forced rebuild), so the adaptive skin of a host loop
+            // follows the resident run's
             const bool out_now = inactive_key(kp, nk);
-            if (out_now != inactive_key(kp, key)) atomicOr(force, 1u);
+            const bool moved_out = out_now != inactive_key(kp, key);
+            if (moved_out) {
+                box.add(3.0e38f, 3.0e38f, 3.0e38f);
+                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+            }
             dst.rec[2 * (size_t)k] = a;
             dst.xyz[k] = make4<T>(a.x, a.y, a.z, srho > T(0) ? T(1) : T(-1));
             raise_flags(err, f);
-            if (xb && !out_now) {
+            if (xb && !out_now && !moved_out) {
                 const float4 b = xb[k];
                 box.add((float)a.x - b.x, (float)a.y - b.y, (float)a.z - b.z);
             }

@@ -38,6 +38,8 @@ KParams make_kparams(const sph_params& p, int n) {
     k.ppt = 1;
     k.pairs = 0;
     k.lanes = 1;
+    k.lanes2 = 1;
+    k.list_win = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];
@@ -101,6 +103,8 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.ppt = 1;
     k.pairs = 0;
     k.lanes = 1;
+    k.lanes2 = 1;
+    k.list_win = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
     k.gmin_z = p.grid_min[2];

@@ -55,6 +55,11 @@ class Solver:
     def set_option(self, opt: int, value: int) -> None:
         call("sph_ctx_set_option", self.handle, opt, int(value))
 
+    def get_option(self, opt: int) -> int:
+        v = C.c_int(0)
+        call("sph_ctx_get_option", self.handle, opt, C.byref(v))
+        return v.value
+
     def upload(self, pos, vel, rho, p, typ, stream=None) -> None:
         """Host numpy arrays or device torch tensors, original particle order."""
         host = isinstance(pos, np.ndarray)

@@ -282,6 +282,7 @@ def run_batch(args):
     sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
+    lanes = lanes_in_effect(sol)
     sol.upload_instances(states, stream=stream)
     sol.step(args.warmup, stream=stream)
     torch.cuda.synchronize()
@@ -315,7 +316,7 @@ def run_batch(args):
                    "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
                    "neighbour_list_skin_over_kh": args.skin / 1000.0,
                    "graph_mode": args.graph_mode,
-                   "lanes_per_particle_pass1_pass2": lanes_in_effect(sol)},
+                   "lanes_per_particle_pass1_pass2": lanes},
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps},
         "autotune": autotune.summary(tuned) if tuned else None,
         "gpu_launches": count_launches(sol_cells_batch(p, n_inst, args.skin), 2 * args.steps,

@@ -48,7 +48,8 @@ PHASE_BYTES = {"sort": B_SORT, "gather_cells": B_PERMUTE, "nbr_build": 16, "pass
 PHASE_KERNEL = {"sort": "k_rs_upsweep/k_rs_scan/k_rs_downsweep",
                 "gather_cells": "k_gather + k_cell_mark/k_cell_fill",
                 "nbr_build": "k_nbr_build (one cell walk; positions read once = 16 B)",
-                "pass1": "k_pass1", "pass2_integrate": "k_pass2<MODE_PRED|MODE_CORR>"}
+                "pass1": "k_pass1_g<2 lanes> (k_pass1 with one lane)",
+                "pass2_integrate": "k_pass2<MODE_PRED|MODE_CORR>"}
 
 
 def dist_env():

@@ -267,7 +267,8 @@ typedef struct sph_ctx sph_ctx;
                              1 (one thread per particle), 2, 4, 8 or 16 (a group of lanes shares a
                              particle's list and reduces its sums; not with SPH_OPT_PAIRS); 0:
                              the defaults below.  With groups in either pass the lists store
-                             their 16-entry windows transposed (a change rebuilds them) */
+                             their entries interleaved in windows of eight (a change rebuilds
+                             them) */
 #define SPH_OPT_PASS1_LANES 14  /* the same for list pass 1 (density sums) alone; default (0):
                              2 in FP32 and mixed precision with a list skin, else 1 */
 #define SPH_OPT_PASS2_LANES 15  /* the same for list pass 2 (forces + integrator) alone;

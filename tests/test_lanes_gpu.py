@@ -92,7 +92,7 @@ def test_per_pass_lanes(sphlib, oracle, cuda, report, g1, g2):
 
 
 def test_lanes_switch(sphlib, cuda, report):
-    """Lane groups read transposed list windows: turning groups on or off rebuilds the lists at
+    """Lane groups read interleaved list windows: turning groups on or off rebuilds the lists at
     the next half step; changing G while groups stay on keeps them (the rebuilds follow a run
     without that change).  The run continues either way."""
     import torch

@@ -61,24 +61,25 @@
 namespace sph {
 
 namespace {
-// Appends slots to a list column.  Plain windows: four slots at a time (one 16-byte store per
-// four), the group being filled staged in the thread's 16 bytes of shared memory — one store
-// per slot at a computed address, where keeping it in registers took a select per register per
-// slot, and the walk's divergent hit path runs for nearly every candidate a warp tests (build
-// −6%).  Transposed windows: each slot stored at its place directly (4-byte stores; staging
-// the window's 16 slots in shared memory took L1 from the build's position reads and was no
-// faster).
+// Appends slots to a list column.  Plain: four slots at a time (one 16-byte store per four),
+// the group being filled staged in the thread's 16 bytes of shared memory — one store per slot
+// at a computed address, where keeping it in registers took a select per register per slot,
+// and the walk's divergent hit path runs for nearly every candidate a warp tests (build −6%).
+// Interleaved: the window of eight staged the same way (the thread's eight slots NS_MAX_THREADS
+// words apart, so a warp's stores hit 32 banks) and stored as two int4.  Shared memory of a
+// block: SlotWriter<WIN>::kStage int4 per thread.
 template <bool WIN>
 struct SlotWriter;
 
 template <>
 struct SlotWriter<false> {
+    static constexpr int kStage = 1;
     int* __restrict__ col;
     int cap;
     int* buf;  // the thread's four staging slots (shared memory, 16-byte aligned)
     int cnt = 0;
-    __device__ __forceinline__ SlotWriter(int* c, int cp, int* stage)
-        : col(c), cap(cp), buf(stage) {}
+    __device__ __forceinline__ SlotWriter(int* c, int cp, int4* stage)
+        : col(c), cap(cp), buf(reinterpret_cast<int*>(stage + threadIdx.x)) {}
     __device__ __forceinline__ void put(int v) {
         buf[cnt & 3] = v;
         cnt++;
@@ -96,22 +97,37 @@ struct SlotWriter<false> {
 
 template <>
 struct SlotWriter<true> {
+    static constexpr int kStage = 2;
     int* __restrict__ col;
     int cap;
+    int* buf;  // the thread's eight staging slots, buf[p * NS_MAX_THREADS] (shared memory)
     int cnt = 0;
-    __device__ __forceinline__ SlotWriter(int* c, int cp, int*) : col(c), cap(cp) {}
-    // entry e of window u goes to chunk 4u + (e mod 4), component (e / 4) mod 4; cap is a
-    // multiple of 16, so every window below cap fits
+    __device__ __forceinline__ SlotWriter(int* c, int cp, int4* stage)
+        : col(c), cap(cp), buf(reinterpret_cast<int*>(stage) + threadIdx.x) {}
+    // entry e of a window goes to chunk e mod 2, component e / 2
     __device__ __forceinline__ void put(int v) {
-        if (cnt < cap)
-            col[((size_t)(((cnt >> 4) << 2) | (cnt & 3)) << 7) | (size_t)((cnt >> 2) & 3)] = v;
+        const int e = cnt & 7;
+        buf[(((e & 1) << 2) | (e >> 1)) * NS_MAX_THREADS] = v;
         cnt++;
+        if ((cnt & 7) == 0 && cnt <= cap) store(cnt - 8, 2);
     }
-    __device__ __forceinline__ void flush() {}
+    // the last, partial window: its chunks that hold entries (chunk a holds entry a first);
+    // cap is a multiple of 16, so the window fits
+    __device__ __forceinline__ void flush() {
+        const int r = cnt & 7;
+        if (r && cnt < cap) store(cnt & ~7, r > 1 ? 2 : 1);
+    }
+    __device__ __forceinline__ void store(int e0, int chunks) {
+        for (int a = 0; a < chunks; a++) {
+            const int* w = buf + 4 * a * NS_MAX_THREADS;
+            *reinterpret_cast<int4*>(col + ((size_t)(e0 + 4 * a) << 5)) =
+                make_int4(w[0], w[NS_MAX_THREADS], w[2 * NS_MAX_THREADS], w[3 * NS_MAX_THREADS]);
+        }
+    }
 };
 
 // List modes of the one-lane passes (template LIST): no list (cell walks), a list of plain
-// windows, or one of transposed windows (KParams::list_win).  The mode is a template
+// windows, or one of interleaved windows (KParams::list_win).  The mode is a template
 // parameter: a runtime choice between the two loops cost pass 2 1%.
 enum { LIST_NONE = 0, LIST_PLAIN = 1, LIST_WIN = 2 };
 
@@ -163,7 +179,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
                                               const vec4_t<typename P::T>* __restrict__ X,
                                               const unsigned* __restrict__ keys,
                                               const int* __restrict__ cs, const NbrList& nl,
-                                              int walls_all, unsigned* err, int* stage, int i) {
+                                              int walls_all, unsigned* err, int4* stage, int i) {
     using T = typename P::T;
     const vec4_t<T> pi = X[i];
     if (nl.xb) nl.xb[i] = as_float4(pi);
@@ -201,9 +217,9 @@ __global__ void __launch_bounds__(NS_MAX_THREADS)
 k_nbr_build(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
             const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
             int walls_all, unsigned* err, const unsigned* gate) {
-    __shared__ int4 s_stage[WIN ? 1 : NS_MAX_THREADS];
+    __shared__ int4 s_stage[SlotWriter<WIN>::kStage * NS_MAX_THREADS];
     if (gated_off(gate)) return;
-    int* stage = reinterpret_cast<int*>(&s_stage[WIN ? 0 : threadIdx.x]);
+    int4* stage = s_stage;
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
@@ -334,7 +350,7 @@ __device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
                                                const vec4_t<typename P::T>* __restrict__ X,
                                                const unsigned* __restrict__ keys,
                                                const int* __restrict__ cs, const NbrList& nl,
-                                               int walls_all, unsigned* err, int* stage, int c) {
+                                               int walls_all, unsigned* err, int4* stage, int c) {
     using T = typename P::T;
     using V = vec4_t<T>;
     const int i0 = 2 * c, i1 = 2 * c + 1;
@@ -510,8 +526,7 @@ k_nbr_build_pairs(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __rest
     if (gated_off(gate)) return;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < (k.n + 1) / 2)
-        nbr_build_pair<P>(k, X, keys, cs, nl, walls_all, err,
-                          reinterpret_cast<int*>(&s_stage[threadIdx.x]), c);
+        nbr_build_pair<P>(k, X, keys, cs, nl, walls_all, err, s_stage, c);
 }
 
 template <class P, bool WRITE_SUMS>

@@ -14,12 +14,12 @@
 // in a fixed tree, so results are deterministic and independent of the launch shape, but not
 // bit-equal to one lane per particle (the sums associate differently).
 //
-// List layout.  The groups read the one-lane list with transposed windows (ns_pair.cuh):
+// List layout.  The groups read the one-lane list with interleaved windows (ns_pair.cuh):
 // lane s of a group takes int4 chunks s, s + G, s + 2G, ... of its particle's column, so at
-// every step the group gathers G consecutive entries.  With G = 4 the 8 particles of a warp read
-// 8 consecutive int4s of each of four chunk rows — four whole lines per request, as the
-// one-lane passes do.  The list build is the one-lane build with another slot order, and each
-// pass picks its own G.
+// every step each pair of lanes gathers two consecutive entries.  With G = 2 the 16 particles
+// of a warp read 16 consecutive int4s of each of two chunk rows — four whole lines per request,
+// as the one-lane passes do.  The list build is the one-lane build with another slot order, and
+// each pass picks its own G.
 //
 // Blocks.  A block of T threads owns T consecutive particles and visits them in G rounds of T/G
 // particles (one group each), parking the reduced sums in shared memory; then every thread
@@ -122,7 +122,8 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
             const T r2 = dist2(dx, dy, dz);
             if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
         };
-        // this lane's chunks s, s + G, ... (the group gathers G consecutive entries per step)
+        // this lane's chunks s, s + G, ... (each pair of lanes gathers two consecutive entries
+        // per step)
         if (k.list_win)
             for_each_slot<true>(nl.idx + nbr_col(nl, i), cnt, s, G, one);
         else

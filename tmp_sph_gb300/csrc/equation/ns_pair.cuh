@@ -40,18 +40,19 @@ __device__ __forceinline__ int4 ld_slots(const int* p) {
     return v;
 }
 
-// List windows.  A column is written in windows of 16 entries, four int4 chunks.  A plain
-// window keeps walk order (chunk a holds entries 4a .. 4a+3), so the one-lane passes sum in
-// the order a cell walk visits.  A transposed window (KParams::list_win, set while a pass runs
-// lane groups) holds entries a, a+4, a+8, a+12 in chunk a: the G lanes of a group, reading
-// chunks s, s + G, ..., then gather G consecutive entries — neighbouring records, a line or
-// two — side by side at every step.  (Reading plain windows that way had a group gathering
-// entries four apart: pass 1 at G = 4 took 1.03 ms against 0.79 with one lane; swapping
-// entries between the lanes of a pair with shuffles cost more than it saved, 0.83 at G = 2.)
-// First entry of chunk c; its four entries are st = 4 (transposed) or 1 (plain) apart.
+// List windows.  A plain column keeps walk order (int4 chunk c holds entries 4c .. 4c+3), so
+// the one-lane passes sum in the order a cell walk visits.  An interleaved column
+// (KParams::list_win, set while a pass runs lane groups) is written in windows of eight
+// entries, two chunks: chunk 2u holds entries 8u, 8u+2, 8u+4, 8u+6 and chunk 2u+1 the odd ones.
+// Lane s of a group reads chunks s, s + G, ..., so the two lanes of every pair gather two
+// consecutive entries — neighbouring records, mostly one line — at each step.  (Reading plain
+// chunks that way had the lanes of a pair four entries apart: pass 1 at G = 2 took 0.86 ms
+// against 0.79 with one lane and 0.76 interleaved; swapping entries between the lanes with
+// shuffles cost more than it saved, 0.83.)  First entry of chunk c; its four entries are
+// st = 2 (interleaved) or 1 (plain) apart.
 template <bool WIN>
 __device__ __forceinline__ int chunk_first(int c) {
-    return WIN ? c + 12 * (c >> 2) : c << 2;
+    return WIN ? c + 6 * (c >> 1) : c << 2;
 }
 
 // one(slot) for the entries of a column (cnt <= cap of them) in chunks c0, c0 + dc, ... (the
@@ -61,7 +62,7 @@ __device__ __forceinline__ int chunk_first(int c) {
 template <bool WIN, class F>
 __device__ __forceinline__ void for_each_slot(const int* __restrict__ col, int cnt, int c0,
                                               int dc, F&& one) {
-    constexpr int st = WIN ? 4 : 1;
+    constexpr int st = WIN ? 2 : 1;
     int c = c0, e = chunk_first<WIN>(c0);
     int4 q = e < cnt ? ld_slots(col + ((size_t)c << 7)) : make_int4(0, 0, 0, 0);
 #pragma unroll 1

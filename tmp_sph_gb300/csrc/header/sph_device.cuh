@@ -53,7 +53,7 @@ struct KParamsT {
     int pairs;  // two consecutive particles per thread over the union of their lists
     int lanes;   // lanes per particle in list pass 1 (1, or 2 .. 16: ns_groups.cu)
     int lanes2;  // and in list pass 2
-    int list_win;  // list windows stored transposed (for lane groups; ns_pair.cuh)
+    int list_win;  // list entries interleaved in windows of eight (for lane groups; ns_pair.cuh)
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
     T inv_cell;          // 1 / cell (the FP64 and mixed solvers' hash scales by it)

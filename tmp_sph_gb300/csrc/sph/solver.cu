@@ -246,15 +246,15 @@ bool stacked_params(const sph_params& P, double skin, int n_inst, sph_params* ou
 }
 
 // Lanes per particle of list pass 1: the option, or by default 2 in FP32 and mixed precision
-// while the lists have a skin (4.96M-particle dam break: pass 1 −4%, step −1.8% in FP32,
+// while the lists have a skin (4.96M-particle dam break: pass 1 −4%, step −1.6% in FP32,
 // −0.9% mixed), and 1 in FP64 (no gain) and without a skin (lists rebuilt every half step:
-// the build of transposed windows costs 27% more, the step 11%).
+// the build of interleaved windows costs 17% more, the step 6%).
 static int pass1_lanes(const sph_ctx* c) {
     if (c->opt_lanes > 0) return c->opt_lanes;
     return c->prec != SPH_PREC_FP64 && c->skin > 0.0 ? 2 : 1;
 }
 
-// Lane groups read transposed list windows, one lane per particle plain ones.
+// Lane groups read interleaved list windows, one lane per particle plain ones.
 static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1 || c->opt_lanes2 > 1; }
 
 template <class T>

@@ -362,7 +362,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=None, choices=[1, 2, 4, 8, 16],
                     help="lanes per particle in both neighbour-list passes")
     ap.add_argument("--pass1-lanes", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
-                    help="lanes per particle in list pass 1 (0: 2 in FP32, 1 otherwise)")
+                    help="lanes per particle in list pass 1 (0: 2 in FP32 with a skin, else 1)")
     ap.add_argument("--pass2-lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
                     help="lanes per particle in list pass 2")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],

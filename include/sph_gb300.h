@@ -270,7 +270,7 @@ typedef struct sph_ctx sph_ctx;
                              their entries interleaved in windows of eight (a change rebuilds
                              them) */
 #define SPH_OPT_PASS1_LANES 14  /* the same for list pass 1 (density sums) alone; default (0):
-                             2 in FP32 and mixed precision with a list skin, else 1 */
+                             2 in FP32 with a list skin, else 1 */
 #define SPH_OPT_PASS2_LANES 15  /* the same for list pass 2 (forces + integrator) alone;
                              default 1 */
 

@@ -130,11 +130,11 @@ def test_lanes_switch(sphlib, cuda, report):
 
 
 def test_lanes_defaults(sphlib, cuda):
-    """Pass 1 takes two lanes per particle in FP32 and mixed precision while the lists have a
-    skin, one in FP64 and without a skin; pass 2 one lane in all."""
+    """Pass 1 takes two lanes per particle in FP32 while the lists have a skin, one without a
+    skin and in the other precisions; pass 2 one lane in all."""
     from tmp_sph_gb300 import api, solver as S
     st, p = small()
-    for prec, want in (("fp32", 2), ("mixed", 2), ("mixed_comp", 2), ("fp64", 1)):
+    for prec, want in (("fp32", 2), ("mixed", 1), ("mixed_comp", 1), ("fp64", 1)):
         with S.Solver(p, len(st["rho"]), precision=prec) as sol:
             assert sol.get_option(api.SPH_OPT_PASS1_LANES) == want, prec
             assert sol.get_option(api.SPH_OPT_PASS2_LANES) == 1, prec

@@ -245,13 +245,13 @@ bool stacked_params(const sph_params& P, double skin, int n_inst, sph_params* ou
     return true;
 }
 
-// Lanes per particle of list pass 1: the option, or by default 2 in FP32 and mixed precision
-// while the lists have a skin (4.96M-particle dam break: pass 1 −4%, step −1.6% in FP32,
-// −0.9% mixed), and 1 in FP64 (no gain) and without a skin (lists rebuilt every half step:
-// the build of interleaved windows costs 17% more, the step 6%).
+// Lanes per particle of list pass 1: the option, or by default 2 in FP32 while the lists have
+// a skin (4.96M-particle dam break: pass 1 −4%, step −1.6%), else 1: without a skin the lists
+// are rebuilt every half step and the build of interleaved windows costs 17% more (the step
+// 6%), and mixed precision and FP64 gain nothing (mixed: 3.640 ms per step either way).
 static int pass1_lanes(const sph_ctx* c) {
     if (c->opt_lanes > 0) return c->opt_lanes;
-    return c->prec != SPH_PREC_FP64 && c->skin > 0.0 ? 2 : 1;
+    return c->prec == SPH_PREC_FP32 && c->skin > 0.0 ? 2 : 1;
 }
 
 // Lane groups read interleaved list windows, one lane per particle plain ones.

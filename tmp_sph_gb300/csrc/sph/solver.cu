@@ -832,12 +832,11 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
         float* srho = st.rho;
         float* sp = st.p;
         int* stype = st.type;
-        cudaError_t e;
-        if ((e = cudaMemcpyAsync(spos, pos, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(svel, vel, (size_t)n * 12, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(srho, rho, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(sp, p, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(stype, type, (size_t)n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        if (cudaMemcpyAsync(spos, pos, (size_t)n * 12, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(svel, vel, (size_t)n * 12, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(srho, rho, (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(sp, p, (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(stype, type, (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
             return SPH_ERR_CUDA;
         dpos = spos; dvel = svel; drho = srho; dp = sp; dtype = stype;
     }
@@ -1196,27 +1195,26 @@ extern "C" int sph_ns(sph_ctx* c, float* s_pos, float* s_vel, float* s_rho, floa
     cudaStream_t s = (cudaStream_t)stream;
     KParams k = make_kparams(c->P, n);
     k.park_inactive = 0;  // the drop-in takes the caller's cells as they are
-    cudaError_t e;
-    if ((e = launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->x, c->keys_sorted,
-                               c->err, s)) != cudaSuccess)
+    if (launch_aos_to_set(k, s_pos, s_vel, s_rho, s_p, s_type, hash, c->x, c->keys_sorted,
+                          c->err, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s)) != cudaSuccess)
+    if (build_cell_starts(c->keys_sorted, n, c->P.num_cells, c->cell_start, s) != cudaSuccess)
         return SPH_ERR_CUDA;
     // the drop-in builds and uses its list within this call, with the constant cutoff
     NbrList dl = c->nl;
     dl.cut2 = nullptr;
     dl.fluid_cells = nullptr;
     const NbrList* nl = list_for(c) ? &dl : nullptr;
-    if (nl && (e = launch_nbr_build<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, *nl,
-                                    c->opt_wall_rates, c->err, s)) != cudaSuccess)
+    if (nl && launch_nbr_build<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, *nl,
+                                        c->opt_wall_rates, c->err, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass1<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum, w_sum,
-                          s)) != cudaSuccess)
+    if (launch_pass1<PrecF32>(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rhop_sum,
+                              w_sum, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_pass2_rates(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt,
-                                vel_dt, c->opt_wall_rates, s)) != cudaSuccess)
+    if (launch_pass2_rates(k, c->x, c->keys_sorted, c->cell_start, nl, c->p1, rho_dt, vel_dt,
+                           c->opt_wall_rates, s) != cudaSuccess)
         return SPH_ERR_CUDA;
-    if ((e = launch_ns_writeback(k, s_type, c->p1.self, s_rho, s_p, dofv, s)) != cudaSuccess)
+    if (launch_ns_writeback(k, s_type, c->p1.self, s_rho, s_p, dofv, s) != cudaSuccess)
         return SPH_ERR_CUDA;
     // the resident state (y) is untouched, but the cell and neighbour lists now describe these
     // arrays: a later sph_step rebuilds them first

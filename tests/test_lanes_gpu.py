@@ -205,6 +205,28 @@ def test_lanes_batch_equals_solo(sphlib, cuda):
             assert np.array_equal(out[k][sl], ref[k]), (b, k)
 
 
+@pytest.mark.parametrize("cap", [32, 48, 64])
+def test_interleaved_windows_at_small_capacities(sphlib, oracle, cuda, report, cap):
+    """Lists of 32-64 slots: counts end in every position of a window of eight, reach the
+    capacity exactly, or pass it (those particles walk their cells).  Pass 1 with two and
+    four lanes over the interleaved windows follows the one-lane run to FP32 rounding and the
+    oracle within the step tolerance."""
+    from tmp_sph_gb300 import api
+    st, p = small()
+    opts = {api.SPH_OPT_NEIGHBOR_CAP: cap}
+    one = run(st, p, 4, 1, opts=opts)
+    ref = oracle.run(oracle.params_like(p), st, 4)
+    fl = st["type"] == 1
+    for g in (2, 4):
+        out = run(st, p, 4, 1, opts={**opts, api.SPH_OPT_PASS1_LANES: g})
+        assert (out["flags"] & ~api.SPH_FLAG_NEIGHBOR_OVERFLOW) == 0
+        e = rel_l2(out["vel"][fl], one["vel"][fl], floor=1e-3 * np.sqrt(fl.sum()))
+        report(f"cap {cap}, pass-1 lanes {g} vs one lane, 4 steps, vel", e, 1e-5)
+        assert e < 1e-5
+        errs = field_errors(out, ref, st)
+        assert all(v < 2e-4 for v in errs.values()), (g, errs)
+
+
 def test_lanes_option_checked(sphlib):
     from tmp_sph_gb300 import api, cases, solver as S
     st, p = small()

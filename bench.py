@@ -60,17 +60,22 @@ def dist_env():
 PHASE_NCU_NAME = {"nbr_build": "k_nbr_build", "pass1": "k_pass1", "pass2_integrate": "k_pass2"}
 
 
-def ncu_traffic() -> dict:
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the committed
-    ncu summary of this workload, keyed by kernel."""
+def ncu_summary(key: str) -> dict:
+    """A per-kernel figure from the committed ncu summary of this workload (a line
+    `key: {json}`): traffic_bytes_per_launch (dram__bytes_read.sum + dram__bytes_write.sum),
+    l1_data_pipe_pct (l1tex__data_pipe_lsu_wavefronts, % of peak)."""
     path = os.path.join(ROOT, "profiles", "neighbour_kernels_large.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return json.loads(line.split(":", 1)[1])
     except (OSError, ValueError):
         pass
     return {}
+
+
+def ncu_traffic() -> dict:
+    return ncu_summary("traffic_bytes_per_launch")
 
 
 def peaks():
@@ -495,6 +500,7 @@ def main():
             "traffic_source": "profiles/neighbour_kernels_large.md (ncu, one launch)",
             "dram_gbs_at_traffic": (traffic / (dom_ms / 1e3) / 1e9) if traffic else None,
             "bytes_per_particle": PHASE_BYTES[dom],
+            "l1_data_pipe_pct": ncu_summary("l1_data_pipe_pct").get(PHASE_NCU_NAME.get(dom, "")),
             "note": "the neighbour kernels are issue- or L1-throughput bound (sparse gather "
                     "of neighbour data), not HBM bound; frac is algorithmic bytes over the "
                     "measured copy bandwidth"}

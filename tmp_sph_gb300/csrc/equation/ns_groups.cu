@@ -4,11 +4,13 @@
 // computeGovering_equationD, src/equation/ns.cu:30-249), same list contents, different
 // assignment of work to lanes.  With one thread per particle every lane of a warp gathers a
 // different neighbour record, and a warp-level gather touches about twenty distinct 128-byte
-// lines: the passes are limited by L1 data-stage wavefronts.  With G lanes per particle the G
-// records a group gathers in one step are entries of one list a few slots apart — nearby slots
-// of a few cell strips — and the 32/G particles of a warp are neighbours in the sorted order
-// with largely the same lists; a warp also runs its loop for the longest list of 32/G
-// particles rather than of 32.
+// lines: the passes are limited by L1 data-stage wavefronts.  With G lanes per particle each
+// pair of lanes of a group gathers two consecutive entries of one list in one step —
+// neighbouring records, mostly one line — and a warp runs its loop for the longest list of
+// 32/G particles rather than of 32.  Measured on the 4.96M-particle dam break: pass 1 at G = 2
+// 0.756 ms against 0.793 with one lane (the resident default in FP32 with a list skin); pass 2
+// stays one lane (0.849 ms at G = 2 against 0.814: its larger per-pair body on half the
+// particles per warp, and more sums to reduce).
 //
 // Sums.  Each lane accumulates its share of the pairs; a group reduces them with xor shuffles
 // in a fixed tree, so results are deterministic and independent of the launch shape, but not

@@ -241,9 +241,12 @@ def set_lanes(sol, args) -> None:
         sol.set_option(api.SPH_OPT_PASS2_LANES, args.pass2_lanes)
 
 
-def lanes_in_effect(sol) -> list:
+def lanes_in_effect(sol) -> dict:
+    """Launch shape of the neighbour kernels in effect (defaults resolved)."""
     from tmp_sph_gb300 import api
-    return [sol.get_option(api.SPH_OPT_PASS1_LANES), sol.get_option(api.SPH_OPT_PASS2_LANES)]
+    return {"lanes_per_particle_pass1_pass2": [sol.get_option(api.SPH_OPT_PASS1_LANES),
+                                               sol.get_option(api.SPH_OPT_PASS2_LANES)],
+            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS)}
 
 
 def config_block(args, p, n, lanes=None):
@@ -254,8 +257,7 @@ def config_block(args, p, n, lanes=None):
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
             "graph_mode": args.graph_mode, "pairs": args.pairs,
-            "lanes_per_particle_pass1_pass2": lanes,
-            "adaptive_skin": args.adaptive_skin}
+            **(lanes or {}), "adaptive_skin": args.adaptive_skin}
 
 
 def run_batch(args):
@@ -322,7 +324,7 @@ def run_batch(args):
                    "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
                    "neighbour_list_skin_over_kh": args.skin / 1000.0,
                    "graph_mode": args.graph_mode,
-                   "lanes_per_particle_pass1_pass2": lanes},
+                   **lanes},
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps},
         "autotune": autotune.summary(tuned) if tuned else None,
         "gpu_launches": count_launches(sol_cells_batch(p, n_inst, args.skin), 2 * args.steps,

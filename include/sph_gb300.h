@@ -253,7 +253,8 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_PRECISION     8  /* SPH_PREC_* below; set before sph_upload (the state is
                                     reallocated; the uploaded state is dropped) */
 #define SPH_OPT_BLOCK_THREADS 9  /* threads per block of the neighbour kernels: 32..256, a
-                                    multiple of 32 (default 128) */
+                                    multiple of 32; 0 (default): 256 in FP32, 128 in the
+                                    other precisions */
 #define SPH_OPT_PARTICLES_PER_THREAD 10  /* particles each thread of the neighbour kernels
                                     handles, grid-stride (1..64, default 1) */
 #define SPH_OPT_PAIRS 11  /* 1: the neighbour kernels take two consecutive particles per thread

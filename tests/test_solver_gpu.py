@@ -342,9 +342,12 @@ def test_launch_shape_options_are_checked(sphlib):
     st, p = cases.build("small", physics="config", dx=0.04)
     with S.Solver(p, len(st["rho"])) as sol:
         lib = api.lib()
-        for bad in (0, 16, 48, 288):
+        for bad in (-32, 16, 48, 288):
             assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_BLOCK_THREADS, bad) == \
                 api.SPH_ERR_ARG
+        # 0 restores the precision's default: 256 threads in FP32
+        assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_BLOCK_THREADS, 0) == api.SPH_OK
+        assert sol.get_option(api.SPH_OPT_BLOCK_THREADS) == 256
         for bad in (0, 65):
             assert lib.sph_ctx_set_option(sol.handle, api.SPH_OPT_PARTICLES_PER_THREAD, bad) == \
                 api.SPH_ERR_ARG

@@ -129,12 +129,14 @@ def apply(sol, best: dict) -> None:
 
 
 def summary(best: dict) -> dict:
-    """The choice without the table, plus the estimate of the default (128 threads, one
-    particle per thread, pass-1 lanes 2 in FP32 and 1 otherwise, skin 0.1 kh)."""
+    """The choice without the table, plus the estimate of the default (in FP32 256 threads and
+    two pass-1 lanes, otherwise 128 threads and one lane; one particle per thread, skin
+    0.1 kh)."""
     out = {k: v for k, v in best.items() if k != "table"}
-    lanes = 2 if best.get("precision", "fp32") == "fp32" else 1
+    fp32 = best.get("precision", "fp32") == "fp32"
+    dflt = (256 if fp32 else 128, 1, 2 if fp32 else 1, 100)
     for m in best["table"]:
-        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == (128, 1, lanes, 100):
+        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == dflt:
             out["default_step_ms_estimate"] = m["step_ms_estimate"]
     return out
 

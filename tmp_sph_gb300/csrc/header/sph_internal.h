@@ -308,7 +308,7 @@ struct sph_ctx {
     int opt_nbr_list = 1;
     int opt_nbr_cap = 0;  // 0: nbr_capacity_for(P)
     int opt_cond_graph = 1;  // graph replay skips the rebuild kernels through conditional nodes
-    int opt_threads = 128;   // neighbour kernels: threads per block
+    int opt_threads = 0;     // neighbour kernels: threads per block (0: the precision's default)
     int opt_ppt = 1;         // neighbour kernels: particles per thread
     int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
     int opt_lanes = 0;       // list pass 1: lanes per particle (0: the precision's default)

@@ -254,6 +254,16 @@ static int pass1_lanes(const sph_ctx* c) {
     return c->prec == SPH_PREC_FP32 && c->skin > 0.0 ? 2 : 1;
 }
 
+// Threads per block of the neighbour kernels: the option, or by default 256 in FP32 (their
+// static shared memory is sized for 256 threads, so 128-thread blocks pack twice as much per
+// SM and leave L1 less room: 4.96M dam break 3.26 against 3.32 ms per step, 7.50 against 7.60
+// rebuilding every half step) and 128 in the other precisions (mixed precision's 56-register
+// pass 2 keeps 36 warps per SM in 128-thread blocks, 32 in 256: 3.64 against 3.75 ms).
+static int block_threads(const sph_ctx* c) {
+    if (c->opt_threads > 0) return c->opt_threads;
+    return c->prec == SPH_PREC_FP32 ? 256 : 128;
+}
+
 // Lane groups read interleaved list windows, one lane per particle plain ones.
 static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1 || c->opt_lanes2 > 1; }
 
@@ -261,7 +271,7 @@ template <class T>
 KParamsT<T> resident_kparams(const sph_ctx* c) {
     KParamsT<T> k = make_kparams_t<T>(c->Pi, c->n);
     k.gz_local = c->gz_inst;
-    k.threads = c->opt_threads;
+    k.threads = block_threads(c);
     k.ppt = c->opt_ppt;
     k.pairs = c->opt_pairs;
     // lane groups need the list (and are not combined with pair mode)
@@ -662,7 +672,8 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             drop_graph(c);
             return SPH_OK;
         case SPH_OPT_BLOCK_THREADS:
-            if (value < 32 || value > 256 || value % 32) return SPH_ERR_ARG;
+            // 0: the precision's default
+            if (value != 0 && (value < 32 || value > 256 || value % 32)) return SPH_ERR_ARG;
             c->opt_threads = value;
             drop_graph(c);
             return SPH_OK;
@@ -765,7 +776,7 @@ extern "C" int sph_ctx_get_option(const sph_ctx* c, int option, int* value) {
         case SPH_OPT_SKIN_PERMILLE: *value = (int)std::lround(c->skin * 1000.0); break;
         case SPH_OPT_CONDITIONAL_GRAPH: *value = c->opt_cond_graph; break;
         case SPH_OPT_PRECISION: *value = c->prec; break;
-        case SPH_OPT_BLOCK_THREADS: *value = c->opt_threads; break;
+        case SPH_OPT_BLOCK_THREADS: *value = block_threads(c); break;
         case SPH_OPT_PARTICLES_PER_THREAD: *value = c->opt_ppt; break;
         case SPH_OPT_PAIRS: *value = c->opt_pairs; break;
         case SPH_OPT_ADAPTIVE_SKIN: *value = c->opt_adaptive_skin; break;

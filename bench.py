@@ -198,19 +198,32 @@ def cpu_baseline(st, p, budget_s: float = 20.0) -> dict:
 
 
 def run_reference(args):
-    ws, rank, _ = dist_env()
-    if rank != 0:
+    """The reference arm: the reference has no CPU implementation of its own, so this times the
+    oracle's C restatement of its step loop (src/sph/sph_run.cu:285-336) on all host cores, on
+    the same workload.  The inputs and parameters come from the oracle side (oracle/workload.py:
+    its own generator and parameter derivation), so this process loads no product library.
+    Under torchrun only rank 0 runs; the others exit at once."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if int(os.environ.get("RANK", "0")) != 0:
         return
-    st, p = build_case(args.case)
+    from oracle import oracle as O, workload as W
+    if args.case not in W.GEOM:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"case {args.case}: the reference arm runs the single-case workloads"}))
+        return
+    st, P = W.build(args.case)
     n = len(st["rho"])
-    from oracle import oracle as O
+    n_fluid = st["n_fluid"]
     threads = O.set_threads(0)
-    P = O.params_like(p)
-    for _ in range(min(args.warmup, 1)):
-        O.run(P, st, 1)
+    # the same number of warm-up steps as the timed arm, within a bounded time
+    t0 = time.perf_counter()
+    warm = 0
+    cur = st
+    while warm < args.warmup and (warm == 0 or time.perf_counter() - t0 < args.ref_budget / 3):
+        cur = O.run(P, cur, 1)
+        warm += 1
     t0 = time.perf_counter()
     steps = 0
-    cur = st
     while steps < args.steps and (steps == 0 or time.perf_counter() - t0 < args.ref_budget):
         cur = O.run(P, cur, 1)
         steps += 1
@@ -218,12 +231,14 @@ def run_reference(args):
     val = n * steps / dt
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "impl": "reference", "n_gpus": ws,
-        "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * dt / steps,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded dam-break generator)",
-        "config": config_block(args, p, n),
+        "data": "synthetic (seeded dam-break generator, oracle side)",
+        "config": config_block(args, P, n),
+        "fluid_particle_steps_per_s": n_fluid * steps / dt,
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} full step(s) on all {threads} host threads "
+                         "sample": f"{steps} full step(s) of the {n}-particle workload after "
+                                   f"{warm} warm-up step(s), on all {threads} host threads "
                                    f"(requested {args.steps}, capped at {args.ref_budget:.0f} s)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -241,19 +256,26 @@ def set_lanes(sol, args) -> None:
         sol.set_option(api.SPH_OPT_PASS2_LANES, args.pass2_lanes)
 
 
+def set_subcell(sol, args) -> None:
+    from tmp_sph_gb300 import api
+    if args.subcell is not None:
+        sol.set_option(api.SPH_OPT_SUBCELL_ORDER, args.subcell)
+
+
 def lanes_in_effect(sol) -> dict:
     """Launch shape of the neighbour kernels in effect (defaults resolved)."""
     from tmp_sph_gb300 import api
     return {"lanes_per_particle_pass1_pass2": [sol.get_option(api.SPH_OPT_PASS1_LANES),
                                                sol.get_option(api.SPH_OPT_PASS2_LANES)],
-            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS)}
+            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS),
+            "subcell_order": sol.get_option(api.SPH_OPT_SUBCELL_ORDER)}
 
 
 def config_block(args, p, n, lanes=None):
     return {"workload": f"dam_break_{args.case}_{getattr(args, 'precision', 'fp32')}", "particles": n,
             "fluid_particles": n - p.num_boundary, "dx_m": p.dx, "h_over_dx": 1.3,
             "cells": p.num_cells, "eos": "tait", "dt_s": p.dt,
-            "parallelism": f"replicas x{dist_env()[0]}",
+            "parallelism": f"replicas x{int(os.environ.get('WORLD_SIZE', '1'))}",
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
             "graph_mode": args.graph_mode, "pairs": args.pairs,
@@ -287,6 +309,7 @@ def run_batch(args):
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     set_lanes(sol, args)
+    set_subcell(sol, args)
     sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
@@ -374,6 +397,9 @@ def main():
                     help="lanes per particle in list pass 2")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
+    ap.add_argument("--subcell", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="order of the particles inside a cell (SPH_OPT_SUBCELL_ORDER; default: "
+                         "the library's)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -405,6 +431,7 @@ def main():
     sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
     sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
     set_lanes(sol, args)
+    set_subcell(sol, args)
     sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
     if tuned:
         autotune.apply(sol, tuned)
@@ -457,6 +484,7 @@ def main():
         v = S.Solver(p, n, precision=precision)
         v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
         set_lanes(v, args)
+        set_subcell(v, args)
         v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
         v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
         v.step(3, stream=stream)

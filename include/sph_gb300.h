@@ -274,6 +274,10 @@ typedef struct sph_ctx sph_ctx;
                              2 in FP32 with a list skin, else 1 */
 #define SPH_OPT_PASS2_LANES 15  /* the same for list pass 2 (forces + integrator) alone;
                              default 1 */
+#define SPH_OPT_SUBCELL_ORDER 16  /* order of the particles inside a cell of the resident
+                             state: 0 as uploaded (original index), 1 eight bins along x, 2 by
+                             octant, 3 Morton order of a 4x4x4 sub-grid (the sort key carries
+                             3 or 6 more bits); a change rebuilds the cell and neighbour lists */
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */

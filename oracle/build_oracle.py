@@ -12,7 +12,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libsph_oracle.so")
-SOURCES = ["sph_oracle.c"]
+SOURCES = ["sph_oracle.c", "sph_oracle_gen.c"]
 DEPS = ["sph_oracle.h", "sph_oracle_phys.inc"]
 FLAGS = ["-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall"]
 

@@ -37,6 +37,17 @@ class OrParams(C.Structure):
         return out
 
 
+class OrDamBreak(C.Structure):
+    """or_dam_break (sph_oracle.h): the seeded dam-break generator's description."""
+    _fields_ = [
+        ("dx", C.c_float), ("tank", F3), ("block", F3), ("wall_layers", C.c_int),
+        ("has_obstacle", C.c_int), ("obstacle_min", F3), ("obstacle_max", F3),
+        ("jitter", C.c_float), ("seed", C.c_ulonglong), ("hydrostatic", C.c_int),
+        ("rho0", C.c_float), ("gravity", C.c_float), ("cs", C.c_float), ("eos", C.c_int),
+        ("tait_gamma", C.c_float),
+    ]
+
+
 _lib = None
 
 
@@ -55,6 +66,8 @@ def lib() -> C.CDLL:
                                          P, P, C.c_double, C.c_double, I, I, PP]),
             "or_sort_particles": (None, [P, P, I]),
             "or_set_threads": (I, [I]),
+            "or_dam_break_count": (C.c_long, [C.POINTER(OrDamBreak), C.POINTER(C.c_long)]),
+            "or_dam_break_generate": (I, [C.POINTER(OrDamBreak), P, P, P, P, P, C.c_long]),
         }
         for suf in ("_f32", "_f64"):
             protos.update({
@@ -107,6 +120,23 @@ def params_like(src) -> OrParams:
     for name, _ in OrParams._fields_:
         setattr(p, name, getattr(src, name))
     return p
+
+
+def dam_break_generate(d: OrDamBreak) -> dict:
+    """Host arrays of a generated dam break (walls, obstacle, water): pos/vel (n,3) f32,
+    rho/p (n,) f32, type (n,) i32, plus n_fluid and n_boundary."""
+    nf = C.c_long(0)
+    n = lib().or_dam_break_count(C.byref(d), C.byref(nf))
+    st = {"pos": np.zeros((n, 3), np.float32), "vel": np.zeros((n, 3), np.float32),
+          "rho": np.zeros(n, np.float32), "p": np.zeros(n, np.float32),
+          "type": np.zeros(n, np.int32)}
+    rc = lib().or_dam_break_generate(C.byref(d), _p(st["pos"]), _p(st["vel"]), _p(st["rho"]),
+                                     _p(st["p"]), _p(st["type"]), n)
+    if rc != 0:
+        raise RuntimeError("oracle generator: particle count mismatch")
+    st["n_fluid"] = int(nf.value)
+    st["n_boundary"] = int(n - nf.value)
+    return st
 
 
 def sort_particles(hash_: np.ndarray, index: np.ndarray) -> None:

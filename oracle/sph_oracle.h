@@ -58,6 +58,26 @@ void or_sort_particles(int* hash, int* index, int n);
 /* Number of threads the OpenMP loops may use (0 = library default). Returns the value used. */
 int or_set_threads(int nthreads);
 
+/* Seeded dam-break generator (sph_oracle_gen.c): the layout of the product's sph_dam_break,
+ * restated so the oracle side builds the benchmark workloads on its own. */
+typedef struct or_dam_break {
+    float dx;
+    float tank[3], block[3];
+    int wall_layers, has_obstacle;
+    float obstacle_min[3], obstacle_max[3];
+    float jitter;
+    unsigned long long seed;
+    int hydrostatic;
+    float rho0, gravity, cs;
+    int eos;
+    float tait_gamma;
+} or_dam_break;
+/* Particles of a case (returned) and its fluid particles (*n_fluid). */
+long or_dam_break_count(const or_dam_break* d, long* n_fluid);
+/* Fill pos/vel [3n], rho, p [n], type [n] (walls, obstacle, water); 0 on success. */
+int or_dam_break_generate(const or_dam_break* d, float* pos, float* vel, float* rho, float* p,
+                          int* type, long n);
+
 /* ---- float instantiation (reference arithmetic) ---- */
 void or_calc_hash_f32(const or_params* P, const float* pos, int* hash, int* index, int n);
 void or_reorder_f32(const or_params* P, const float* pos, const float* vel, const float* rho,

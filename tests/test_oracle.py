@@ -126,3 +126,20 @@ def test_openmp_deterministic(sphlib, oracle, threads):
     b = oracle.run(P, st, 2)
     for k in ("pos", "vel", "rho", "p"):
         assert np.array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("name", ["small", "precision", "large", "obstacle"])
+def test_oracle_workload_matches_product_workload(sphlib, oracle, name):
+    """The oracle side builds every benchmark workload by itself (its own MT19937-64 generator
+    and parameter derivation, so bench.py's reference leg loads no product library) and gets
+    the product generator's state and the product's parameters bit for bit, jitter included."""
+    from oracle import workload as W
+    from tmp_sph_gb300 import cases
+    a, pa = W.build(name)
+    b, pb = cases.build(name)
+    for k in ("pos", "vel", "rho", "p", "type"):
+        assert a[k].dtype == b[k].dtype and np.array_equal(a[k], b[k]), (name, k)
+    assert (a["n_fluid"], a["n_boundary"]) == (b["n_fluid"], b["n_boundary"])
+    assert pa.as_dict() == oracle.params_like(pb).as_dict()
+    if name == "large":
+        assert len(a["rho"]) == 4963548 and a["n_fluid"] == 3840000

@@ -18,13 +18,15 @@ namespace sph {
 // bits [0, key_bits).  Scratch layout and size come from sort_scratch_bytes(); no allocation.
 // vals_in == NULL means the values are the identity 0..n-1.  The sorted output lands in
 // keys_out / vals_out (which may alias keys_in / vals_in).  err (may be NULL) receives
-// SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.
+// SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.  out_shift > 0 stores the sorted
+// keys shifted down by that many bits (the resident sort orders by cell and place in the cell,
+// and hands on the cell keys).
 size_t sort_scratch_bytes(int n);
 // gate: see gated_off() — NULL sorts unconditionally.
 cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
                              int* vals_out, int n, int key_bits, void* scratch,
                              size_t scratch_bytes, unsigned* err, cudaStream_t s,
-                             const unsigned* gate = nullptr);
+                             const unsigned* gate = nullptr, int out_shift = 0);
 int key_bits_for(int num_cells);
 
 // ---------------------------------------------------------------- cell list (lib/mesh.cu)
@@ -314,6 +316,7 @@ struct sph_ctx {
     int opt_lanes = 0;       // list pass 1: lanes per particle (0: the precision's default)
     int opt_lanes2 = 1;      // list pass 2: lanes per particle
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
+    int opt_subcell = 0;     // order of the particles inside a cell (subcell_code mode)
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

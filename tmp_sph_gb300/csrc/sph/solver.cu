@@ -280,6 +280,8 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.lanes2 = groups ? c->opt_lanes2 : 1;
     k.list_win = k.lanes > 1 || k.lanes2 > 1;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
+    k.sub_mode = c->opt_subcell;
+    k.sub_bits = subcell_bits(c->opt_subcell);
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
@@ -395,12 +397,13 @@ template <class P>
 cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStream_t s,
                           cudaEvent_t* ev) {
     // with park_inactive, key num_cells marks the slots outside the neighbour search
-    const int bits = key_bits_for(c->Pi.num_cells + (c->P.park_inactive ? 1 : 0));
+    // and below the cell, the particle's place in it (k.sub_bits), which the sort drops again
+    const int bits = key_bits_for(c->Pi.num_cells + (c->P.park_inactive ? 1 : 0)) + k.sub_bits;
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
     cudaError_t e;
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
-                         c->sort_scratch_bytes, c->err, s, gate);
+                         c->sort_scratch_bytes, c->err, s, gate, k.sub_bits);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_GATHER], s);
     // permute the live set y into cell order through x, then copy it back
@@ -709,6 +712,15 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             }
             break;  // the list layout changed: rebuild
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
+        case SPH_OPT_SUBCELL_ORDER:
+            if (value < 0 || value > 3) return SPH_ERR_ARG;
+            // the stacked key must still fit the 32-bit sort
+            if (key_bits_for(c->Pi.num_cells + 1) + subcell_bits(value) > 31) return SPH_ERR_ARG;
+            if (value == c->opt_subcell) return SPH_OK;
+            c->opt_subcell = value;
+            c->rehash = c->loaded;  // the next keys carry the new sub-cell bits
+            drop_graph(c);
+            break;
         case SPH_OPT_PRECISION: {
             if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && !prec_is_mixed(value))
                 return SPH_ERR_ARG;
@@ -780,6 +792,7 @@ extern "C" int sph_ctx_get_option(const sph_ctx* c, int option, int* value) {
         case SPH_OPT_PARTICLES_PER_THREAD: *value = c->opt_ppt; break;
         case SPH_OPT_PAIRS: *value = c->opt_pairs; break;
         case SPH_OPT_ADAPTIVE_SKIN: *value = c->opt_adaptive_skin; break;
+        case SPH_OPT_SUBCELL_ORDER: *value = c->opt_subcell; break;
         case SPH_OPT_LANES_PER_PARTICLE:
         case SPH_OPT_PASS1_LANES: *value = pass1_lanes(c); break;
         case SPH_OPT_PASS2_LANES: *value = c->opt_lanes2; break;

@@ -9,12 +9,21 @@ The timed loop replays the step as a CUDA graph with the state resident in HBM; 
 (~180 MB read and written per pass) is larger than the 129 MB L2, so no flush is needed.
 
 Printed: one JSON line (rank 0) with
-  value        particle-steps/s over all ranks (weak scaling: every rank runs its own replica)
-  e2e          the same metric through sph_step_host (pinned host buffers, upload + step +
-               download inside the timed region)
-  roofline     the dominant kernel's algorithmic bytes per launch / its CUDA-event duration
-  cpu_baseline the oracle (C restatement of the reference, OpenMP) on a bounded sample
-  clocks       nvidia-smi SM clocks and throttle reasons sampled during the timed region
+  value          particle-steps/s over all ranks (weak scaling: every rank runs its own
+                 replica); fluid_particle_steps_per_s counts fluid particles only
+  e2e            the same metric through sph_step_host (pinned host buffers, upload + step +
+                 download inside the timed region)
+  roofline       the dominant kernel's algorithmic bytes per launch / its CUDA-event duration,
+                 with the DRAM traffic of a committed ncu capture at the same launch shape
+  roofline_fp32  flops of the evaluated pairs per step (counted from the pair algebra, pair
+                 counts of the initial state) / step time, over the FP32 FMA peak measured now
+  configured_run the configured 1000 steps from rest, all timed, then the developed flow
+  batched        config 4: 64 dam breaks of uneven size in one batched mixed-precision solver
+                 (graph replay), beside the plain FP32 single-instance value above
+  reference_cuda the reference's own CUDA versions (opt_src_v4, the best, and src/) on the
+                 same state and GPU, from kernels compiled out of its sources (oracle/_ref)
+  cpu_baseline   the oracle (C restatement of the reference, OpenMP) on a bounded sample
+  clocks         nvidia-smi SM clocks and throttle reasons sampled during the timed region
 
 --impl reference times the reference's hot path on the host cores instead: the reference has
 no CPU implementation of its own, so that is the oracle's restatement of it (all threads).
@@ -58,24 +67,31 @@ def dist_env():
 
 
 PHASE_NCU_NAME = {"nbr_build": "k_nbr_build", "pass1": "k_pass1", "pass2_integrate": "k_pass2"}
+PROFILE_JSON = os.path.join(ROOT, "profiles", "neighbour_kernels.json")
 
 
-def ncu_summary(key: str) -> dict:
-    """A per-kernel figure from the committed ncu summary of this workload (a line
-    `key: {json}`): traffic_bytes_per_launch (dram__bytes_read.sum + dram__bytes_write.sum),
-    l1_data_pipe_pct (l1tex__data_pipe_lsu_wavefronts, % of peak)."""
-    path = os.path.join(ROOT, "profiles", "neighbour_kernels_large.md")
+def ncu_capture(phase: str, workload: str, shape: dict) -> dict:
+    """The committed ncu capture of a phase's kernel (profiles/neighbour_kernels.json: one
+    record per capture with the kernel, workload and launch shape it was taken at, its DRAM
+    bytes per launch and L1 data-pipe utilisation).  Only a capture taken at the launch shape
+    in effect describes the timed kernel; otherwise the result says why there is none."""
+    name = PHASE_NCU_NAME.get(phase)
+    if not name:
+        return {"reason": f"no ncu capture is kept for phase {phase}"}
     try:
-        for line in open(path):
-            if line.startswith(key + ":"):
-                return json.loads(line.split(":", 1)[1])
-    except (OSError, ValueError):
-        pass
-    return {}
-
-
-def ncu_traffic() -> dict:
-    return ncu_summary("traffic_bytes_per_launch")
+        with open(PROFILE_JSON) as f:
+            caps = json.load(f)["captures"]
+    except (OSError, ValueError, KeyError):
+        return {"reason": "profiles/neighbour_kernels.json missing"}
+    seen = []
+    for c in caps:
+        if not c.get("kernel", "").startswith(name) or c.get("workload") != workload:
+            continue
+        cshape = {k: c.get(k) for k in shape}
+        if cshape == shape:
+            return c
+        seen.append(cshape)
+    return {"reason": f"no capture of {name} on {workload} at {shape} (captured: {seen})"}
 
 
 def peaks():
@@ -245,30 +261,140 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# Flops of one evaluated pair, counted from the pair algebra of the kernels
+# (tmp_sph_gb300/csrc/equation/ns_pair.cuh, Pass1Acc::pair and Pass2Acc::pair; the reference's
+# form is src/equation/ns.cu:99-108 and :206-248).  A fused multiply-add counts 2, a square
+# root or reciprocal 1; the relative position and squared distance (8) are included.
+FLOPS_P1_FLUID = 28   # pass 1, fluid i and fluid j: velocity-divergence term
+FLOPS_P1_WALL = 24    # pass 1, boundary i and fluid j: pressure-extrapolation sums
+FLOPS_P2_FLUID = 45   # pass 2, fluid i and fluid j: continuity, diffusion, pressure, damper, AV
+FLOPS_P2_WALL = 41    # pass 2, fluid i and boundary j (no damper, no viscosity)
+FLOPS_PARTICLE = 35   # per fluid particle and half step: sums to rates, integrator, EOS, hash
+
+
+def pair_counts(st: dict, kh: float, sample: int = 200_000, seed: int = 7) -> dict:
+    """Ordered pairs closer than kh in the state (the pairs the passes evaluate): fluid-fluid
+    and fluid-boundary, estimated from a seeded sample of fluid particles with k-d trees."""
+    from scipy.spatial import cKDTree
+    pos = np.asarray(st["pos"], np.float64)
+    fl = np.asarray(st["type"]) == 1
+    F, B = pos[fl], pos[~fl]
+    rng = np.random.default_rng(seed)
+    sel = F[rng.choice(len(F), min(sample, len(F)), replace=False)]
+    ff = (cKDTree(F).query_ball_point(sel, kh, return_length=True) - 1).mean()
+    fb = cKDTree(B).query_ball_point(sel, kh, return_length=True).mean() if len(B) else 0.0
+    return {"fluid": int(fl.sum()), "ff_pairs": float(ff * len(F)), "fb_pairs": float(fb * len(F)),
+            "ff_per_fluid": float(ff), "fb_per_fluid": float(fb), "sample": len(sel)}
+
+
+def flops_per_step(pc: dict) -> float:
+    """Algorithmic FP32 flops of one full step (two half steps) for the pair counts pc."""
+    half = (pc["ff_pairs"] * (FLOPS_P1_FLUID + FLOPS_P2_FLUID) + pc["fb_pairs"] * FLOPS_P1_WALL
+            + pc["fb_pairs"] * FLOPS_P2_WALL + pc["fluid"] * FLOPS_PARTICLE)
+    return 2.0 * half
+
+
+def fp32_peak(stream) -> dict:
+    """FP32 FMA throughput of this GPU, measured now (sph_measure_fp32_peak, CUDA events)."""
+    import ctypes as C
+    import torch
+    from tmp_sph_gb300 import api
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    blocks = sms * 8
+    sink = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    fl, ms = C.c_double(0), C.c_double(0)
+    api.call("sph_measure_fp32_peak", C.c_void_p(sink.data_ptr()), blocks, 40000, C.byref(fl),
+             C.byref(ms), C.c_void_p(stream.cuda_stream))
+    return {"tflops": fl.value / (ms.value / 1e3) / 1e12, "ms": ms.value, "blocks": blocks,
+            "how": "sph_measure_fp32_peak: 8 independent FMA chains per thread, CUDA events"}
+
+
+def reference_cuda_leg(st: dict, p, versions=(("v4", 1, 10), ("src", 0, 2))) -> dict:
+    """The reference's own CUDA step loops on this GPU, on the same state: its best version
+    (opt_src_v4) and its baseline (src/), from the kernels compiled out of its sources
+    (oracle/_ref, launched by oracle/ref_harness.cu with its launch shapes and thrust sort).
+    A baseline leg like cpu_baseline: none of this library's code runs in it.  The reference
+    kernels implement only the linear EOS, so they run the same geometry and constants with
+    p = cs^2 (rho - rho0)."""
+    import torch
+    try:
+        from oracle import oracle as O
+        from oracle.ref_harness import RefHarness
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"harness not importable: {e}"}
+    P = O.params_like(p)
+    P.eos = 0
+    n = len(st["rho"])
+    out = {}
+    cuda = torch.device("cuda", torch.cuda.current_device())
+    for v, warm, steps in versions:
+        try:
+            H = RefHarness(v)
+        except Exception as e:  # noqa: BLE001
+            out[v] = {"unavailable": str(e).splitlines()[0][:200]}
+            continue
+        H.set_params(P, n)
+        d, s_, w, tmp = H.alloc(st, cuda)
+        H.init_ids(d)
+        H.step(d, s_, w, tmp, warm)
+        H.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.current_stream())
+        H.step(d, s_, w, tmp, steps)
+        e1.record(torch.cuda.current_stream())
+        H.sync()
+        ms = e0.elapsed_time(e1)
+        out[v] = {"value": n * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                  "steps": steps, "warmup": warm}
+        del d, s_, w, tmp
+        torch.cuda.empty_cache()
+    out["note"] = ("reference kernels compiled from its sources for sm_103a, default stream, "
+                   "CUDA events; linear EOS (the only form they implement)")
+    return out
+
+
+def time_run(sol, stream, steps: int) -> tuple[float, int]:
+    """(milliseconds, list rebuilds) of `steps` steps on `stream`, by CUDA events."""
+    import torch
+    r0 = sol.rebuild_count(stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sol.step(steps, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), sol.rebuild_count(stream=stream) - r0
+
+
+def configured_run(sol, stream, st, n: int, n_fluid: int, run_steps: int, steps: int) -> dict:
+    """The configured run on a fresh solver `sol`: the initial state uploaded, all `run_steps`
+    steps timed (the flow develops and the lists are rebuilt more often than in a short window
+    from rest), then `steps` more steps of the developed flow timed alone."""
+    sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
+    ms, rb = time_run(sol, stream, run_steps)
+    ms2, rb2 = time_run(sol, stream, steps)
+    return {"run": {"steps": run_steps, "ms_per_step": ms / run_steps,
+                    "value": n * run_steps / (ms / 1e3),
+                    "fluid_value": n_fluid * run_steps / (ms / 1e3),
+                    "list_rebuilds": rb, "half_steps": 2 * run_steps},
+            "developed_flow": {"after_steps": run_steps, "steps": steps,
+                               "ms_per_step": ms2 / steps, "value": n * steps / (ms2 / 1e3),
+                               "fluid_value": n_fluid * steps / (ms2 / 1e3),
+                               "list_rebuilds": rb2, "half_steps": 2 * steps},
+            "device_error_flags": sol.error_flags(stream=stream)}
+
+
 def set_lanes(sol, args) -> None:
-    """Lanes per particle of the two list passes: --lanes for both, else --pass1-lanes (0: the
-    precision's default) and --pass2-lanes."""
+    """Lanes per particle of list pass 1 (--pass1-lanes; 0: the precision's default)."""
     from tmp_sph_gb300 import api
-    if args.lanes is not None:
-        sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, args.lanes)
-    else:
-        sol.set_option(api.SPH_OPT_PASS1_LANES, args.pass1_lanes)
-        sol.set_option(api.SPH_OPT_PASS2_LANES, args.pass2_lanes)
-
-
-def set_subcell(sol, args) -> None:
-    from tmp_sph_gb300 import api
-    if args.subcell is not None:
-        sol.set_option(api.SPH_OPT_SUBCELL_ORDER, args.subcell)
+    sol.set_option(api.SPH_OPT_PASS1_LANES, args.pass1_lanes)
 
 
 def lanes_in_effect(sol) -> dict:
     """Launch shape of the neighbour kernels in effect (defaults resolved)."""
     from tmp_sph_gb300 import api
-    return {"lanes_per_particle_pass1_pass2": [sol.get_option(api.SPH_OPT_PASS1_LANES),
-                                               sol.get_option(api.SPH_OPT_PASS2_LANES)],
-            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS),
-            "subcell_order": sol.get_option(api.SPH_OPT_SUBCELL_ORDER)}
+    return {"lanes_per_particle_pass1_pass2": [sol.get_option(api.SPH_OPT_PASS1_LANES), 1],
+            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS)}
 
 
 def config_block(args, p, n, lanes=None):
@@ -278,83 +404,142 @@ def config_block(args, p, n, lanes=None):
             "parallelism": f"replicas x{int(os.environ.get('WORLD_SIZE', '1'))}",
             "l2": "state larger than L2 (no flush needed)",
             "neighbour_list_skin_over_kh": args.skin / 1000.0,
-            "graph_mode": args.graph_mode, "pairs": args.pairs,
+            "graph_mode": args.graph_mode,
             **(lanes or {}), "adaptive_skin": args.adaptive_skin}
 
 
+def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup: int,
+                  run_steps: int = 0, ws: int = 1, rank: int = 0, clocks=None) -> dict:
+    """Config 4: n_inst independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water blocks
+    of width U[0.2, 0.6] m and height U[0.15, 0.45] m drawn from the seed) advanced together by
+    one batched solver: every half step of all instances is the same few launches, replayed as
+    one CUDA graph.  With ws > 1 ranks the one batch is split by instance (contiguous blocks of
+    about equal particle counts, replicas.partition) and each rank advances its share: no
+    collective on the data path, strong scaling.  `steps` timed after `warmup`, then, with
+    run_steps, the configured run from rest (run_steps steps timed) continued into the
+    developed flow."""
+    import torch
+    from tmp_sph_gb300 import api, cases, replicas, solver as S
+    states, p = cases.batch(n_inst, seed=20240611)
+    counts = [len(st["rho"]) for st in states]
+    lo, hi = replicas.partition(counts, ws)[rank]
+    mine = states[lo:hi]
+    n = sum(counts[lo:hi])
+    n_all = sum(counts)
+    fluid = [int((st["type"] == 1).sum()) for st in states]
+    n_fluid_all = sum(fluid)
+    tuned = None
+    skin = args.skin
+    if args.autotune:
+        from tmp_sph_gb300 import autotune
+        tuned = autotune.tune(p, mine, precision=precision)
+        skin = tuned["skin_permille"]
+    def make_solver():
+        v = S.Solver(p, n, precision=precision)
+        v.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+        v.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+        set_lanes(v, args)
+        v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
+        if tuned:
+            from tmp_sph_gb300 import autotune
+            autotune.apply(v, tuned)
+        return v
+
+    sol = make_solver()
+    lanes = lanes_in_effect(sol)
+    sol.upload_instances(mine, stream=stream)
+    sol.step(warmup, stream=stream)
+    torch.cuda.synchronize()
+    r0 = sol.rebuild_count(stream=stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = clocks if clocks is not None else _NoClock()
+    with clk:
+        replicas.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        sol.step(steps, stream=stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        replicas.barrier()
+    ms = replicas.reduce_max(ev0.elapsed_time(ev1))
+    rebuilds = sol.rebuild_count(stream=stream) - r0
+    out = {"value": n_all * steps / (ms / 1e3), "unit": UNIT,
+           "fluid_value": n_fluid_all * steps / (ms / 1e3), "ms_per_step": ms / steps,
+           "steps": steps, "warmup": warmup,
+           "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+                     "fp64": "f64"}[precision],
+           "config": {"workload": f"dam_break_batch{n_inst}_{precision}", "instances": n_inst,
+                      "instances_this_rank": hi - lo, "particles": n_all,
+                      "particles_this_rank": n, "fluid_particles": n_fluid_all,
+                      "fluid_min": min(fluid), "fluid_max": max(fluid),
+                      "parallelism": (f"instances split over {ws} ranks (no collective)"
+                                      if ws > 1 else "one batched solver"),
+                      "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
+                      "neighbour_list_skin_over_kh": skin / 1000.0,
+                      "graph_mode": args.graph_mode, **lanes},
+           "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * steps},
+           "gpu_launches": count_launches(sol_cells_batch(p, n_inst, skin), 2 * steps,
+                                          rebuilds, args.graph_mode),
+           "autotune": None}
+    if tuned:
+        from tmp_sph_gb300 import autotune
+        out["autotune"] = autotune.summary(tuned)
+    flags = sol.error_flags(stream=stream)
+    sol.close()
+    if run_steps > 0:
+        sol = make_solver()
+        sol.upload_instances(mine, stream=stream)
+        ms_run, rb_run = time_run(sol, stream, run_steps)
+        ms_run = replicas.reduce_max(ms_run)
+        ms_dev, rb_dev = time_run(sol, stream, steps)
+        ms_dev = replicas.reduce_max(ms_dev)
+        out["configured_run"] = {"steps": run_steps, "ms_per_step": ms_run / run_steps,
+                                 "value": n_all * run_steps / (ms_run / 1e3),
+                                 "list_rebuilds": rb_run, "half_steps": 2 * run_steps}
+        out["developed_flow"] = {"after_steps": run_steps, "steps": steps,
+                                 "ms_per_step": ms_dev / steps,
+                                 "value": n_all * steps / (ms_dev / 1e3),
+                                 "list_rebuilds": rb_dev, "half_steps": 2 * steps}
+        flags |= sol.error_flags(stream=stream)
+        sol.close()
+    out["device_error_flags"] = flags
+    return out
+
+
+class _NoClock:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+    def summary(self):
+        return None
+
+
 def run_batch(args):
-    """--case batchN: N independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water blocks of
-    width U[0.2, 0.6] m and height U[0.15, 0.45] m) advanced together by one batched solver.
-    Device-resident throughput only (all instances' particles per second)."""
+    """--case batchN: the batched solver alone (batch_measure), one JSON line."""
     import torch
     import torch.distributed as dist
-    from tmp_sph_gb300 import api, build, cases, replicas, solver as S
+    from tmp_sph_gb300 import build
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
     n_inst = int(args.case[5:] or 64)
-    # weak scaling: every rank advances its own batch of n_inst instances (its own seed)
-    states, p = cases.batch(n_inst, seed=20240611 + 1009 * rank)
-    n = sum(len(st["rho"]) for st in states)
     stream = torch.cuda.Stream()
-    tuned = None
-    if args.autotune:
-        from tmp_sph_gb300 import autotune
-        tuned = autotune.tune(p, states, precision=args.precision)
-        args.skin = tuned["skin_permille"]
-    sol = S.Solver(p, n, precision=args.precision)
-    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
-    sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
-    sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
-    set_lanes(sol, args)
-    set_subcell(sol, args)
-    sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
-    if tuned:
-        autotune.apply(sol, tuned)
-    lanes = lanes_in_effect(sol)
-    sol.upload_instances(states, stream=stream)
-    sol.step(args.warmup, stream=stream)
-    torch.cuda.synchronize()
-    r0 = sol.rebuild_count(stream=stream)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(gpu_uuid(local)) as clk:
-        replicas.barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        sol.step(args.steps, stream=stream)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        replicas.barrier()
-    ms = replicas.reduce_max(ev0.elapsed_time(ev1))
-    n_job = int(replicas.reduce_sum(n))
-    rebuilds = sol.rebuild_count(stream=stream) - r0
-    flags = sol.error_flags(stream=stream)
-    sol.close()
-    fluid = [int((st["type"] == 1).sum()) for st in states]
-    line = {
-        "metric": METRIC, "value": n_job * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
-                  "fp64": "f64"}[args.precision],
-        "data": "synthetic (seeded dam-break generator)",
-        "config": {"workload": f"dam_break_batch{n_inst}_{args.precision}",
-                   "instances_per_gpu": n_inst, "particles": n_job, "particles_rank0": n,
-                   "fluid_min": min(fluid), "fluid_max": max(fluid),
-                   "parallelism": f"instances x{ws} (independent batches, no collective)",
-                   "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
-                   "neighbour_list_skin_over_kh": args.skin / 1000.0,
-                   "graph_mode": args.graph_mode,
-                   **lanes},
-        "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps},
-        "autotune": autotune.summary(tuned) if tuned else None,
-        "gpu_launches": count_launches(sol_cells_batch(p, n_inst, args.skin), 2 * args.steps,
-                                       rebuilds, args.graph_mode),
-        "clocks": clk.summary(),
-        "device_error_flags": flags,
-    }
+    clk = ClockSampler(gpu_uuid(local))
+    b = batch_measure(n_inst, args.precision, args, stream, args.steps, args.warmup,
+                      run_steps=args.run_steps, ws=ws, rank=rank, clocks=clk)
+    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_step"],
+            "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak",
+            "vs_baseline": None, "dtype": b["dtype"],
+            "data": "synthetic (seeded dam-break generator)", "config": b["config"],
+            **{k: v for k, v in b.items() if k not in ("value", "ms_per_step", "dtype", "config",
+                                                      "steps", "warmup", "unit")},
+            "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -379,6 +564,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--run-steps", type=int, default=1000,
+                    help="steps of the configured run timed from rest (0: skip that block)")
+    ap.add_argument("--batch-instances", type=int, default=64,
+                    help="instances of the batched block of the default line (0: skip it)")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip timing the reference's own CUDA versions")
     ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
                     help="rebuild kernels of the step graph under conditional nodes, or launched "
                          "every half step and returning at once when the lists are kept")
@@ -387,19 +578,10 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="pick threads per block, particles per thread and skin with the "
                          "autotuner first (overrides --skin)")
-    ap.add_argument("--pairs", type=int, default=0, choices=[0, 1],
-                    help="two particles per thread over a union neighbour list (FP32, FP64)")
-    ap.add_argument("--lanes", type=int, default=None, choices=[1, 2, 4, 8, 16],
-                    help="lanes per particle in both neighbour-list passes")
     ap.add_argument("--pass1-lanes", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
                     help="lanes per particle in list pass 1 (0: 2 in FP32 with a skin, else 1)")
-    ap.add_argument("--pass2-lanes", type=int, default=1, choices=[1, 2, 4, 8, 16],
-                    help="lanes per particle in list pass 2")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
-    ap.add_argument("--subcell", type=int, default=None, choices=[0, 1, 2, 3],
-                    help="order of the particles inside a cell (SPH_OPT_SUBCELL_ORDER; default: "
-                         "the library's)")
     ap.add_argument("--skin", type=int, default=100,
                     help="neighbour-list skin in thousandths of kh (0: rebuild every half step)")
     args = ap.parse_args()
@@ -420,21 +602,25 @@ def main():
     build.build()
     st, p = build_case(args.case)
     n = len(st["rho"])
+    n_fluid = int((st["type"] == 1).sum())
     stream = torch.cuda.Stream()
     tuned = None
     if args.autotune:
         from tmp_sph_gb300 import autotune
         tuned = autotune.tune(p, st, precision=args.precision)
         args.skin = tuned["skin_permille"]
+
+    def configure(v):
+        v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+        v.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+        set_lanes(v, args)
+        v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
+        if tuned:
+            from tmp_sph_gb300 import autotune
+            autotune.apply(v, tuned)
+
     sol = S.Solver(p, n, precision=args.precision)
-    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
-    sol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
-    sol.set_option(api.SPH_OPT_PAIRS, args.pairs)
-    set_lanes(sol, args)
-    set_subcell(sol, args)
-    sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
-    if tuned:
-        autotune.apply(sol, tuned)
+    configure(sol)
     lanes = lanes_in_effect(sol)
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
 
@@ -465,45 +651,6 @@ def main():
     rebuilds = sol.rebuild_count(stream=stream) - rebuilds0
     value = n * ws * args.steps / (ms / 1e3)
 
-    # the same solver rebuilding its lists every half step (no skin): the cost a fast flow
-    # approaches, for comparison with the reuse measured above
-    k0 = min(args.steps, 50)
-    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
-    sol.step(3, stream=stream)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    sol.step(k0, stream=stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms0 = ev0.elapsed_time(ev1)
-    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
-    no_reuse = {"value": n * k0 / (ms0 / 1e3), "ms_per_step": ms0 / k0, "steps": k0}
-
-    # the same workload in the other precisions of the solver (same skin, graph replay)
-    def time_precision(precision: str, steps: int) -> dict:
-        v = S.Solver(p, n, precision=precision)
-        v.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
-        set_lanes(v, args)
-        set_subcell(v, args)
-        v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
-        v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
-        v.step(3, stream=stream)
-        torch.cuda.synchronize()
-        r0 = v.rebuild_count(stream=stream)
-        ev0.record(stream)
-        v.step(steps, stream=stream)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        t = ev0.elapsed_time(ev1)
-        out = {"value": n * steps / (t / 1e3), "ms_per_step": t / steps, "steps": steps,
-               "list_rebuilds": v.rebuild_count(stream=stream) - r0,
-               "device_error_flags": v.error_flags(stream=stream)}
-        v.close()
-        return out
-
-    variants = {prec: time_precision(prec, min(args.steps, 10 if prec == "fp64" else 50))
-                for prec in ("fp32", "mixed", "mixed_comp", "fp64") if prec != args.precision}
-
     # per-kernel device time from CUDA events around every phase, same stream
     prof_steps = min(args.steps, 20)
     sol.set_option(api.SPH_OPT_PROFILE, 1)
@@ -512,6 +659,40 @@ def main():
     prof = sol.profile(reset=True)
     sol.set_option(api.SPH_OPT_PROFILE, 0)
     flags |= sol.error_flags(stream=stream)
+
+    # the same solver rebuilding its lists every half step (no skin): the cost a fast flow
+    # approaches, for comparison with the reuse measured above
+    k0 = min(args.steps, 50)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
+    sol.step(3, stream=stream)
+    ms0, _ = time_run(sol, stream, k0)
+    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, args.skin)
+    no_reuse = {"value": n * k0 / (ms0 / 1e3), "ms_per_step": ms0 / k0, "steps": k0}
+
+    # the configured run (run_steps steps from rest, all timed) and the developed flow after it
+    run = None
+    if args.run_steps > 0:
+        fresh = S.Solver(p, n, precision=args.precision)
+        configure(fresh)
+        run = configured_run(fresh, stream, st, n, n_fluid, args.run_steps, args.steps)
+        fresh.close()
+        flags |= run["device_error_flags"]
+
+    # the same workload in the other precisions of the solver (same skin, graph replay)
+    def time_precision(precision: str, steps: int) -> dict:
+        v = S.Solver(p, n, precision=precision)
+        configure(v)
+        v.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
+        v.step(3, stream=stream)
+        t, rb = time_run(v, stream, steps)
+        out = {"value": n * steps / (t / 1e3), "ms_per_step": t / steps, "steps": steps,
+               "list_rebuilds": rb, "device_error_flags": v.error_flags(stream=stream)}
+        v.close()
+        return out
+
+    variants = {prec: time_precision(prec, min(args.steps, 10 if prec == "fp64" else 50))
+                for prec in ("fp32", "mixed", "mixed_comp", "fp64") if prec != args.precision}
+
     hbm_peak, peak_kind = peaks()
     phases = {}
     for name, v in prof.items():
@@ -521,38 +702,78 @@ def main():
                         "share": v["ms"] / max(1e-9, sum(x["ms"] for x in prof.values())),
                         "kernels": PHASE_KERNEL[name]}
     dom = max(phases, key=lambda k: phases[k]["ms_per_launch"])
-    traffic = ncu_traffic().get(PHASE_NCU_NAME.get(dom, ""))
     dom_ms = phases[dom]["ms_per_launch"]
+    workload = f"dam_break_{args.case}_{args.precision}"
+    shape = {"block_threads": lanes["block_threads"],
+             "lanes_pass1": lanes["lanes_per_particle_pass1_pass2"][0]}
+    cap = ncu_capture(dom, workload, shape)
+    traffic = cap.get("dram_bytes_per_launch")
     roof = {"bound": "hbm", "kernel": PHASE_KERNEL[dom],
             "achieved": phases[dom]["algorithmic_gbs"], "peak": hbm_peak, "unit": "GB/s",
             "frac": phases[dom]["algorithmic_gbs"] / hbm_peak, "peak_kind": peak_kind,
             "traffic": traffic,
-            "traffic_source": "profiles/neighbour_kernels_large.md (ncu, one launch)",
+            "traffic_source": ("profiles/neighbour_kernels.json: " + cap["kernel"] + " at "
+                               + json.dumps(shape)) if traffic else cap.get("reason"),
             "dram_gbs_at_traffic": (traffic / (dom_ms / 1e3) / 1e9) if traffic else None,
             "bytes_per_particle": PHASE_BYTES[dom],
-            "l1_data_pipe_pct": ncu_summary("l1_data_pipe_pct").get(PHASE_NCU_NAME.get(dom, "")),
+            "l1_data_pipe_pct": cap.get("l1_data_pipe_pct"),
             "note": "the neighbour kernels are issue- or L1-throughput bound (sparse gather "
                     "of neighbour data), not HBM bound; frac is algorithmic bytes over the "
                     "measured copy bandwidth"}
+
+    # FP32 arithmetic roofline: flops of the evaluated pairs (counted at the initial state)
+    # over the FP32 FMA peak measured on this GPU now
+    fp32 = None
+    try:
+        pc = pair_counts(st, float(p.kh))
+        f_step = flops_per_step(pc)
+        pk = fp32_peak(stream)
+        ach = f_step * (value / ws / n) / 1e12
+        fp32 = {"bound": "fp32", "achieved": ach, "peak": pk["tflops"], "unit": "TFLOP/s",
+                "frac": ach / pk["tflops"], "peak_kind": "measured (this run)",
+                "flops_per_step": f_step, "flops_per_particle_step": f_step / n,
+                "pairs": pc, "peak_how": pk["how"],
+                "flops_per_pair": {"pass1_fluid": FLOPS_P1_FLUID, "pass1_boundary": FLOPS_P1_WALL,
+                                   "pass2_fluid": FLOPS_P2_FLUID, "pass2_boundary": FLOPS_P2_WALL,
+                                   "per_fluid_particle_half_step": FLOPS_PARTICLE}}
+    except Exception as e:  # noqa: BLE001
+        fp32 = {"unavailable": str(e)[:200]}
 
     # end to end through the C ABI with pinned host buffers
     hst = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory()
            for k in ("pos", "vel", "rho", "p", "type")}
     hnp = {k: v.numpy() for k, v in hst.items()}
-    e2e_sol = sol
-    e2e_sol.set_option(api.SPH_OPT_USE_GRAPH, 1)
-    e2e_sol.step_host(hnp, 1, stream=stream)  # warm
+    sol.set_option(api.SPH_OPT_USE_GRAPH, 1)
+    sol.step_host(hnp, 1, stream=stream)  # warm
     for k in hst:
         hnp[k][...] = st[k]
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        e2e_sol.step_host(hnp, 1, stream=stream)
+        sol.step_host(hnp, 1, stream=stream)
     e2e_s = time.perf_counter() - t0
     barrier()
     e2e_val = n * ws * args.e2e_steps / e2e_s
     h2d = n * (12 + 12 + 4 + 4 + 4)
     d2h = n * (12 + 12 + 4 + 4)
+    flags |= sol.error_flags(stream=stream)
+    sol.close()
+
+    # the spec comparison on one line: batched mixed precision (config 4) against the
+    # plain FP32 single-instance drop-in above
+    batched = None
+    if args.batch_instances > 0 and ws == 1:
+        batched = batch_measure(args.batch_instances, "mixed", args, stream, args.steps,
+                                args.warmup, run_steps=args.run_steps,
+                                clocks=ClockSampler(gpu_uuid(local)))
+        batched["vs_plain_fp32"] = batched["value"] / value
+
+    ref_cuda = None
+    if rank == 0 and ws == 1 and not args.no_reference_cuda:
+        ref_cuda = reference_cuda_leg(st, p)
+        for v in ("v4", "src"):
+            if isinstance(ref_cuda.get(v), dict) and "value" in ref_cuda[v]:
+                ref_cuda[v]["this_over_reference"] = value / ref_cuda[v]["value"]
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -567,24 +788,28 @@ def main():
                   "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
         "config": config_block(args, p, n, lanes),
+        "fluid_particle_steps_per_s": n_fluid * ws * args.steps / (ms / 1e3),
         "hbm_gbs_algorithmic": value / ws * b_alg / 1e9,
         "hbm_frac_step_algorithmic": value / ws * b_alg / 1e9 / hbm_peak,
         "bytes_per_particle_step": b_alg,
         "roofline": roof,
+        "roofline_fp32": fp32,
         "phases": phases,
         "cpu_baseline": cpu,
+        "reference_cuda": ref_cuda,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
         "gpu_launches": count_launches(sol_cells, 2 * args.steps, rebuilds, args.graph_mode),
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
                           "skin_permille": args.skin},
+        "configured_run": run,
         "rebuild_every_half_step": no_reuse,
+        "batched": batched,
         "autotune": autotune.summary(tuned) if tuned else None,
         "precision_variants": variants,
         "clocks": clk.summary(),
         "device_error_flags": flags,
     }
-    sol.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

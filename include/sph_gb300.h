@@ -171,6 +171,14 @@ const char* sph_status_string(int status);
 /* Library version string. */
 const char* sph_version(void);
 
+/* Measured FP32 arithmetic peak (no reference counterpart: the denominator of the solver's
+ * FP32 roofline fraction).  Launches blocks x 256 threads of independent fused multiply-add
+ * chains, `iters` rounds of 128 FMAs each, once to warm up and once timed by CUDA events on
+ * `stream`; *flops receives the flops of the timed launch, *ms its duration.  sink: device
+ * buffer of blocks * 256 floats (overwritten).  Synchronises the stream. */
+int sph_measure_fp32_peak(float* sink, int blocks, int iters, double* flops, double* ms,
+                          void* stream);
+
 /* ---------------------------------------------------------------- drop-in functions */
 /* calcHash (src/header/mesh.cuh:20, src/lib/mesh.cu:26-70): hash[i] = cell of pos[3i..3i+2],
  * index[i] = i.  The cell coordinate is floorf((p - grid_min)/cell_size) in IEEE FP32,
@@ -257,27 +265,21 @@ typedef struct sph_ctx sph_ctx;
                                     other precisions */
 #define SPH_OPT_PARTICLES_PER_THREAD 10  /* particles each thread of the neighbour kernels
                                     handles, grid-stride (1..64, default 1) */
-#define SPH_OPT_PAIRS 11  /* 1: the neighbour kernels take two consecutive particles per thread
-                             over the union of their neighbour lists, gathering each neighbour
-                             record once for both (FP32 and FP64; ignored in mixed precision) */
+/* 11 is not used (it selected a two-particles-per-thread mode, measured slower and removed) */
 #define SPH_OPT_ADAPTIVE_SKIN 13  /* 1 (default): each list rebuild picks the skin of the next
                              lists, between 0.02 and SPH_OPT_SKIN_PERMILLE, from how long the
                              last lists lasted (tight lists for slow flow, wide for fast); 0: the
                              lists always use SPH_OPT_SKIN_PERMILLE */
-#define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in both list passes:
-                             1 (one thread per particle), 2, 4, 8 or 16 (a group of lanes shares a
-                             particle's list and reduces its sums; not with SPH_OPT_PAIRS); 0:
-                             the defaults below.  With groups in either pass the lists store
-                             their entries interleaved in windows of eight (a change rebuilds
-                             them) */
-#define SPH_OPT_PASS1_LANES 14  /* the same for list pass 1 (density sums) alone; default (0):
-                             2 in FP32 with a list skin, else 1 */
-#define SPH_OPT_PASS2_LANES 15  /* the same for list pass 2 (forces + integrator) alone;
-                             default 1 */
-#define SPH_OPT_SUBCELL_ORDER 16  /* order of the particles inside a cell of the resident
-                             state: 0 as uploaded (original index), 1 eight bins along x, 2 by
-                             octant, 3 Morton order of a 4x4x4 sub-grid (the sort key carries
-                             3 or 6 more bits); a change rebuilds the cell and neighbour lists */
+#define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in list pass 1 (the
+                             wall extrapolation and velocity divergence): 1 (one thread per
+                             particle), 2, 4, 8 or 16 (a group of lanes shares a particle's list
+                             and reduces its sums); 0 (default): 2 in FP32 with a list skin,
+                             else 1.  With groups the lists store their entries interleaved in
+                             windows of eight (a change rebuilds them).  Pass 2 runs one lane
+                             per particle (groups were slower there at every size measured) */
+#define SPH_OPT_PASS1_LANES 14  /* the same as SPH_OPT_LANES_PER_PARTICLE */
+/* 15 is not used (it selected lane groups in pass 2, removed) */
+
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
 #define SPH_PREC_FP32  0  /* FP32 state and arithmetic, the reference's precision (default) */

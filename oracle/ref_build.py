@@ -21,7 +21,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE = "/root/reference"
+# Where the reference's source tree is: SPH_REFERENCE_DIR, else the checkout this recipe was
+# written against.  Nothing that runs on a GPU host reads it (the fatbins built here travel).
+REFERENCE = os.environ.get("SPH_REFERENCE_DIR", "/root/reference")
 FATBIN = os.path.join(OUT, "ref_src.fatbin")
 HARNESS = os.path.join(OUT, "libref_harness.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -52,6 +54,15 @@ def nvcc() -> str:
 
 def reference_present() -> bool:
     return os.path.isdir(os.path.join(REFERENCE, "src", "equation"))
+
+
+def require_reference() -> str:
+    """The reference tree, or a clear error naming the variable that locates it."""
+    if not reference_present():
+        raise FileNotFoundError(
+            f"reference sources not found at {REFERENCE} (expected src/equation there); "
+            "set SPH_REFERENCE_DIR to the ZZPHUB/tmp_sph checkout")
+    return REFERENCE
 
 
 def build_fatbin(force: bool = False, version: str = "src") -> str | None:

@@ -1,6 +1,5 @@
-"""GPU tests of the lane-group list passes (SPH_OPT_LANES_PER_PARTICLE, SPH_OPT_PASS1_LANES,
-SPH_OPT_PASS2_LANES): G lanes share one particle's neighbour list and reduce their partial sums
-with shuffles.  Every G reads the list the one-lane build writes; the sums associate
+"""GPU tests of the lane-group list pass 1 (SPH_OPT_LANES_PER_PARTICLE = SPH_OPT_PASS1_LANES):
+G lanes share one particle's neighbour list and reduce their partial sums with shuffles.  Every G reads the list the one-lane build writes; the sums associate
 differently, so the results match the oracle and the one-lane kernels to FP32 rounding; for a
 fixed G they are deterministic and independent of the block size, of graph replay, and of
 batching."""
@@ -74,23 +73,6 @@ def test_lanes_close_to_one_lane(sphlib, cuda, report, lanes):
     assert a["flags"] == 0 and b["flags"] == 0
 
 
-@pytest.mark.parametrize("g1,g2", [(4, 1), (1, 4), (2, 8)])
-def test_per_pass_lanes(sphlib, oracle, cuda, report, g1, g2):
-    """Each pass takes its own G over the same list: against the oracle, and a switch of G
-    between steps keeps the lists (no extra rebuild) and continues the run."""
-    from tmp_sph_gb300 import api
-    st, p = small()
-    P = oracle.params_like(p)
-    opts = {api.SPH_OPT_PASS1_LANES: g1, api.SPH_OPT_PASS2_LANES: g2}
-    out = run(st, p, 20, 1, opts=opts)
-    ref = oracle.run(P, st, 20)
-    assert out["flags"] == 0
-    e = field_errors(out, ref, st)
-    for k, v in e.items():
-        report(f"pass lanes {g1}/{g2}, 20 steps {k}", v, 2e-4)
-    assert all(v < 2e-4 for v in e.values()), e
-
-
 def test_lanes_switch(sphlib, cuda, report):
     """Lane groups read interleaved list windows: turning groups on or off rebuilds the lists at
     the next half step; changing G while groups stay on keeps them (the rebuilds follow a run
@@ -99,26 +81,28 @@ def test_lanes_switch(sphlib, cuda, report):
     from tmp_sph_gb300 import api, solver as S
     st, p = small()
     s = torch.cuda.Stream()
-    segments = ((None, 0), (api.SPH_OPT_PASS1_LANES, 4), (api.SPH_OPT_PASS2_LANES, 2),
-                (api.SPH_OPT_LANES_PER_PARTICLE, 1), (api.SPH_OPT_PASS1_LANES, 0))
+    # (option, G, whether the list windows change)
+    segments = ((None, 0, False), (api.SPH_OPT_PASS1_LANES, 4, True),
+                (api.SPH_OPT_PASS1_LANES, 2, False), (api.SPH_OPT_LANES_PER_PARTICLE, 1, True),
+                (api.SPH_OPT_PASS1_LANES, 0, True))
     counts = {}
-    for keep_pass2 in (False, True):
+    for keep_g in (False, True):
         with S.Solver(p, len(st["rho"])) as sol:
             sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, 1)
             sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
-            counts[keep_pass2] = []
-            for opt, g in segments:
+            counts[keep_g] = []
+            for opt, g, windows in segments:
                 before = sol.rebuild_count(stream=s)
-                if opt is not None and not (keep_pass2 and opt == api.SPH_OPT_PASS2_LANES):
+                # the run with keep_g skips the change of G that keeps the windows
+                if opt is not None and not (keep_g and not windows):
                     sol.set_option(opt, g)
                 sol.step(1, stream=s)
-                if opt in (api.SPH_OPT_PASS1_LANES, api.SPH_OPT_LANES_PER_PARTICLE):
-                    assert sol.rebuild_count(stream=s) > before, (opt, g)  # windows changed
+                if windows:
+                    assert sol.rebuild_count(stream=s) > before, (opt, g)
                 sol.step(3, stream=s)
-                counts[keep_pass2].append(sol.rebuild_count(stream=s))
-            if not keep_pass2:
+                counts[keep_g].append(sol.rebuild_count(stream=s))
+            if not keep_g:
                 assert sol.get_option(api.SPH_OPT_PASS1_LANES) == 2  # the FP32 default
-                assert sol.get_option(api.SPH_OPT_PASS2_LANES) == 1
                 out = sol.download(stream=s)
             assert sol.error_flags(stream=s) == 0
     assert counts[False] == counts[True], counts
@@ -131,13 +115,12 @@ def test_lanes_switch(sphlib, cuda, report):
 
 def test_lanes_defaults(sphlib, cuda):
     """Pass 1 takes two lanes per particle in FP32 while the lists have a skin, one without a
-    skin and in the other precisions; pass 2 one lane in all."""
+    skin and in the other precisions."""
     from tmp_sph_gb300 import api, solver as S
     st, p = small()
     for prec, want in (("fp32", 2), ("mixed", 1), ("mixed_comp", 1), ("fp64", 1)):
         with S.Solver(p, len(st["rho"]), precision=prec) as sol:
             assert sol.get_option(api.SPH_OPT_PASS1_LANES) == want, prec
-            assert sol.get_option(api.SPH_OPT_PASS2_LANES) == 1, prec
             sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
             assert sol.get_option(api.SPH_OPT_PASS1_LANES) == 1, prec
 
@@ -236,10 +219,12 @@ def test_lanes_option_checked(sphlib):
                 sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, bad)
         for good in (0, 1, 2, 4, 8, 16):
             sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, good)
-        for opt in (api.SPH_OPT_PASS1_LANES, api.SPH_OPT_PASS2_LANES):
-            with pytest.raises(api.SphError):
-                sol.set_option(opt, 5)
-            sol.set_option(opt, 4)
-            assert sol.get_option(opt) == 4
         with pytest.raises(api.SphError):
-            sol.set_option(api.SPH_OPT_PASS2_LANES, 0)  # pass 2 has no precision default
+            sol.set_option(api.SPH_OPT_PASS1_LANES, 5)
+        sol.set_option(api.SPH_OPT_PASS1_LANES, 4)
+        assert sol.get_option(api.SPH_OPT_PASS1_LANES) == 4
+        assert sol.get_option(api.SPH_OPT_LANES_PER_PARTICLE) == 4
+        # the retired options (pair mode 11, pass-2 lane groups 15) are refused
+        for retired in (11, 15):
+            with pytest.raises(api.SphError):
+                sol.set_option(retired, 1)

@@ -371,50 +371,6 @@ def test_obstacle_case_matches_oracle(sphlib, oracle, cuda, report):
     assert np.array_equal(out["pos"][rig], st["pos"][rig])
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_pair_mode(sphlib, oracle, cuda, report, precision):
-    """Two particles per thread over the union of their lists: the same pairs as one particle
-    per thread; a particle's neighbours come in the same order unless its pair straddles two
-    cells, so results agree to rounding; an overflowing union walks the cells per particle,
-    which matches the walking passes bit for bit.  Odd particle counts leave a pair of one."""
-    from tmp_sph_gb300 import api, cases
-    from gpu_util import perturbed
-    from test_precision_gpu import run_prec, errors
-    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    st = perturbed(st, vamp=1.0, ramp=0.005)
-    odd = {k: (v[:-1] if isinstance(v, np.ndarray) and len(v) == len(st["rho"]) else v)
-           for k, v in st.items()}
-    assert len(odd["rho"]) % 2 == 1
-    for s in (st, odd):
-        one = run_prec(s, p, 8, precision)
-        two = run_prec(s, p, 8, precision, {api.SPH_OPT_PAIRS: 1})
-        assert one["flags"] == 0 and two["flags"] == 0
-        e = errors(two["f64"], one["f64"], s)
-        for k, v in e.items():
-            report(f"pairs vs single {precision} n={len(s['rho'])} {k}", v, 1e-4)
-        assert all(v < 1e-4 for v in e.values()), e
-        assert two["rebuilds"] >= 2
-    over = run_prec(st, p, 4, precision, {api.SPH_OPT_PAIRS: 1, api.SPH_OPT_NEIGHBOR_CAP: 8,
-                                          api.SPH_OPT_SKIN_PERMILLE: 0})
-    assert over["flags"] & api.SPH_FLAG_NEIGHBOR_OVERFLOW
-    walk0 = run_prec(st, p, 4, precision, {api.SPH_OPT_NEIGHBOR_LIST: 0,
-                                           api.SPH_OPT_SKIN_PERMILLE: 0})
-    for k in ("pos", "vel", "rho", "p"):
-        assert np.array_equal(over[k], walk0[k]), k
-
-
-def test_pair_mode_matches_oracle(sphlib, oracle, cuda, report):
-    from tmp_sph_gb300 import api, cases
-    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
-    out, flags = run_opts(st, p, 20, {api.SPH_OPT_PAIRS: 1})
-    ref = oracle.run(oracle.params_like(p), st, 20)
-    assert flags == 0
-    e = field_errors(out, ref, st)
-    for k, v in e.items():
-        report(f"pairs 20 steps vs oracle {k}", v, 2e-4)
-    assert all(v < 2e-4 for v in e.values()), e
-
-
 def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):
     """The lists are rebuilt when the box of all displacements since the last build has a
     half-diagonal beyond skin/2: a block carried at 1 m/s past static walls keeps them for

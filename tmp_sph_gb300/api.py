@@ -43,12 +43,9 @@ SPH_OPT_CONDITIONAL_GRAPH = 7
 SPH_OPT_PRECISION = 8
 SPH_OPT_BLOCK_THREADS = 9
 SPH_OPT_PARTICLES_PER_THREAD = 10
-SPH_OPT_PAIRS = 11
 SPH_OPT_LANES_PER_PARTICLE = 12
 SPH_OPT_PASS1_LANES = 14
-SPH_OPT_PASS2_LANES = 15
 SPH_OPT_ADAPTIVE_SKIN = 13
-SPH_OPT_SUBCELL_ORDER = 16
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
               "mixed_comp": SPH_PREC_MIXED_COMP}
@@ -156,6 +153,8 @@ _PROTOS = {
     "sph_params_to_reference": (_I, [_PP, C.POINTER(SphRefSimParams)]),
     "sph_status_string": (C.c_char_p, [_I]),
     "sph_version": (C.c_char_p, []),
+    "sph_measure_fp32_peak": (_I, [_P, _I, _I, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   _P]),
     "sph_calc_hash": (_I, [_PP, _P, _P, _P, _I, _P]),
     "sph_sort_scratch_bytes": (_I, [_I, C.POINTER(C.c_size_t)]),
     "sph_sort_particles": (_I, [_P, _P, _I, _I, _P, C.c_size_t, _P]),

@@ -63,7 +63,6 @@ def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> d
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
     sol.set_option(api.SPH_OPT_PASS1_LANES, lanes)
-    sol.set_option(api.SPH_OPT_PASS2_LANES, 1)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
     sol.step(1, stream=stream)  # warm: first launches of this shape
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
@@ -124,7 +123,6 @@ def apply(sol, best: dict) -> None:
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, best["threads"])
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, best["ppt"])
     sol.set_option(api.SPH_OPT_PASS1_LANES, best.get("lanes", 0))
-    sol.set_option(api.SPH_OPT_PASS2_LANES, 1)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, best["skin_permille"])
 
 

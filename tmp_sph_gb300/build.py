@@ -34,6 +34,7 @@ SOURCES = [
     "io/dam_break.cpp",
     "io/probes.cu",
     "io/vtk.cpp",
+    "io/peak.cu",
 ]
 HEADERS = ["header/sph_device.cuh", "header/sph_internal.h", "equation/ns_pair.cuh"]
 

@@ -334,237 +334,6 @@ k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     reduce_disp_box(box, disp, s_box);
 }
 
-// ---------------------------------------------------------------- particle pairs
-// Pair mode (KParams::pairs, FP32 and FP64): a thread handles the two consecutive sorted
-// particles 2c and 2c+1 (a "pair", usually in one cell) over the union of their neighbour
-// lists, so each listed record is gathered once for both.  The passes are limited by those
-// gathers (one L1 data-stage wavefront per distinct line a warp instruction touches), and the
-// union of two consecutive particles' lists is about 1.38 times one list: 31% fewer gathers
-// for up to twice the pair bodies per gather.  The list is indexed by pair (warp-interleaved
-// over pairs); its slots hold every j within the list cutoff of either particle, in walk
-// order; each particle tests r < kh (and j != itself) on every slot.  A pair whose union
-// overflowed walks the cells for each of its two particles.
-
-template <class P>
-__device__ __forceinline__ void nbr_build_pair(const KParamsT<typename P::T>& k,
-                                               const vec4_t<typename P::T>* __restrict__ X,
-                                               const unsigned* __restrict__ keys,
-                                               const int* __restrict__ cs, const NbrList& nl,
-                                               int walls_all, unsigned* err, int4* stage, int c) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    const int i0 = 2 * c, i1 = 2 * c + 1;
-    const V p0 = X[i0];
-    const V p1 = i1 < k.n ? X[i1] : p0;
-    if (nl.xb) {
-        nl.xb[i0] = as_float4(p0);
-        if (i1 < k.n) nl.xb[i1] = as_float4(p1);
-    }
-    // particles outside the neighbour search (park_inactive) sort last: take no candidates
-    const bool has1 = i1 < k.n && !inactive_key(k, keys[i1]);
-    if (inactive_key(k, keys[i0])) {
-        nl.count[c] = 0;
-        return;
-    }
-    const bool keep0 = fluid_rec(p0.w) || walls_all;
-    const bool keep1 = has1 && (fluid_rec(p1.w) || walls_all);
-    SlotWriter<false> w(nl.idx + nbr_col(nl, c), nl.cap, stage);
-    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
-    auto visit = [&](int j) {
-        const V pj = ld_pos(X, (size_t)j);
-        const bool fj = fluid_rec(pj.w);
-        bool in = dist2(p0.x - pj.x, p0.y - pj.y, p0.z - pj.z) < cut2 && j != i0 &&
-                  (keep0 || fj);
-        if (has1)
-            in = in || (dist2(p1.x - pj.x, p1.y - pj.y, p1.z - pj.z) < cut2 && j != i1 &&
-                        (keep1 || fj));
-        if (in) w.put(j);
-    };
-    int x0, y0, z0;
-    cell_of_key(k.gx, k.gy, keys[i0], x0, y0, z0);
-    for_each_candidate<false>(k, cs, x0, y0, z0, [&](int j, unsigned) { visit(j); });
-    if (has1 && keys[i1] != keys[i0]) {
-        // the cells around the second particle's cell that the first walk did not cover
-        int x1, y1, z1;
-        cell_of_key(k.gx, k.gy, keys[i1], x1, y1, z1);
-#pragma unroll 1
-        for (int z = z1 - 1; z <= z1 + 1; z++) {
-            if ((unsigned)z >= (unsigned)k.gz) continue;
-#pragma unroll 1
-            for (int y = y1 - 1; y <= y1 + 1; y++) {
-                if ((unsigned)y >= (unsigned)k.gy) continue;
-                const int row = (z * k.gy + y) * k.gx;
-                const bool row_seen = abs(z - z0) <= 1 && abs(y - y0) <= 1;
-#pragma unroll 1
-                for (int x = max(x1 - 1, 0); x <= min(x1 + 1, k.gx - 1); x++) {
-                    if (row_seen && abs(x - x0) <= 1) continue;
-                    const int j0 = max(__ldg(cs + row + x), 0);
-                    const int j1 = min(__ldg(cs + row + x + 1), k.n);  // bounds guard only
-                    for (int j = j0; j < j1; j++) visit(j);
-                }
-            }
-        }
-    }
-    w.flush();
-    nl.count[c] = w.cnt;
-    raise_flags(err, w.cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);
-}
-
-// Iterate a pair's union list: f(j, a, b) with the record of every slot.  Returns false (and
-// calls nothing) when the union overflowed the list.
-template <class P, class F>
-__device__ __forceinline__ bool visit_union(const NbrList& nl,
-                                            const vec4_t<typename P::T>* __restrict__ R, int c,
-                                            F&& f) {
-    using V = vec4_t<typename P::T>;
-    const int cnt = __ldg(nl.count + c);
-    if (cnt > nl.cap) return false;
-    for_each_slot<false>(nl.idx + nbr_col(nl, c), cnt, 0, 1, [&](int j) {
-        V a, b;
-        ld_rec(R, j, a, b);
-        f(j, a, b);
-    });
-    return true;
-}
-
-template <class P, bool WRITE_SUMS>
-__device__ __forceinline__ void pass1_pair(const KParamsT<typename P::T>& k,
-                                           const ParticleSetT<typename P::T>& in,
-                                           const unsigned* __restrict__ keys,
-                                           const int* __restrict__ cs, const NbrList& nl,
-                                           const Pass1OutT<typename P::T>& out,
-                                           float* __restrict__ rhop_sum,
-                                           float* __restrict__ w_sum, int c) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    const int i0 = 2 * c, i1 = 2 * c + 1;
-    const bool has1 = i1 < k.n;
-    Pass1Acc<P> a0, a1;
-    a0.load(in.rec, i0);
-    if (has1) a1.load(in.rec, i1);
-    // particles outside the neighbour search (park_inactive) take no pairs
-    const bool use0 = !inactive_key(k, keys[i0]);
-    const bool use1 = has1 && !inactive_key(k, keys[i1]);
-    auto one = [&](Pass1Acc<P>& acc, int i, int j, const V& a, const V& b) {
-        const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;
-        const T r2 = dist2(dx, dy, dz);
-        if (r2 < k.kh2 && j != i) acc.pair(k, a, b, dx, dy, dz, r2);
-    };
-    const bool listed = visit_union<P>(nl, in.rec, c, [&](int j, const V& a, const V& b) {
-        if (use0) one(a0, i0, j, a, b);
-        if (use1) one(a1, i1, j, a, b);
-    });
-    if (!listed) {
-        visit_records<P, LIST_NONE, 1>(k, cs, keys, nl, in.xyz, in.rec, i0, a0.pi,
-                                   [&](int, const V& aj, const V& vj, T dx, T dy, T dz, T r2) {
-            a0.pair(k, aj, vj, dx, dy, dz, r2);
-        });
-        if (has1)
-            visit_records<P, LIST_NONE, 1>(k, cs, keys, nl, in.xyz, in.rec, i1, a1.pi,
-                                       [&](int, const V& aj, const V& vj, T dx, T dy, T dz,
-                                           T r2) { a1.pair(k, aj, vj, dx, dy, dz, r2); });
-    }
-    a0.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i0);
-    if (has1) a1.template finish<WRITE_SUMS>(k, out, rhop_sum, w_sum, i1);
-}
-
-template <class P, int MODE>
-__device__ __forceinline__ void pass2_pair(const KParamsT<typename P::T>& k, int c,
-                                           const ParticleSetT<typename P::T>& in,
-                                           const unsigned* __restrict__ keys,
-                                           const int* __restrict__ cs, const NbrList& nl,
-                                           const Pass1OutT<typename P::T>& p1,
-                                           float* __restrict__ rho_dt,
-                                           float* __restrict__ vel_dt, int wall_rates,
-                                           const ParticleSetT<typename P::T>& out,
-                                           unsigned* __restrict__ out_hash, unsigned* err,
-                                           DispBox& box) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    const int i0 = 2 * c, i1 = 2 * c + 1;
-    const bool has1 = i1 < k.n;
-    Pass2Acc<P, MODE> a0, a1;
-    a0.load(k, p1, i0, wall_rates);
-    if (has1) a1.load(k, p1, i1, wall_rates);
-    // particles outside the neighbour search (park_inactive) take no pairs
-    a0.active = a0.active && !inactive_key(k, keys[i0]);
-    const bool act1 = has1 && a1.active && !inactive_key(k, keys[i1]);
-    if (a0.active || act1) {
-        auto one = [&](Pass2Acc<P, MODE>& acc, int i, int j, const V& a, const V& b) {
-            const T dx = acc.pi.x - a.x, dy = acc.pi.y - a.y, dz = acc.pi.z - a.z;
-            const T r2 = dist2(dx, dy, dz);
-            if (r2 < k.kh2 && j != i) acc.pair(k, p1, j, a, b, dx, dy, dz, r2);
-        };
-        const bool listed = visit_union<P>(nl, p1.nrec, c, [&](int j, const V& a, const V& b) {
-            if (a0.active) one(a0, i0, j, a, b);
-            if (act1) one(a1, i1, j, a, b);
-        });
-        if (!listed) {
-            if (a0.active)
-                visit_records<P, LIST_NONE, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i0, a0.pi,
-                                           [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
-                                               T r2) { a0.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
-            if (act1)
-                visit_records<P, LIST_NONE, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i1, a1.pi,
-                                           [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
-                                               T r2) { a1.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
-        }
-    }
-    pass2_finish<P, MODE>(k, i0, a0, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
-                          err, box);
-    if (has1)
-        pass2_finish<P, MODE>(k, i1, a1, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
-                              err, box);
-}
-
-template <class P>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_nbr_build_pairs(KParamsT<typename P::T> k, const vec4_t<typename P::T>* __restrict__ X,
-                  const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-                  int walls_all, unsigned* err, const unsigned* gate) {
-    __shared__ int4 s_stage[NS_MAX_THREADS];
-    if (gated_off(gate)) return;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < (k.n + 1) / 2)
-        nbr_build_pair<P>(k, X, keys, cs, nl, walls_all, err, s_stage, c);
-}
-
-template <class P, bool WRITE_SUMS>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_pass1_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
-              const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-              Pass1OutT<typename P::T> out, float* __restrict__ rhop_sum,
-              float* __restrict__ w_sum) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < (k.n + 1) / 2) pass1_pair<P, WRITE_SUMS>(k, in, keys, cs, nl, out, rhop_sum, w_sum, c);
-}
-
-template <class P, int MODE>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_pass2_pairs(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
-              const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-              Pass1OutT<typename P::T> p1, float* __restrict__ rho_dt,
-              float* __restrict__ vel_dt, int wall_rates, ParticleSetT<typename P::T> out,
-              unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    DispBox box;
-    if (c < (k.n + 1) / 2)
-        pass2_pair<P, MODE>(k, c, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash,
-                            err, box);
-    if (MODE == MODE_RATES || disp == nullptr) return;
-    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
-    reduce_disp_box(box, disp, s_box);
-}
-
-// Pair mode applies to the FP32 and FP64 policies (mixed-precision slots carry each
-// neighbour's cell relative to one particle, which a pair of particles in two cells cannot
-// share); the launchers below dispatch on KParams::pairs.
-template <class KP>
-inline dim3 pair_grid(const KP& k) {
-    const long pairs = ((long)k.n + 1) / 2;
-    return dim3((unsigned)((pairs + k.threads - 1) / k.threads > 0 ? (pairs + k.threads - 1) / k.threads : 1));
-}
-
 // Launch shape of a neighbour kernel: KParams::threads per block, KParams::ppt particles per
 // thread.
 template <class KP>
@@ -596,17 +365,6 @@ void pass1_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const unsigned* keys, const int* cs, const NbrList& nl,
                   const Pass1OutT<typename P::T>& o, float* rhop_sum, float* w_sum,
                   cudaStream_t s) {
-    if constexpr (LIST == LIST_PLAIN && !P::kMixed) {  // pair lists keep plain windows
-        if (k.pairs) {
-            if (rhop_sum && w_sum && P::kId == SPH_PREC_FP32)
-                k_pass1_pairs<P, true><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl, o,
-                                                                           rhop_sum, w_sum);
-            else
-                k_pass1_pairs<P, false><<<pair_grid(k), k.threads, 0, s>>>(k, in, keys, cs, nl,
-                                                                            o, nullptr, nullptr);
-            return;
-        }
-    }
     if (k.ppt > 1)
         pass1_launch_gs<P, LIST, true>(k, in, keys, cs, nl, o, rhop_sum, w_sum, s);
     else
@@ -654,13 +412,6 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
                   const Pass1OutT<typename P::T>& p1, float* rho_dt, float* vel_dt,
                   int wall_rates, ParticleSetT<typename P::T> out, unsigned* out_hash,
                   unsigned* err, unsigned* disp, cudaStream_t s) {
-    if constexpr (!P::kMixed) {
-        if (nl && k.pairs) {
-            k_pass2_pairs<P, MODE><<<pair_grid(k), k.threads, 0, s>>>(
-                k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
-            return;
-        }
-    }
     if (k.ppt > 1)
         pass2_launch_gs<P, MODE, true>(k, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
                                        out_hash, err, disp, s);
@@ -671,11 +422,10 @@ void pass2_launch(const KParamsT<typename P::T>& k, const ParticleSetT<typename 
 
 }  // namespace
 
-int nbr_capacity_for(const sph_params& p, double skin, bool pairs) {
-    // 1.5x the particles of a lattice inside the list sphere (of the union of two spheres, about
-    // 1.4 times one, for a pair), rounded up to 16
+int nbr_capacity_for(const sph_params& p, double skin) {
+    // 1.5x the particles of a lattice inside the list sphere, rounded up to 16
     const double r = (double)p.kh * (1.0 + skin) / (double)p.dx;
-    const double lattice = 4.18879020478639 * r * r * r * (pairs ? 1.4 : 1.0);
+    const double lattice = 4.18879020478639 * r * r * r;
     int cap = (int)(1.5 * lattice) + 16;
     cap = (cap + 15) & ~15;
     return cap < 32 ? 32 : cap;
@@ -687,13 +437,6 @@ cudaError_t launch_nbr_build(const KParamsT<typename P::T>& k,
                              const int* cs, const NbrList& nl, int walls_all, unsigned* err,
                              cudaStream_t s, const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    if constexpr (!P::kMixed) {
-        if (k.pairs) {
-            k_nbr_build_pairs<P><<<pair_grid(k), k.threads, 0, s>>>(k, in.xyz, keys, cs, nl,
-                                                                     walls_all, err, gate);
-            return cudaGetLastError();
-        }
-    }
     const dim3 g = ns_grid(k);
     if (k.ppt > 1) {
         if (k.list_win)
@@ -747,8 +490,6 @@ cudaError_t launch_pass2_step(const KParamsT<typename P::T>& k, HalfStep half,
                               ParticleSetT<typename P::T> out, unsigned* out_hash, unsigned* err,
                               unsigned* disp, cudaStream_t s) {
     if (k.n <= 0) return cudaSuccess;
-    if (nl && k.lanes2 > 1)
-        return launch_pass2_groups<P>(k, half, in, keys, cs, *nl, p1, out, out_hash, err, disp, s);
     if (half == HALF_PREDICT)
         pass2_launch<P, MODE_PRED>(k, in, keys, cs, nl, p1, nullptr, nullptr, 0, out, out_hash,
                                    err, disp, s);

@@ -1,4 +1,4 @@
-// ns_groups.cu — the neighbour kernels with a group of G lanes per particle (G = 2, 4, 8, 16).
+// ns_groups.cu — neighbour pass 1 with a group of G lanes per particle (G = 2, 4, 8, 16).
 //
 // Same passes as ns.cu (reference: computeBoundary_Delta_acoustic_D and
 // computeGovering_equationD, src/equation/ns.cu:30-249), same list contents, different
@@ -8,9 +8,10 @@
 // pair of lanes of a group gathers two consecutive entries of one list in one step —
 // neighbouring records, mostly one line — and a warp runs its loop for the longest list of
 // 32/G particles rather than of 32.  Measured on the 4.96M-particle dam break: pass 1 at G = 2
-// 0.756 ms against 0.793 with one lane (the resident default in FP32 with a list skin); pass 2
-// stays one lane (0.849 ms at G = 2 against 0.814: its larger per-pair body on half the
-// particles per warp, and more sums to reduce).
+// 0.756 ms against 0.793 with one lane (the resident default in FP32 with a list skin).  Pass 2
+// runs one lane per particle: with groups it was slower at every G measured (0.849 ms at G = 2
+// against 0.814: its larger per-pair body on half the particles per warp, and more sums to
+// reduce), so that variant was removed.
 //
 // Sums.  Each lane accumulates its share of the pairs; a group reduces them with xor shuffles
 // in a fixed tree, so results are deterministic and independent of the launch shape, but not
@@ -25,8 +26,7 @@
 //
 // Blocks.  A block of T threads owns T consecutive particles and visits them in G rounds of T/G
 // particles (one group each), parking the reduced sums in shared memory; then every thread
-// finishes one particle (pass 1: the record pass 2 gathers; pass 2: the predictor or
-// corrector, the next key and the displacement), so the per-particle epilogue runs on all
+// finishes one particle (the record pass 2 gathers), so the per-particle epilogue runs on all
 // lanes rather than on one lane per group.
 #include <cuda_runtime.h>
 
@@ -198,58 +198,6 @@ k_pass1_g(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     }
 }
 
-// ---------------------------------------------------------------- pass 2 (predictor / corrector)
-template <class P, int MODE, int G>
-__global__ void __launch_bounds__(NS_MAX_THREADS)
-k_pass2_g(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
-          const unsigned* __restrict__ keys, const int* __restrict__ cs, NbrList nl,
-          Pass1OutT<typename P::T> p1, ParticleSetT<typename P::T> out,
-          unsigned* __restrict__ out_hash, unsigned* err, unsigned* disp) {
-    using T = typename P::T;
-    using V = vec4_t<T>;
-    __shared__ T s_sum[4][NS_MAX_THREADS];
-    __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
-    const int nt = (int)blockDim.x, base = (int)blockIdx.x * nt, s = sub_lane<G>();
-#pragma unroll 1
-    for (int r = 0; r < G; r++) {
-        const int loc = r * (nt / G) + (int)threadIdx.x / G;
-        const int i = base + loc;
-        Pass2Acc<P, MODE> acc;
-        if (i < k.n) {
-            acc.load(k, p1, i, 0);
-            if (acc.active)
-                visit_group<P, G, 2>(k, cs, keys, nl, p1.nrec, p1.nrec, i, acc.pi,
-                                     [&](int j, const V& aj, const V& vj, T dx, T dy, T dz,
-                                         T r2) { acc.pair(k, p1, j, aj, vj, dx, dy, dz, r2); });
-        }
-        reduce_group<G>(acc.sd);
-        reduce_group<G>(acc.sx);
-        reduce_group<G>(acc.sy);
-        reduce_group<G>(acc.sz);
-        if (s == 0) {
-            s_sum[0][loc] = acc.sd.get();
-            s_sum[1][loc] = acc.sx.get();
-            s_sum[2][loc] = acc.sy.get();
-            s_sum[3][loc] = acc.sz.get();
-        }
-    }
-    __syncthreads();
-    const int i = base + (int)threadIdx.x;
-    DispBox box;
-    if (i < k.n) {
-        Pass2Acc<P, MODE> acc;
-        acc.load(k, p1, i, 0);
-        acc.sd = sum_of<T, P::kComp>(s_sum[0][threadIdx.x]);
-        acc.sx = sum_of<T, P::kComp>(s_sum[1][threadIdx.x]);
-        acc.sy = sum_of<T, P::kComp>(s_sum[2][threadIdx.x]);
-        acc.sz = sum_of<T, P::kComp>(s_sum[3][threadIdx.x]);
-        pass2_finish<P, MODE>(k, i, acc, in, keys, nl, nullptr, nullptr, 0, out, out_hash, err,
-                              box);
-    }
-    // the block's displacement box; blockDim is a multiple of 32, every thread gets here
-    reduce_disp_box(box, disp, s_box);
-}
-
 inline int group_blocks(int n, int threads) { return (n + threads - 1) / threads; }
 
 template <int G>
@@ -287,38 +235,11 @@ cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
     });
 }
 
-template <class P>
-cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
-                                const ParticleSetT<typename P::T>& in, const unsigned* keys,
-                                const int* cs, const NbrList& nl,
-                                const Pass1OutT<typename P::T>& p1,
-                                ParticleSetT<typename P::T> out, unsigned* out_hash,
-                                unsigned* err, unsigned* disp, cudaStream_t s) {
-    if (k.n <= 0) return cudaSuccess;
-    // whole warps per block (each block's rounds split its warps into groups)
-    if (k.threads % 32 != 0) return cudaErrorInvalidValue;
-    return with_group(k.lanes2, [&](auto tag) {
-        constexpr int G = decltype(tag)::value;
-        const int blocks = group_blocks(k.n, k.threads);
-        if (half == HALF_PREDICT)
-            k_pass2_g<P, MODE_PRED, G><<<blocks, k.threads, 0, s>>>(k, in, keys, cs, nl, p1, out,
-                                                                    out_hash, err, disp);
-        else
-            k_pass2_g<P, MODE_CORR, G><<<blocks, k.threads, 0, s>>>(k, in, keys, cs, nl, p1, out,
-                                                                    out_hash, err, disp);
-        return cudaGetLastError();
-    });
-}
-
 #define SPH_NS_GROUPS_INSTANTIATE(P)                                                          \
     template cudaError_t launch_pass1_groups<P>(const KParamsT<P::T>&,                        \
                                                 const ParticleSetT<P::T>&, const unsigned*,   \
                                                 const int*, const NbrList&,                   \
-                                                const Pass1OutT<P::T>&, cudaStream_t);        \
-    template cudaError_t launch_pass2_groups<P>(                                              \
-        const KParamsT<P::T>&, HalfStep, const ParticleSetT<P::T>&, const unsigned*,          \
-        const int*, const NbrList&, const Pass1OutT<P::T>&, ParticleSetT<P::T>, unsigned*,   \
-        unsigned*, unsigned*, cudaStream_t);
+                                                const Pass1OutT<P::T>&, cudaStream_t);
 SPH_NS_GROUPS_INSTANTIATE(PrecF32)
 SPH_NS_GROUPS_INSTANTIATE(PrecF64)
 SPH_NS_GROUPS_INSTANTIATE(PrecMix)

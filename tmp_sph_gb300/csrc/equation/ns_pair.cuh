@@ -476,13 +476,13 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
         const int inst = k.inst_cells ? in.inst[i] : 0;
         if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
-        unsigned ncell;
-        out_hash[i] = sort_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f, &ncell);
+        const unsigned nk = slot_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f);
+        out_hash[i] = nk;
         raise_flags(err, f);
         if (k.park_inactive) {
             // a particle that leaves (or rejoins) the neighbour search needs new lists; one
             // outside it is in no list, so its moves do not count
-            const bool now = inactive_key(k, ncell);
+            const bool now = inactive_key(k, nk);
             if (now != inactive_key(k, keys[i])) {
                 box.add(3.0e38f, 3.0e38f, 3.0e38f);
                 box.add(-3.0e38f, -3.0e38f, -3.0e38f);
@@ -558,13 +558,13 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
         const int inst = k.inst_cells ? in.inst[i] : 0;
         if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
-        unsigned ncell;
-        out_hash[i] = sort_key(k, inst, fi, np.x, np.y, np.z, &f, &ncell);
+        const unsigned nk = slot_key(k, inst, fi, np.x, np.y, np.z, &f);
+        out_hash[i] = nk;
         raise_flags(err, f);
         if (k.park_inactive) {
             // a particle that leaves (or rejoins) the neighbour search needs new lists; one
             // outside it is in no list, so its moves do not count
-            const bool now = inactive_key(k, ncell);
+            const bool now = inactive_key(k, nk);
             if (now != inactive_key(k, keys[i])) {
                 box.add(3.0e38f, 3.0e38f, 3.0e38f);
                 box.add(-3.0e38f, -3.0e38f, -3.0e38f);

@@ -50,9 +50,7 @@ struct KParamsT {
     // most 256) and particles per thread.
     int threads;
     int ppt;
-    int pairs;  // two consecutive particles per thread over the union of their lists
     int lanes;   // lanes per particle in list pass 1 (1, or 2 .. 16: ns_groups.cu)
-    int lanes2;  // and in list pass 2
     int list_win;  // list entries interleaved in windows of eight (for lane groups; ns_pair.cuh)
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
@@ -76,10 +74,6 @@ struct KParamsT {
     // 1: a fluid particle outside the escape box takes key num_cells (sorted after every cell,
     // outside the neighbour search); 0: it is parked and stays in the search (reference)
     int park_inactive;
-    // Order of the particles inside a cell (resident solver): sort keys carry sub_bits bits of
-    // the particle's place in its cell below the cell key (subcell_code); 0: original order.
-    int sub_mode;
-    int sub_bits;
 };
 using KParams = KParamsT<float>;
 
@@ -156,39 +150,13 @@ __device__ __forceinline__ double cell_units(double p, double gmin, const KParam
 __device__ __forceinline__ float floor_of(float v) { return floorf(v); }
 __device__ __forceinline__ double floor_of(double v) { return floor(v); }
 
-// Bin of a fraction f in [0, 1) among `levels` equal bins (clamped: rounding at a cell face).
-template <class R>
-__device__ __forceinline__ unsigned frac_bin(R f, int levels) {
-    const int b = (int)(f * (R)levels);
-    return (unsigned)(b < 0 ? 0 : (b >= levels ? levels - 1 : b));
-}
-
-// Place of a particle inside its cell, from its fractional cell coordinates: the low bits of
-// the resident sort key, so the sort also orders the particles of a cell.  Mode 1: eight bins
-// along x (the 3-cell x-strips a cell walk reads become sorted along x at bin granularity);
-// mode 2: the octant (z, y, x halves); mode 3: two levels of octants (Morton order of a
-// 4 x 4 x 4 sub-grid).  Nearby particles become nearby slots, so the lanes of a warp hold
-// particles whose neighbour lists are alike.
-__host__ __device__ __forceinline__ int subcell_bits(int mode) {
-    return mode == 1 || mode == 2 ? 3 : (mode == 3 ? 6 : 0);
-}
-template <class R>
-__device__ __forceinline__ unsigned subcell_code(int mode, R fx, R fy, R fz) {
-    if (mode == 1) return frac_bin(fx, 8);
-    if (mode == 2) return (frac_bin(fz, 2) << 2) | (frac_bin(fy, 2) << 1) | frac_bin(fx, 2);
-    const unsigned x = frac_bin(fx, 4), y = frac_bin(fy, 4), z = frac_bin(fz, 4);
-    return ((z >> 1) << 5) | ((y >> 1) << 4) | ((x >> 1) << 3) | ((z & 1u) << 2) |
-           ((y & 1u) << 1) | (x & 1u);
-}
-
 // Hash used by the resident solver: identical to the reference for in-grid positions; an
 // out-of-grid or non-finite position is clamped into the grid (of one instance) and reported
 // through `flag`.  KT is the constant block's real type, PT the position's (a mixed-precision
-// solver hashes its double positions on the float grid, in double).  With `sub` (and a
-// sub-cell order in k), *sub receives the particle's subcell_code (0 when it was clamped).
+// solver hashes its double positions on the float grid, in double).
 template <class KT, class PT>
 __device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT y, PT z,
-                                                 unsigned* flag, unsigned* sub = nullptr) {
+                                                 unsigned* flag) {
     if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
         *flag |= SPH_FLAG_NONFINITE | SPH_FLAG_OUT_OF_GRID;
         x = isfinite(x) ? x : (PT)k.gmin_x;
@@ -200,25 +168,21 @@ __device__ __forceinline__ int cell_hash_clamped(const KParamsT<KT>& k, PT x, PT
     const auto uz = cell_units(z, k.gmin_z, k);
     const auto fx = floor_of(ux), fy = floor_of(uy), fz = floor_of(uz);
     int cx = (int)fx, cy = (int)fy, cz = (int)fz;
-    bool clamped = false;
     if ((unsigned)cx >= (unsigned)k.gx || (unsigned)cy >= (unsigned)k.gy ||
         (unsigned)cz >= (unsigned)k.gz_local) {
         *flag |= SPH_FLAG_OUT_OF_GRID;
-        clamped = true;
         cx = clampi(cx, 0, k.gx - 1);
         cy = clampi(cy, 0, k.gy - 1);
         cz = clampi(cz, 0, k.gz_local - 1);
     }
-    if (sub) *sub = clamped ? 0u : subcell_code(k.sub_mode, ux - fx, uy - fy, uz - fz);
     return (cz * k.gy + cy) * k.gx + cx;
 }
 
 // Resident key of a particle of instance `inst` (0 for a single simulation).
 template <class KT, class PT>
 __device__ __forceinline__ unsigned resident_key(const KParamsT<KT>& k, int inst, PT x, PT y, PT z,
-                                                 unsigned* flag, unsigned* sub = nullptr) {
-    return (unsigned)cell_hash_clamped(k, x, y, z, flag, sub) +
-           (unsigned)inst * (unsigned)k.inst_cells;
+                                                 unsigned* flag) {
+    return (unsigned)cell_hash_clamped(k, x, y, z, flag) + (unsigned)inst * (unsigned)k.inst_cells;
 }
 
 // ---------------------------------------------------------------- equation of state
@@ -264,22 +228,6 @@ __device__ __forceinline__ unsigned slot_key(const KParamsT<KT>& k, int inst, bo
                                              PT y, PT z, unsigned* flag) {
     if (k.park_inactive && fluid && escaped(k, x, y, z)) return (unsigned)k.num_cells;
     return resident_key(k, inst, x, y, z, flag);
-}
-
-// The key the resident sort orders by: the slot key shifted up by k.sub_bits with the
-// particle's place in its cell (subcell_code) below it; *cell receives the slot key itself.
-// The sort hands its consumers the slot keys again (radix_sort_pairs' out_shift).
-template <class KT, class PT>
-__device__ __forceinline__ unsigned sort_key(const KParamsT<KT>& k, int inst, bool fluid, PT x,
-                                             PT y, PT z, unsigned* flag, unsigned* cell) {
-    if (k.park_inactive && fluid && escaped(k, x, y, z)) {
-        *cell = (unsigned)k.num_cells;
-        return (unsigned)k.num_cells << k.sub_bits;
-    }
-    unsigned sub = 0;
-    const unsigned c = resident_key(k, inst, x, y, z, flag, k.sub_bits ? &sub : nullptr);
-    *cell = c;
-    return (c << k.sub_bits) | sub;
 }
 
 template <class KT>

@@ -18,15 +18,13 @@ namespace sph {
 // bits [0, key_bits).  Scratch layout and size come from sort_scratch_bytes(); no allocation.
 // vals_in == NULL means the values are the identity 0..n-1.  The sorted output lands in
 // keys_out / vals_out (which may alias keys_in / vals_in).  err (may be NULL) receives
-// SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.  out_shift > 0 stores the sorted
-// keys shifted down by that many bits (the resident sort orders by cell and place in the cell,
-// and hands on the cell keys).
+// SPH_FLAG_KEY_RANGE if a key has bits at or above key_bits.
 size_t sort_scratch_bytes(int n);
 // gate: see gated_off() — NULL sorts unconditionally.
 cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
                              int* vals_out, int n, int key_bits, void* scratch,
                              size_t scratch_bytes, unsigned* err, cudaStream_t s,
-                             const unsigned* gate = nullptr, int out_shift = 0);
+                             const unsigned* gate = nullptr);
 int key_bits_for(int num_cells);
 
 // ---------------------------------------------------------------- cell list (lib/mesh.cu)
@@ -130,9 +128,8 @@ struct NbrList {
     // has an empty list without walking them.
     const unsigned char* fluid_cells = nullptr;
 };
-// List slots per particle (per pair of particles with pairs): 1.5x the lattice particles within
-// kh (1 + skin), rounded up to 16.
-int nbr_capacity_for(const sph_params& p, double skin = 0.0, bool pairs = false);
+// List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
+int nbr_capacity_for(const sph_params& p, double skin = 0.0);
 
 // Neighbour passes (equation/ns.cu), one instantiation per precision policy P.
 // nl == NULL walks the cells in every pass.
@@ -188,21 +185,13 @@ cudaError_t launch_upload_convert(const KParamsT<typename P::T>& k, const float*
                                   const int* type, const int* inst_off, int n_inst,
                                   ParticleSetT<typename P::T> dst, unsigned* hash, unsigned* err,
                                   cudaStream_t s);
-// Lane-group variants of the list passes (equation/ns_groups.cu): k.lanes (pass 1) and
-// k.lanes2 (pass 2) in {2, 4, 8, 16} lanes per particle over the one-lane list; launch_pass1 /
-// launch_pass2_step dispatch to them when the pass's G > 1.
+// Lane-group variant of list pass 1 (equation/ns_groups.cu): k.lanes in {2, 4, 8, 16} lanes
+// per particle over the one-lane list; launch_pass1 dispatches to it when k.lanes > 1.
 template <class P>
 cudaError_t launch_pass1_groups(const KParamsT<typename P::T>& k,
                                 const ParticleSetT<typename P::T>& in, const unsigned* keys,
                                 const int* cs, const NbrList& nl,
                                 const Pass1OutT<typename P::T>& out, cudaStream_t s);
-template <class P>
-cudaError_t launch_pass2_groups(const KParamsT<typename P::T>& k, HalfStep half,
-                                const ParticleSetT<typename P::T>& in, const unsigned* keys,
-                                const int* cs, const NbrList& nl,
-                                const Pass1OutT<typename P::T>& p1,
-                                ParticleSetT<typename P::T> out, unsigned* out_hash,
-                                unsigned* err, unsigned* disp, cudaStream_t s);
 
 // Upload original-order arrays into the current sorted order (slot k takes particle id[k]),
 // measuring displacements from the list-build positions xb into *disp; a changed particle
@@ -312,11 +301,8 @@ struct sph_ctx {
     int opt_cond_graph = 1;  // graph replay skips the rebuild kernels through conditional nodes
     int opt_threads = 0;     // neighbour kernels: threads per block (0: the precision's default)
     int opt_ppt = 1;         // neighbour kernels: particles per thread
-    int opt_pairs = 0;       // neighbour kernels: two particles per thread over a union list
     int opt_lanes = 0;       // list pass 1: lanes per particle (0: the precision's default)
-    int opt_lanes2 = 1;      // list pass 2: lanes per particle
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
-    int opt_subcell = 0;     // order of the particles inside a cell (subcell_code mode)
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(RS_THREADS)
 k_rs_downsweep(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
                unsigned* __restrict__ keys_out, int* __restrict__ vals_out,
                const unsigned* __restrict__ hist, int n, int shift, unsigned xmask_in,
-               unsigned xmask_out, int out_shift, int tiles, const unsigned* gate) {
+               unsigned xmask_out, int tiles, const unsigned* gate) {
     __shared__ unsigned s_cnt[RS_WARPS][RS_RADIX];
     __shared__ unsigned s_gbase[RS_RADIX];
     __shared__ unsigned s_tpre[RS_RADIX];
@@ -215,7 +215,7 @@ k_rs_downsweep(const unsigned* __restrict__ keys_in, const int* __restrict__ val
         unsigned d = (k >> shift) & 0xffu;
         unsigned g = s_gbase[d] + (unsigned)e - s_tpre[d];
         if (g < (unsigned)n) {  // always true for consistent histograms; guards the store
-            keys_out[g] = (k ^ xmask_out) >> out_shift;
+            keys_out[g] = k ^ xmask_out;
             vals_out[g] = s_vals[e];
         }
     }
@@ -460,16 +460,15 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     dst.rec[2 * (size_t)i + 1] = make4<T>(vx, vy, vz, signed_rho_t<T>(t, (T)rho[i]));
     if constexpr (P::kMixed) {
         const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[i] - (double)kp.rho0};
-        unsigned cell;
-        hash[i] = sort_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f, &cell);
+        const unsigned h = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
         dst.xm[i] = xm;
         dst.txm[i] = xm;
-        dst.rec[2 * (size_t)i] = offsets_in_cell(kp, cell, xm, p[i]);
+        dst.rec[2 * (size_t)i] = offsets_in_cell(kp, h, xm, p[i]);
+        hash[i] = h;
     } else {
         dst.rec[2 * (size_t)i] = make4<T>(x, y, z, (T)p[i]);
         dst.tpos[i] = make4<T>(x, y, z, (T)rho[i]);
-        unsigned cell;
-        hash[i] = sort_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f, &cell);
+        hash[i] = slot_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f);
     }
     raise_flags(err, f);
 }
@@ -505,25 +504,25 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
             const T srho = signed_rho_t<T>(t, (T)rho[r]);
             dst.rec[2 * (size_t)k + 1] = make4<T>(vx, vy, vz, srho);
             vec4_t<T> a;
-            unsigned nk, ncell;
+            unsigned nk;
             const unsigned key = keys[k];
             if constexpr (P::kMixed) {
                 const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[r] - (double)kp.rho0};
                 dst.xm[k] = xm;
                 dst.txm[k] = xm;
                 a = offsets_in_cell(kp, key, xm, p[r]);
-                nk = sort_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f, &ncell);
+                nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
             } else {
                 a = make4<T>(x, y, z, (T)p[r]);
                 dst.tpos[k] = make4<T>(x, y, z, (T)rho[r]);
-                nk = sort_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f, &ncell);
+                nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, (T)x, (T)y, (T)z, &f);
             }
             hash[k] = nk;
             // a particle entering or leaving the neighbour search (park_inactive) needs new
             // lists; one that stays outside it is in no list.  Marked as pass 2 marks it (a
             // box no skin covers, not a forced rebuild), so the adaptive skin of a host loop
             // follows the resident run's
-            const bool out_now = inactive_key(kp, ncell);
+            const bool out_now = inactive_key(kp, nk);
             const bool moved_out = out_now != inactive_key(kp, key);
             if (moved_out) {
                 box.add(3.0e38f, 3.0e38f, 3.0e38f);
@@ -554,13 +553,12 @@ __global__ void k_rehash(KParamsT<typename P::T> kp, ParticleSetT<typename P::T>
     unsigned f = 0;
     const int inst = set.inst ? set.inst[i] : 0;
     const bool fluid = set.type[i] == SPH_TYPE_FLUID;
-    unsigned cell;
     if constexpr (P::kMixed) {
         const dvec4 q = set.xm[i];
-        hash[i] = sort_key(kp, inst, fluid, q.x, q.y, q.z, &f, &cell);
+        hash[i] = slot_key(kp, inst, fluid, q.x, q.y, q.z, &f);
     } else {
         const auto q = set.xyz[i];
-        hash[i] = sort_key(kp, inst, fluid, q.x, q.y, q.z, &f, &cell);
+        hash[i] = slot_key(kp, inst, fluid, q.x, q.y, q.z, &f);
     }
     raise_flags(err, f);
 }
@@ -686,10 +684,9 @@ size_t sort_scratch_bytes(int n) {
 cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsigned* keys_out,
                              int* vals_out, int n, int key_bits, void* scratch,
                              size_t scratch_bytes, unsigned* err, cudaStream_t s,
-                             const unsigned* gate, int out_shift) {
+                             const unsigned* gate) {
     if (n <= 0) return cudaSuccess;
-    if (key_bits < 1 || key_bits > 32 || !scratch || scratch_bytes < sort_scratch_bytes(n) ||
-        out_shift < 0 || out_shift >= key_bits)
+    if (key_bits < 1 || key_bits > 32 || !scratch || scratch_bytes < sort_scratch_bytes(n))
         return cudaErrorInvalidValue;
     const int passes = (key_bits + 7) / 8;
     // a gated sort must not need the ungated copies below
@@ -730,8 +727,7 @@ cudaError_t radix_sort_pairs(const unsigned* keys_in, const int* vals_in, unsign
                                                    sc.hist, tiles, totals, err, gate);
         k_rs_scan<<<RS_RADIX, RS_THREADS, 0, s>>>(sc.hist, tiles, totals, gate);
         k_rs_downsweep<<<tiles, RS_THREADS, 0, s>>>(kin, vin, kdst, vdst, sc.hist, n, shift, xin,
-                                                     xout, p == passes - 1 ? out_shift : 0,
-                                                     tiles, gate);
+                                                     xout, tiles, gate);
         kin = kdst;
         vin = vdst;
     }

@@ -36,9 +36,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.inst_cells = 0;
     k.threads = 128;
     k.ppt = 1;
-    k.pairs = 0;
     k.lanes = 1;
-    k.lanes2 = 1;
     k.list_win = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
@@ -79,8 +77,6 @@ KParams make_kparams(const sph_params& p, int n) {
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
     k.park_inactive = p.park_inactive;
-    k.sub_mode = 0;
-    k.sub_bits = 0;
     return k;
 }
 
@@ -103,9 +99,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.inst_cells = 0;
     k.threads = 128;
     k.ppt = 1;
-    k.pairs = 0;
     k.lanes = 1;
-    k.lanes2 = 1;
     k.list_win = 0;
     k.gmin_x = p.grid_min[0];
     k.gmin_y = p.grid_min[1];
@@ -147,8 +141,6 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
     k.park_inactive = p.park_inactive;
-    k.sub_mode = 0;
-    k.sub_bits = 0;
     return k;
 }
 

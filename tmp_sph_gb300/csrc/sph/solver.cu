@@ -265,7 +265,7 @@ static int block_threads(const sph_ctx* c) {
 }
 
 // Lane groups read interleaved list windows, one lane per particle plain ones.
-static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1 || c->opt_lanes2 > 1; }
+static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1; }
 
 template <class T>
 KParamsT<T> resident_kparams(const sph_ctx* c) {
@@ -273,15 +273,11 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.gz_local = c->gz_inst;
     k.threads = block_threads(c);
     k.ppt = c->opt_ppt;
-    k.pairs = c->opt_pairs;
-    // lane groups need the list (and are not combined with pair mode)
-    const bool groups = c->opt_nbr_list && c->nl.idx && !c->opt_pairs;
+    // lane groups need the list
+    const bool groups = c->opt_nbr_list && c->nl.idx;
     k.lanes = groups ? pass1_lanes(c) : 1;
-    k.lanes2 = groups ? c->opt_lanes2 : 1;
-    k.list_win = k.lanes > 1 || k.lanes2 > 1;
+    k.list_win = k.lanes > 1;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
-    k.sub_mode = c->opt_subcell;
-    k.sub_bits = subcell_bits(c->opt_subcell);
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
@@ -397,13 +393,12 @@ template <class P>
 cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStream_t s,
                           cudaEvent_t* ev) {
     // with park_inactive, key num_cells marks the slots outside the neighbour search
-    // and below the cell, the particle's place in it (k.sub_bits), which the sort drops again
-    const int bits = key_bits_for(c->Pi.num_cells + (c->P.park_inactive ? 1 : 0)) + k.sub_bits;
+    const int bits = key_bits_for(c->Pi.num_cells + (c->P.park_inactive ? 1 : 0));
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
     cudaError_t e;
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
-                         c->sort_scratch_bytes, c->err, s, gate, k.sub_bits);
+                         c->sort_scratch_bytes, c->err, s, gate);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_GATHER], s);
     // permute the live set y into cell order through x, then copy it back
@@ -536,11 +531,7 @@ void free_list(NbrList& nl) {
 
 cudaError_t alloc_list(sph_ctx* c) {
     // the option is rounded up to a multiple of 16, like the derived capacity
-    // pair mode keeps one union list per two particles (also used per particle by sph_ns, so
-    // the rows still cover every particle)
-    const bool pairs = c->opt_pairs != 0;
-    int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15
-                                 : nbr_capacity_for(c->P, c->skin, pairs);
+    int cap = c->opt_nbr_cap > 0 ? (c->opt_nbr_cap + 15) & ~15 : nbr_capacity_for(c->P, c->skin);
     if (c->nl.idx && c->nl.cap == cap) return cudaSuccess;
     free_list(c->nl);
     // warp-interleaved blocks of cap x 32 slots: whole warps, the last one padded
@@ -690,37 +681,17 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             if (reset_skin_sync(c) != cudaSuccess) return SPH_ERR_CUDA;
             break;  // the next lists take the first skin of the new mode
         case SPH_OPT_LANES_PER_PARTICLE:
-        case SPH_OPT_PASS1_LANES:
-        case SPH_OPT_PASS2_LANES: {
-            // 0: the default of the precision (pass 1 only)
-            const bool dflt = value == 0 && option != SPH_OPT_PASS2_LANES;
-            if (!dflt && value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
+        case SPH_OPT_PASS1_LANES: {
+            // 0: the default of the precision
+            if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
                 return SPH_ERR_ARG;
             const bool win = list_windows(c);
-            if (option != SPH_OPT_PASS2_LANES) c->opt_lanes = value;
-            if (option != SPH_OPT_PASS1_LANES) c->opt_lanes2 = dflt ? 1 : value;
+            c->opt_lanes = value;
             drop_graph(c);
             if (win == list_windows(c)) return SPH_OK;
             break;  // the slot order of the lists changed: rebuild
         }
-        case SPH_OPT_PAIRS:
-            c->opt_pairs = value != 0;
-            drop_graph(c);
-            if (alloc_list(c) != cudaSuccess) {
-                cudaGetLastError();
-                return SPH_ERR_NOMEM;
-            }
-            break;  // the list layout changed: rebuild
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
-        case SPH_OPT_SUBCELL_ORDER:
-            if (value < 0 || value > 3) return SPH_ERR_ARG;
-            // the stacked key must still fit the 32-bit sort
-            if (key_bits_for(c->Pi.num_cells + 1) + subcell_bits(value) > 31) return SPH_ERR_ARG;
-            if (value == c->opt_subcell) return SPH_OK;
-            c->opt_subcell = value;
-            c->rehash = c->loaded;  // the next keys carry the new sub-cell bits
-            drop_graph(c);
-            break;
         case SPH_OPT_PRECISION: {
             if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && !prec_is_mixed(value))
                 return SPH_ERR_ARG;
@@ -790,12 +761,9 @@ extern "C" int sph_ctx_get_option(const sph_ctx* c, int option, int* value) {
         case SPH_OPT_PRECISION: *value = c->prec; break;
         case SPH_OPT_BLOCK_THREADS: *value = block_threads(c); break;
         case SPH_OPT_PARTICLES_PER_THREAD: *value = c->opt_ppt; break;
-        case SPH_OPT_PAIRS: *value = c->opt_pairs; break;
         case SPH_OPT_ADAPTIVE_SKIN: *value = c->opt_adaptive_skin; break;
-        case SPH_OPT_SUBCELL_ORDER: *value = c->opt_subcell; break;
         case SPH_OPT_LANES_PER_PARTICLE:
         case SPH_OPT_PASS1_LANES: *value = pass1_lanes(c); break;
-        case SPH_OPT_PASS2_LANES: *value = c->opt_lanes2; break;
         default: return SPH_ERR_ARG;
     }
     return SPH_OK;

@@ -353,6 +353,31 @@ def reference_cuda_leg(st: dict, p, versions=(("v4", 1, 10), ("src", 0, 2))) -> 
     return out
 
 
+def graph_node_gap_us(stream, nodes: int = 64, replays: int = 50) -> float:
+    """Device time per kernel node of a replayed CUDA graph whose nodes are a chain of tiny
+    dependent kernels (one-element adds): the launch-to-launch cost a persistent kernel could
+    save per launch it replaces."""
+    import torch
+    x = torch.zeros(1, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        x.add_(1.0)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(nodes):
+                x.add_(1.0)
+    g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        for _ in range(replays):
+            g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return 1e3 * e0.elapsed_time(e1) / (nodes * replays)
+
+
 def time_run(sol, stream, steps: int) -> tuple[float, int]:
     """(milliseconds, list rebuilds) of `steps` steps on `stream`, by CUDA events."""
     import torch
@@ -554,6 +579,148 @@ def sol_cells_batch(p, n_inst: int, skin: int) -> int:
     return dims[0] * dims[1] * n_inst * (dims[2] + 1)
 
 
+# ---------------------------------------------------------------- --components
+# Cost of the components either side of the step (python bench.py --components [--case large]):
+# * generator and .dat files (the reference's ini_fluid inputs, src/io/io.cu:10-111): seconds to
+#   generate the case, to write its seven text files and to read them back;
+# * probes (src/io/io.cu:236-279): one sph_probe_read with a surge front, two pressure probes
+#   and two water-height gauges plus the FP64 reductions, against one step;
+# * snapshots (src/sph/sph_run.cu:258-281): step time with an asynchronous snapshot of the
+#   whole state every 1 / 10 steps against none (the copy runs on a second stream), and the
+#   legacy-VTK writer for one frame (binary and ASCII);
+# * escaped particles (src/sph/sph_run.cu:437-447): step time of a case whose escape box cuts
+#   the water column, parked particles kept in the neighbour search (the reference's
+#   behaviour) or taken out of it (park_inactive).
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def step_ms(sol, stream, steps: int) -> float:
+    import torch
+    e0, e1 = _events()
+    sol.step(2, stream=stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sol.step(steps, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def measure_files(case: str) -> dict:
+    from tmp_sph_gb300 import api, cases
+    t0 = time.perf_counter()
+    st, p = cases.build(case, physics="config")
+    t_gen = time.perf_counter() - t0
+    n = len(st["rho"])
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        api.write_dat(d, st)
+        t_w = time.perf_counter() - t0
+        size = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+        t0 = time.perf_counter()
+        back = api.read_dat(d, n)
+        t_r = time.perf_counter() - t0
+    same = all(np.array_equal(back[k], st[k]) for k in ("pos", "vel", "rho", "p", "type"))
+    return {"particles": n, "generate_s": t_gen, "write_dat_s": t_w, "read_dat_s": t_r,
+            "dat_bytes": size, "round_trip_exact": bool(same)}
+
+
+def measure_solver(case: str, steps: int) -> dict:
+    import tempfile
+    import torch
+    from tmp_sph_gb300 import api, cases, solver as S
+    from tmp_sph_gb300.output import write_vtk
+    st, p = cases.build(case, physics="config")
+    n = len(st["rho"])
+    s = torch.cuda.Stream()
+    out = {"particles": n}
+    dx = float(p.dx)
+    probes = [(api.SPH_PROBE_FRONT, 0, 0, 0, 0, 0),
+              (api.SPH_PROBE_PRESSURE, 1.0, 0.25, 0.05, 0, 0),
+              (api.SPH_PROBE_PRESSURE, 0.0, 0.25, 0.02, 0, 0),
+              (api.SPH_PROBE_HEIGHT, 0.2, 0.25, 0, 1.5 * dx, 0),
+              (api.SPH_PROBE_HEIGHT, 0.8, 0.25, 0, 1.5 * dx, 0)]
+    with S.Solver(p, n) as sol:
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        base = step_ms(sol, s, steps)
+        out["step_ms"] = base
+        # probes: device time of the reduction launches (one read; the call synchronises)
+        sol.probe(probes, stream=s)
+        ts = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sol.probe(probes, stream=s)
+            ts.append(time.perf_counter() - t0)
+        out["probe_read_ms"] = 1e3 * float(np.median(ts))
+        # snapshots on the copy stream while the steps continue
+        host = {"pos": torch.empty((n, 3)).pin_memory(), "vel": torch.empty((n, 3)).pin_memory(),
+                "p": torch.empty(n).pin_memory(), "type": torch.empty(n, dtype=torch.int32).pin_memory()}
+        for every in (10, 1):
+            e0, e1 = _events()
+            torch.cuda.synchronize()
+            e0.record(s)
+            for k in range(steps):
+                if k % every == 0:
+                    api.call("sph_snapshot_begin", sol.handle, api.ptr(host["pos"]),
+                             api.ptr(host["vel"]), None, api.ptr(host["p"]),
+                             api.ptr(host["type"]), S._stream(s))
+                sol.step(1, stream=s)
+            e1.record(s)
+            api.call("sph_snapshot_wait", sol.handle)
+            torch.cuda.synchronize()
+            out[f"step_ms_snapshot_every_{every}"] = e0.elapsed_time(e1) / steps
+        out["snapshot_bytes"] = n * (12 + 12 + 4 + 4)
+        h = {k: v.numpy() for k, v in host.items()}
+        with tempfile.TemporaryDirectory() as d:
+            for binary in (True, False):
+                path = os.path.join(d, "f.vtk")
+                t0 = time.perf_counter()
+                write_vtk(path, h["pos"], h["vel"], h["p"], h["type"], binary=binary)
+                dt = time.perf_counter() - t0
+                key = "vtk_binary" if binary else "vtk_ascii"
+                out[key + "_s"] = dt
+                out[key + "_bytes"] = os.path.getsize(path)
+    return out
+
+
+def measure_parking(steps: int) -> dict:
+    """The 765,828-particle case with the escape box's top at 0.28 m: the top 2 cm of the
+    water column (about 32,000 particles) escapes in the first half step."""
+    import torch
+    from tmp_sph_gb300 import cases, solver as S
+    st, p = cases.build("precision", physics="config")
+    p.escape_max = type(p.escape_max)(p.escape_max[0], p.escape_max[1], 0.28)
+    n = len(st["rho"])
+    out = {"particles": n}
+    for mode in (1, 0):
+        p.park_inactive = mode
+        s = torch.cuda.Stream()
+        with S.Solver(p, n) as sol:
+            sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+            ms = step_ms(sol, s, steps)
+            _, stats = sol.probe(stream=s)
+            flags = sol.error_flags(stream=s)
+        out[f"park_inactive_{mode}"] = {"step_ms": ms, "parked": stats["parked"],
+                                        "device_error_flags": flags}
+    return out
+
+
+def run_components(args):
+    import torch
+    from tmp_sph_gb300 import build
+    torch.cuda.set_device(0)
+    build.build()
+    steps = min(args.steps, 20)
+    rep = {"components": True, "case": args.case, "files": measure_files(args.case),
+           "solver": measure_solver(args.case, steps), "parking": measure_parking(steps)}
+    print(json.dumps(rep), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -570,6 +737,9 @@ def main():
                     help="instances of the batched block of the default line (0: skip it)")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's own CUDA versions")
+    ap.add_argument("--components", action="store_true",
+                    help="time the components either side of the step instead (generator, "
+                         ".dat files, probes, snapshots, VTK writer, escaped particles)")
     ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
                     help="rebuild kernels of the step graph under conditional nodes, or launched "
                          "every half step and returning at once when the lists are kept")
@@ -590,6 +760,8 @@ def main():
         return run_reference(args)
     if args.case.startswith("batch"):
         return run_batch(args)
+    if args.components:
+        return run_components(args)
 
     import torch
     import torch.distributed as dist
@@ -767,6 +939,12 @@ def main():
                                 args.warmup, run_steps=args.run_steps,
                                 clocks=ClockSampler(gpu_uuid(local)))
         batched["vs_plain_fp32"] = batched["value"] / value
+        # what a persistent kernel could save: the graph's launch gaps (three kernel nodes per
+        # half step that keeps its lists) against the step time
+        gap = graph_node_gap_us(stream)
+        batched["graph_node_gap_us"] = gap
+        batched["launch_gap_share"] = 6 * gap / (1e3 * batched["ms_per_step"])
+        batched["launch_gap_share_plain_fp32"] = 6 * gap / (1e3 * ms / args.steps)
 
     ref_cuda = None
     if rank == 0 and ws == 1 and not args.no_reference_cuda:

@@ -198,9 +198,11 @@ int sph_sort_particles(int* hash, int* index, int n, int key_bits,
  * the reference.  For callers bound to the three-argument sortParticles form that may not
  * allocate device memory during a run.  Scratch is a fixed array of this library (one per
  * device, about 9.5 MB); n > SPH_SORT_NOALLOC_MAX_N returns SPH_ERR_SCRATCH.  The first call
- * on a device looks up that array's address (make it before any stream capture); nothing in
- * the array needs to start at zero.  Calls on one device whose executions overlap race on the
- * shared array: order them on one stream or with events. */
+ * on a device looks up that array's address (make it before any stream capture); later calls
+ * outside a capture look it up again (so a cudaDeviceReset between calls is harmless), calls
+ * inside one use the last address.  Nothing in the array needs to start at zero.  Calls on one
+ * device whose executions overlap race on the shared array: order them on one stream or with
+ * events. */
 #define SPH_SORT_NOALLOC_MAX_N (1 << 20)
 int sph_sort_particles_noalloc(int* hash, int* index, int n, int key_bits, void* stream);
 

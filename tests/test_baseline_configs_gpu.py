@@ -134,8 +134,11 @@ def test_batch_keys_radix_sort_matches_stable_argsort(sphlib, cuda):
 def test_config2_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
     """One resident FP32 step of the 4,963,548-particle dam break against one step of the
     oracle (the C restatement of src/sph/sph_run.cu:285-336) on the same input: relative L2 of
-    the fluid displacement and velocity below 1e-4 (float rounding of sums taken in another
-    order; the cell lists of both are bit-exact, above)."""
+    the fluid velocity and density perturbation below 1e-4 (float rounding of sums taken in
+    another order; the cell lists of both are bit-exact, above).  One step from rest moves a
+    particle by about g dt^2 ~ 1e-8 m, below the spacing of float positions near 0.5 m
+    (6e-8 m), so positions are compared in units of that spacing: at most 8 apart (the GPU
+    fuses the x + dt/2 v multiply-add, the oracle rounds twice)."""
     import torch
     from tmp_sph_gb300 import solver as S
     st, p = large
@@ -148,13 +151,14 @@ def test_config2_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
         assert sol.error_flags(stream=s) == 0
     ref = oracle.run(oracle.params_like(p), st, 1)
     fl = st["type"] == 1
-    e_d = rel_l2(out["pos"][fl] - st["pos"][fl], ref["pos"][fl] - st["pos"][fl])
+    spacing = np.spacing(np.abs(ref["pos"][fl]).astype(np.float32)).astype(np.float64)
+    ulps = float(np.max(np.abs(out["pos"][fl].astype(np.float64) - ref["pos"][fl]) / spacing))
     e_v = rel_l2(out["vel"][fl], ref["vel"][fl])
     e_r = rel_l2(out["rho"][fl] - 1000.0, ref["rho"][fl] - 1000.0)
-    report("config2_step1_disp", e_d, 1e-4)
+    report("config2_step1_pos_max_ulps", ulps, 8)
     report("config2_step1_vel", e_v, 1e-4)
     report("config2_step1_drho", e_r, 1e-4)
-    assert e_d < 1e-4 and e_v < 1e-4 and e_r < 1e-4, (e_d, e_v, e_r)
+    assert ulps <= 8 and e_v < 1e-4 and e_r < 1e-4, (ulps, e_v, e_r)
 
 
 CONFIG1_TOL = 1e-3

@@ -14,6 +14,9 @@
 //  * The first call on a device does the setup: it looks up the device address of
 //    g_sort_scratch for the current device (cudaGetSymbolAddress, which may load this module
 //    on that device).  Make that first call, per device, before any stream capture begins.
+//    Every later call made while its stream is not capturing looks the address up again, so
+//    a device whose context was destroyed and recreated since (cudaDeviceReset) gets the
+//    address of its new array; a call inside a capture uses the address of the last lookup.
 //  * Nothing in the scratch has to start at zero: the sort clears its digit totals itself at
 //    the start of every call and writes the key/value buffers and the per-tile histograms
 //    before reading them.
@@ -40,16 +43,23 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of g_sort_scratch on the current device, looked up once per device.
-int scratch_for_current_device(void** out) {
+// Device address of g_sort_scratch on the current device: looked up on the first call and on
+// every call whose stream is not being captured (the array moves when the context is
+// recreated); inside a capture the last lookup's address is used.
+int scratch_for_current_device(cudaStream_t stream, void** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return SPH_ERR_CUDA;
     }
     if (dev < 0 || dev >= kMaxDevices) return SPH_ERR_ARG;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return SPH_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
         if (sph::sort_scratch_bytes(SPH_SORT_NOALLOC_MAX_N) > kScratchBytes) return SPH_ERR_SCRATCH;
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_sort_scratch) != cudaSuccess || !p) {
@@ -71,7 +81,7 @@ extern "C" int sph_sort_particles_noalloc(int* hash, int* index, int n, int key_
     if (n > SPH_SORT_NOALLOC_MAX_N) return SPH_ERR_SCRATCH;
     if (n <= 1) return SPH_OK;
     void* scratch = nullptr;
-    const int st = scratch_for_current_device(&scratch);
+    const int st = scratch_for_current_device((cudaStream_t)stream, &scratch);
     if (st != SPH_OK) return st;
     cudaError_t e = sph::radix_sort_pairs(reinterpret_cast<unsigned*>(hash), index,
                                           reinterpret_cast<unsigned*>(hash), index, n, key_bits,

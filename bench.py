@@ -503,14 +503,27 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
                       "neighbour_list_skin_over_kh": skin / 1000.0,
                       "graph_mode": args.graph_mode, **lanes},
            "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * steps},
-           "gpu_launches": count_launches(sol_cells_batch(p, n_inst, skin), 2 * steps,
-                                          rebuilds, args.graph_mode),
+           "gpu_launches": count_launches(
+               sol_cells_batch(p, n_inst, skin, tuned["divisions"] if tuned else 1), 2 * steps,
+               rebuilds, args.graph_mode),
            "autotune": None}
     if tuned:
         from tmp_sph_gb300 import autotune
         out["autotune"] = autotune.summary(tuned)
     flags = sol.error_flags(stream=stream)
     sol.close()
+    if run_steps > 0 and tuned:
+        # the library default over the same configured run, beside the autotuner's pick
+        dsol = S.Solver(p, n, precision=precision)
+        dsol.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+        dsol.upload_instances(mine, stream=stream)
+        ms_d, rb_d = time_run(dsol, stream, run_steps)
+        ms_d = replicas.reduce_max(ms_d)
+        out["configured_run_default"] = {"steps": run_steps, "ms_per_step": ms_d / run_steps,
+                                         "value": n_all * run_steps / (ms_d / 1e3),
+                                         "list_rebuilds": rb_d, "half_steps": 2 * run_steps}
+        flags |= dsol.error_flags(stream=stream)
+        dsol.close()
     if run_steps > 0:
         sol = make_solver()
         sol.upload_instances(mine, stream=stream)
@@ -571,12 +584,12 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
-def sol_cells_batch(p, n_inst: int, skin: int) -> int:
+def sol_cells_batch(p, n_inst: int, skin: int, divisions: int = 1) -> int:
     """Cells of the stacked grid of n_inst instances (for the launch count's key width)."""
     import math
-    cell = max(float(p.kh) * (1.0 + skin / 1000.0), float(p.cell_size))
+    cell = max(float(p.kh) * (1.0 + skin / 1000.0), float(p.cell_size)) / divisions
     dims = [max(1, math.ceil((p.grid_max[c] - p.grid_min[c]) / cell)) for c in range(3)]
-    return dims[0] * dims[1] * n_inst * (dims[2] + 1)
+    return dims[0] * dims[1] * n_inst * (dims[2] + divisions)
 
 
 # ---------------------------------------------------------------- --components
@@ -849,6 +862,13 @@ def main():
         run = configured_run(fresh, stream, st, n, n_fluid, args.run_steps, args.steps)
         fresh.close()
         flags |= run["device_error_flags"]
+        if tuned:
+            # the autotuner's pick against the library default over the same configured run
+            fresh = S.Solver(p, n, precision=args.precision)
+            fresh.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
+            run["default"] = configured_run(fresh, stream, st, n, n_fluid, args.run_steps,
+                                            args.steps)
+            fresh.close()
 
     # the same workload in the other precisions of the solver (same skin, graph replay)
     def time_precision(precision: str, steps: int) -> dict:

@@ -161,7 +161,7 @@ def test_config2_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
     assert ulps <= 8 and e_v < 1e-4 and e_r < 1e-4, (ulps, e_v, e_r)
 
 
-CONFIG1_TOL = 1e-3
+CONFIG1_TOL = 2e-4  # measured 1.2e-5 / 6.0e-6 / 4.0e-5 / 4.0e-5 on a GB300
 
 
 def test_config1_200_steps_match_reference(sphlib, cuda, report):

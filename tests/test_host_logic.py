@@ -42,10 +42,11 @@ def test_autotune_cost_model():
     # never more than two rebuilds per step
     assert math.isclose(autotune.step_cost(m1, P, 1e3), 2.2 + 2 * 3.5)
     st = {"type": np.array([1, 1, 0]), "pos": np.array([[0, 0, 0.1], [0, 0, 0.3], [0, 0, 0.9]])}
-    # every combination of threads, particles per thread, pass-1 lanes and skin
-    cands = autotune.candidates(threads=(64, 128), ppt=(1, 2, 4), skins=(0, 100), lanes=(1, 2))
-    assert len(cands) == 2 * 3 * 2 * 2 and len(set(cands)) == len(cands)
     assert math.isclose(autotune.surge_speed([st], -9.81), 2 * math.sqrt(9.81 * 0.3))
+    # the default the confirmation runs compare against
+    assert autotune.default_choice("fp32") == {"threads": 256, "ppt": 1, "lanes": 2,
+                                               "skin_permille": 100, "divisions": 1}
+    assert autotune.default_choice("mixed")["threads"] == 128
 
 
 def test_launch_count():

@@ -46,6 +46,7 @@ SPH_OPT_PARTICLES_PER_THREAD = 10
 SPH_OPT_LANES_PER_PARTICLE = 12
 SPH_OPT_PASS1_LANES = 14
 SPH_OPT_ADAPTIVE_SKIN = 13
+SPH_OPT_CELL_DIVISIONS = 16
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
               "mixed_comp": SPH_PREC_MIXED_COMP}

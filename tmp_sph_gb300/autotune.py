@@ -2,20 +2,24 @@
 
 Picks, for one workload on the GPU at hand, the threads per block and particles per thread of
 the neighbour kernels, the lanes per particle of list pass 1 (pass 2 keeps one: lane groups
-made it slower at every G measured) and the neighbour-list skin (which sets the cell size,
-kh (1 + skin)).
+made it slower at every G measured), the neighbour-list skin, and the cell size: cells of
+kh (1 + skin) / d for d = 1, 2 or 3 cells per list cutoff (SPH_OPT_CELL_DIVISIONS; d = 3 gives
+cells of about dx, the reference's own gridSize of opt_src_v4/sph/sph_run.cu:73).
 It loads the workload once; for every candidate it forces one list rebuild, runs two profiled
 steps and reads the per-phase device time (SPH_OPT_PROFILE): the cost of a rebuild (sort,
-gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The step
-cost it ranks by is
+gather, cell starts, list build) and the cost of a half step's two neighbour passes.  The
+model it ranks by is
 
     2 t_pass + r t_rebuild,    r = v dt / (skin kh)   (r = 2 with skin 0),
 
 with r the rebuilds per step a flow carried at v past static walls needs (the list is rebuilt
 once the box of all displacements has a half-diagonal of skin kh / 2, which such a flow reaches
-after moving skin kh).  v defaults to the dam-break surge-front
-speed 2 sqrt(g H) of the tallest water column H, so a short tuning run from rest does not
-reward a large skin for rebuilds the flow has not needed yet.
+after moving skin kh).  v defaults to the dam-break surge-front speed 2 sqrt(g H) of the
+tallest water column H.  The search is staged: the launch shape (threads, particles per
+thread, pass-1 lanes) at the default skin and cell size, then skin and cell size for the best
+shape.  The model's best few and the library default are then run for `confirm_steps` steps
+each (adaptive skin on, as the solver runs them) and the fastest measured wins, so the choice
+is never slower than the default on the workload it was tuned on.
 
     from tmp_sph_gb300 import autotune
     best = autotune.tune(params, states)            # one state dict or a list (batched)
@@ -33,6 +37,8 @@ THREADS = (64, 128, 256)
 PPT = (1, 2, 4)
 LANES = (1, 2, 4)
 SKINS = (0, 50, 100, 150, 200, 300)
+DIVISIONS = (1, 2, 3)
+DEFAULT_SKIN = 100
 
 # profile phases: 0 sort, 1 gather + cell starts, 2 list build, 3 pass 1, 4 pass 2
 _REBUILD = ("sort", "gather_cells", "nbr_build")
@@ -57,12 +63,14 @@ def _upload(sol, states, stream):
         sol.upload_instances(states, stream=stream)
 
 
-def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> dict:
+def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1,
+            divisions: int = 1) -> dict:
     """Rebuild and pass costs (ms) of one candidate on the loaded state, from two profiled
     steps (setting the skin forces the next half step to rebuild; the state advances)."""
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
     sol.set_option(api.SPH_OPT_PASS1_LANES, lanes)
+    sol.set_option(api.SPH_OPT_CELL_DIVISIONS, divisions)
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
     sol.step(1, stream=stream)  # warm: first launches of this shape
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
@@ -77,8 +85,9 @@ def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1) -> d
     t_pass = sum(prof[k]["ms"] for k in _PASSES) / 4.0  # per half step
     # with every half step rebuilding (skin 0) the rebuild time covers four rebuilds
     return {"threads": threads, "ppt": ppt, "lanes": lanes, "skin_permille": skin,
-            "rebuild_ms": t_re / max(1, rebuilds), "pass_ms_per_half_step": t_pass,
-            "rebuilds_seen": rebuilds, "flags": sol.error_flags(stream=stream)}
+            "divisions": divisions, "rebuild_ms": t_re / max(1, rebuilds),
+            "pass_ms_per_half_step": t_pass, "rebuilds_seen": rebuilds,
+            "flags": sol.error_flags(stream=stream)}
 
 
 def step_cost(m: dict, p, v: float) -> float:
@@ -87,35 +96,87 @@ def step_cost(m: dict, p, v: float) -> float:
     return 2.0 * m["pass_ms_per_half_step"] + rate * m["rebuild_ms"]
 
 
-def candidates(threads=THREADS, ppt=PPT, skins=SKINS, lanes=LANES) -> list[tuple]:
-    """(threads, ppt, pass-1 lanes, skin) to measure: every combination (particles per thread
-    apply to pass 2 and the list build whatever pass 1's lanes)."""
-    return [(t, k, g, s) for t, k, g, s in itertools.product(threads, ppt, lanes, skins)]
+def default_choice(precision: str) -> dict:
+    """The library's default: in FP32 256 threads and two pass-1 lanes, otherwise 128 threads
+    and one lane; one particle per thread, skin 0.1 kh, cells of the list cutoff."""
+    fp32 = precision == "fp32"
+    return {"threads": 256 if fp32 else 128, "ppt": 1, "lanes": 2 if fp32 else 1,
+            "skin_permille": DEFAULT_SKIN, "divisions": 1}
+
+
+def _key(m: dict) -> tuple:
+    return (m["threads"], m["ppt"], m["lanes"], m["skin_permille"], m.get("divisions", 1))
+
+
+def timed_run(p, states, choice: dict, precision: str, steps: int, stream) -> float:
+    """Milliseconds per step of `steps` steps from the uploaded states with `choice` applied
+    (adaptive skin on, graph replay), after one warm-up step."""
+    import torch
+    n = sum(len(st["rho"]) for st in states)
+    with S.Solver(p, n, precision=precision) as sol:
+        apply(sol, choice)
+        _upload(sol, states, stream)
+        sol.step(1, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sol.step(steps, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
 
 
 def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=SKINS,
-         lanes=LANES, speed: float | None = None) -> dict:
-    """Best (threads, ppt, lanes, skin) for this workload; `states` is one state dict or a list
-    of them (batched instances).  Returns the choice with the measured table."""
+         lanes=LANES, divisions=DIVISIONS, speed: float | None = None,
+         confirm_steps: int = 100, confirm_top: int = 3) -> dict:
+    """Best (threads, ppt, lanes, skin, divisions) for this workload; `states` is one state dict
+    or a list of them (batched instances).  Returns the choice with the measured table and the
+    confirmation runs."""
     import torch
     states = states if isinstance(states, list) else [states]
     n = sum(len(st["rho"]) for st in states)
     v = speed if speed is not None else surge_speed(states, float(p.gravity))
     stream = torch.cuda.Stream()
     table = []
+    dflt = default_choice(precision)
+    skin0 = dflt["skin_permille"] if dflt["skin_permille"] in skins else skins[0]
     with S.Solver(p, n, precision=precision) as sol:
         # every candidate's lists at its own skin (no adaptive skin while measuring)
         sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, 0)
         _upload(sol, states, stream)
-        for t, k, g, s in candidates(threads, ppt, skins, lanes):
-            m = measure(sol, stream, t, k, s, g)
+        # stage 1: launch shape at the default skin and cell size
+        for t, k, g in itertools.product(threads, ppt, lanes):
+            m = measure(sol, stream, t, k, skin0, g, 1)
+            m["step_ms_estimate"] = step_cost(m, p, v)
+            table.append(m)
+        ok = [m for m in table if m["flags"] == 0] or table
+        shape = min(ok, key=lambda m: m["step_ms_estimate"])
+        # stage 2: skin and cell size for that shape
+        for s_, d in itertools.product(skins, divisions):
+            if s_ == skin0 and d == 1:
+                continue
+            m = measure(sol, stream, shape["threads"], shape["ppt"], s_, shape["lanes"], d)
             m["step_ms_estimate"] = step_cost(m, p, v)
             table.append(m)
     ok = [m for m in table if m["flags"] == 0] or table
-    best = min(ok, key=lambda m: m["step_ms_estimate"])
-    return {"threads": best["threads"], "ppt": best["ppt"], "lanes": best["lanes"],
-            "skin_permille": best["skin_permille"], "speed_m_s": v, "precision": precision,
-            "step_ms_estimate": best["step_ms_estimate"], "table": table}
+    ranked = sorted(ok, key=lambda m: m["step_ms_estimate"])
+    # confirmation: the model's best few and the default, each run as the solver runs it
+    confirm = []
+    seen = set()
+    for m in ranked[:confirm_top] + [dflt]:
+        c = {k: m[k] for k in ("threads", "ppt", "lanes", "skin_permille")}
+        c["divisions"] = m.get("divisions", 1)
+        if _key(c) in seen:
+            continue
+        seen.add(_key(c))
+        c["ms_per_step"] = timed_run(p, states, c, precision, confirm_steps, stream)
+        c["default"] = _key(c) == _key(dflt)
+        confirm.append(c)
+    best = min(confirm, key=lambda c: c["ms_per_step"])
+    out = {k: best[k] for k in ("threads", "ppt", "lanes", "skin_permille", "divisions")}
+    out.update({"speed_m_s": v, "precision": precision, "ms_per_step": best["ms_per_step"],
+                "confirm_steps": confirm_steps, "confirm": confirm, "table": table})
+    return out
 
 
 def apply(sol, best: dict) -> None:
@@ -123,19 +184,16 @@ def apply(sol, best: dict) -> None:
     sol.set_option(api.SPH_OPT_BLOCK_THREADS, best["threads"])
     sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, best["ppt"])
     sol.set_option(api.SPH_OPT_PASS1_LANES, best.get("lanes", 0))
+    sol.set_option(api.SPH_OPT_CELL_DIVISIONS, best.get("divisions", 1))
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, best["skin_permille"])
 
 
 def summary(best: dict) -> dict:
-    """The choice without the table, plus the estimate of the default (in FP32 256 threads and
-    two pass-1 lanes, otherwise 128 threads and one lane; one particle per thread, skin
-    0.1 kh)."""
+    """The choice and the confirmation runs (the default among them), without the table."""
     out = {k: v for k, v in best.items() if k != "table"}
-    fp32 = best.get("precision", "fp32") == "fp32"
-    dflt = (256 if fp32 else 128, 1, 2 if fp32 else 1, 100)
-    for m in best["table"]:
-        if (m["threads"], m["ppt"], m.get("lanes", 1), m["skin_permille"]) == dflt:
-            out["default_step_ms_estimate"] = m["step_ms_estimate"]
+    for c in best.get("confirm", []):
+        if c.get("default"):
+            out["default_ms_per_step"] = c["ms_per_step"]
     return out
 
 

@@ -14,10 +14,12 @@
 // have dofv = 0, so q = p').  It also writes self[i] = (p', rho', dofv, 0) for the particle's
 // own side.
 //
-// Cells are walked as nine x-strips: the three cells (x-1 .. x+1) of one (y, z) row are
+// Cells are walked as x-strips: with cells at least as wide as the list cutoff the 27 cells
+// around a particle's cell are nine strips of three cells (x-1 .. x+1) of one (y, z) row,
 // consecutive in the sorted order, so each strip is one contiguous slot range
 // [cell_start[row + x-1], cell_start[row + x+2]) — the dense cell_start array gives empty cells
-// the start of the next non-empty one.
+// the start of the next non-empty one.  With cells of a half or a third of the cutoff
+// (KParams::reach 2 or 3) the walk covers 25 strips of five cells or 49 strips of seven.
 //
 // Neighbour list.  About 15% of the ~475 candidates of a 27-cell walk lie inside the
 // support radius, and the lanes of a warp (particles of two or three adjacent cells) almost
@@ -150,11 +152,11 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             auto one = [&](int e) {
-                const int j = P::kMixed ? (int)((unsigned)e & IDX_MASK) : e;
+                const int j = P::kMixed ? slot_index(k, e) : e;
                 V a, b;
                 ld_rec(R, j, a, b);
                 T dx, dy, dz;
-                rel_pos<P>(k, pi, a, (unsigned)e >> CODE_SHIFT, dx, dy, dz);
+                rel_pos<P>(k, pi, a, P::kMixed ? slot_code(k, e) : 0u, dx, dy, dz);
                 const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
             };
@@ -185,14 +187,15 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
     if (!keep_all && nl.fluid_cells && !inactive_key(k, keys[i])) {
-        // a boundary particle with no fluid in its 27 cells has an empty list
+        // a boundary particle with no fluid in the cells it walks has an empty list
         int cx, cy, cz;
         cell_of_key(k.gx, k.gy, keys[i], cx, cy, cz);
         bool any = false;
-        for (int z = max(cz - 1, 0); z <= min(cz + 1, k.gz - 1); z++)
-            for (int y = max(cy - 1, 0); y <= min(cy + 1, k.gy - 1); y++) {
+        const int r = k.reach;
+        for (int z = max(cz - r, 0); z <= min(cz + r, k.gz - 1); z++)
+            for (int y = max(cy - r, 0); y <= min(cy + r, k.gy - 1); y++) {
                 const int row = (z * k.gy + y) * k.gx;
-                for (int x = max(cx - 1, 0); x <= min(cx + 1, k.gx - 1); x++)
+                for (int x = max(cx - r, 0); x <= min(cx + r, k.gx - 1); x++)
                     any = any || __ldg(nl.fluid_cells + row + x) != 0;
             }
         if (!any) {
@@ -205,7 +208,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
         if (keep_all || fluid_rec(pj.w))
-            w.put(P::kMixed ? (int)((unsigned)j | (code << CODE_SHIFT)) : j);
+            w.put(P::kMixed ? make_slot(k, j, code) : j);
     });
     w.flush();
     nl.count[i] = w.cnt;

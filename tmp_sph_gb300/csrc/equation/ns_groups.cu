@@ -67,37 +67,6 @@ __device__ __forceinline__ Sum<T, COMP> sum_of(T v) {
     return s;
 }
 
-// The nine x-strips of particle i's cells: strip t is rows (dz, dy) = (t/3 - 1, t%3 - 1), slots
-// [j0, j1); with cell codes, b1 and b2 are the first slots of its second and third cells.
-struct Strip {
-    int j0 = 0, j1 = 0, xl = 0, b1 = 0, b2 = 0;
-};
-
-template <bool CODES, class KP>
-__device__ __forceinline__ Strip strip_of(const KP& k, const int* __restrict__ cs, int cx,
-                                          int cy, int cz, int t) {
-    Strip st;
-    const int z = cz + t / 3 - 1, y = cy + t % 3 - 1;
-    if ((unsigned)z >= (unsigned)k.gz || (unsigned)y >= (unsigned)k.gy) return st;
-    const int row = (z * k.gy + y) * k.gx;
-    st.xl = cx > 0 ? cx - 1 : 0;
-    const int xh = cx < k.gx - 1 ? cx + 1 : k.gx - 1;
-    st.j0 = max(__ldg(cs + row + st.xl), 0);
-    st.j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
-    if constexpr (CODES) {
-        st.b1 = st.xl + 1 <= xh ? __ldg(cs + row + st.xl + 1) : st.j1;
-        st.b2 = st.xl + 2 <= xh ? __ldg(cs + row + st.xl + 2) : st.j1;
-    }
-    return st;
-}
-
-// Cell code of slot j of strip t (its cell relative to (cx, ., .)), as the one-lane walk
-// stores it.
-__device__ __forceinline__ unsigned strip_code(const Strip& st, int t, int cx, int j) {
-    const int xc = st.xl + (j >= st.b1) + (j >= st.b2);
-    return (unsigned)(((t / 3) << 4) | ((t % 3) << 2) | (xc - cx + 1));
-}
-
 // ---------------------------------------------------------------- neighbour visits
 // The group's share of particle i's neighbours (r2 < kh2) with their records: from the list,
 // lane s taking chunks s, s + G, ... of four entries; or, when i overflowed the list, by walking
@@ -116,11 +85,11 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
     const int cnt = __ldg(nl.count + i);
     if (cnt <= nl.cap) {
         auto one = [&](int e) {
-            const int j = P::kMixed ? (int)((unsigned)e & IDX_MASK) : e;
+            const int j = P::kMixed ? slot_index(k, e) : e;
             V a, b;
             ld_rec(R, j, a, b);
             T dx, dy, dz;
-            rel_pos<P>(k, pi, a, (unsigned)e >> CODE_SHIFT, dx, dy, dz);
+            rel_pos<P>(k, pi, a, P::kMixed ? slot_code(k, e) : 0u, dx, dy, dz);
             const T r2 = dist2(dx, dy, dz);
             if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
         };
@@ -132,24 +101,40 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
             for_each_slot<false>(nl.idx + nbr_col(nl, i), cnt, s, G, one);
         return;
     }
+    // the cells one by one (each a contiguous slot range), G candidates per step
     const unsigned key = keys[i];
     if (inactive_key(k, key)) return;
     int cx, cy, cz;
     cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+    const int r = k.reach;
+    const int xl = cx > r - 1 ? cx - r : 0;
+    const int xh = cx < k.gx - r ? cx + r : k.gx - 1;
 #pragma unroll 1
-    for (int t = 0; t < 9; t++) {
-        const Strip st = strip_of<P::kMixed>(k, cs, cx, cy, cz, t);
+    for (int dz = -r; dz <= r; dz++) {
+        const int z = cz + dz;
+        if ((unsigned)z >= (unsigned)k.gz) continue;
 #pragma unroll 1
-        for (int j = st.j0 + s; j < st.j1; j += G) {
-            const V pj = ld_pos(X, (size_t)XSTRIDE * (size_t)j);
-            const unsigned code = P::kMixed ? strip_code(st, t, cx, j) : 0u;
-            T dx, dy, dz;
-            rel_pos<P>(k, pi, pj, code, dx, dy, dz);
-            const T r2 = dist2(dx, dy, dz);
-            if (r2 < k.kh2 && j != i) {
-                V a, b;
-                ld_rec(R, j, a, b);
-                f(j, a, b, dx, dy, dz, r2);
+        for (int dy = -r; dy <= r; dy++) {
+            const int y = cy + dy;
+            if ((unsigned)y >= (unsigned)k.gy) continue;
+            const int row = (z * k.gy + y) * k.gx;
+#pragma unroll 1
+            for (int xc = xl; xc <= xh; xc++) {
+                const unsigned code = P::kMixed ? cell_code(k, xc - cx, dy, dz) : 0u;
+                const int j0 = max(__ldg(cs + row + xc), 0);
+                const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
+#pragma unroll 1
+                for (int j = j0 + s; j < j1; j += G) {
+                    const V pj = ld_pos(X, (size_t)XSTRIDE * (size_t)j);
+                    T dx, dy2, dz2;
+                    rel_pos<P>(k, pi, pj, code, dx, dy2, dz2);
+                    const T r2 = dist2(dx, dy2, dz2);
+                    if (r2 < k.kh2 && j != i) {
+                        V a, b;
+                        ld_rec(R, j, a, b);
+                        f(j, a, b, dx, dy2, dz2, r2);
+                    }
+                }
             }
         }
     }

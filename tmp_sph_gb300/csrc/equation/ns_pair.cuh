@@ -18,9 +18,26 @@ namespace {
 // are picked by the autotuner.  ppt > 1 runs the grid-stride instantiation (GS), which holds
 // its loop state in registers (pass 2: 64 instead of 48), so ppt = 1 has its own.
 constexpr int NS_MAX_THREADS = 256;
-// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^26).
-constexpr int CODE_SHIFT = 26;
-constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
+// Mixed precision: a list slot is j | code << k.code_shift (j < 2^code_shift), code the
+// neighbour's cell relative to i's (cell_code).
+template <class KP>
+__device__ __forceinline__ int slot_index(const KP& k, int e) {
+    return (int)((unsigned)e & ((1u << k.code_shift) - 1u));
+}
+template <class KP>
+__device__ __forceinline__ unsigned slot_code(const KP& k, int e) {
+    return (unsigned)e >> k.code_shift;
+}
+template <class KP>
+__device__ __forceinline__ int make_slot(const KP& k, int j, unsigned code) {
+    return (int)((unsigned)j | (code << k.code_shift));
+}
+// Cell (dx, dy, dz) relative to i's, each in [-reach, reach], as code_bits bits per axis.
+template <class KP>
+__device__ __forceinline__ unsigned cell_code(const KP& k, int dx, int dy, int dz) {
+    const int r = k.reach, b = k.code_bits;
+    return (unsigned)(((dz + r) << (2 * b)) | ((dy + r) << b) | (dx + r));
+}
 
 // Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
 // col + 32 * 4g (col = the warp's block + 4 * lane).  The 32 particles of a warp share one block
@@ -129,29 +146,29 @@ struct Sum {
     }
 };
 
-// Visit every candidate slot j of the 27 cells around (cx, cy, cz): f(j, code).  Without CODES
-// each x-strip is one range and code is 0; with CODES the strip's three cells are visited one
-// by one and code = (dz+1) << 4 | (dy+1) << 2 | (dx+1) is j's cell relative to (cx, cy, cz).
-// Both visit the same slots in the same order.
+// Visit every candidate slot j of the (2 reach + 1)^3 cells around (cx, cy, cz): f(j, code).
+// Without CODES each x-strip is one range and code is 0; with CODES the strip's cells are
+// visited one by one and code = cell_code(j's cell relative to (cx, cy, cz)).  Both visit the
+// same slots in the same order.
 template <bool CODES, class KP, class F>
 __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
                                                    int cx, int cy, int cz, F&& f) {
-    const int xl = cx > 0 ? cx - 1 : 0;
-    const int xh = cx < k.gx - 1 ? cx + 1 : k.gx - 1;
+    const int r = k.reach;
+    const int xl = cx > r - 1 ? cx - r : 0;
+    const int xh = cx < k.gx - r ? cx + r : k.gx - 1;
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; dz++) {
+    for (int dz = -r; dz <= r; dz++) {
         const int z = cz + dz;
         if ((unsigned)z >= (unsigned)k.gz) continue;
 #pragma unroll 1
-        for (int dy = -1; dy <= 1; dy++) {
+        for (int dy = -r; dy <= r; dy++) {
             const int y = cy + dy;
             if ((unsigned)y >= (unsigned)k.gy) continue;
             const int row = (z * k.gy + y) * k.gx;
             if constexpr (CODES) {
 #pragma unroll 1
                 for (int xc = xl; xc <= xh; xc++) {
-                    const unsigned code =
-                        (unsigned)(((dz + 1) << 4) | ((dy + 1) << 2) | (xc - cx + 1));
+                    const unsigned code = cell_code(k, xc - cx, dy, dz);
                     const int j0 = max(__ldg(cs + row + xc), 0);
                     const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
                     for (int j = j0; j < j1; j++) f(j, code);
@@ -204,9 +221,10 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
                                         typename P::T& dy, typename P::T& dz) {
     using T = typename P::T;
     if constexpr (P::kMixed) {
-        const int rz = (int)(code >> 4) - 1;
-        const int ry = (int)((code >> 2) & 3u) - 1;
-        const int rx = (int)(code & 3u) - 1;
+        const unsigned b = (unsigned)k.code_bits, m = (1u << b) - 1u;
+        const int rz = (int)(code >> (2u * b)) - k.reach;
+        const int ry = (int)((code >> b) & m) - k.reach;
+        const int rx = (int)(code & m) - k.reach;
         dx = (pi.x - pj.x) - (T)rx * k.cell;
         dy = (pi.y - pj.y) - (T)ry * k.cell;
         dz = (pi.z - pj.z) - (T)rz * k.cell;

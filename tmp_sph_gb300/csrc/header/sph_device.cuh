@@ -41,11 +41,18 @@ struct KParamsT {
     int n;
     int gx, gy, gz;      // grid dimensions
     int num_cells;
-    // Batched instances are stacked along z, each gz_local cells high plus one empty layer,
-    // so the resident key of a particle of instance b is b * inst_cells + its cell in its own
-    // grid.  A single simulation has gz_local = gz and inst_cells = 0.
+    // Batched instances are stacked along z, each gz_local cells high plus `reach` empty
+    // layers, so the resident key of a particle of instance b is b * inst_cells + its cell in
+    // its own grid.  A single simulation has gz_local = gz and inst_cells = 0.
     int gz_local;
     int inst_cells;
+    // Cells walked on each side of a particle's cell: 1 (27 cells of at least the list cutoff),
+    // 2 or 3 (cells of a half or a third of it: 125 or 343 cells, fewer candidates in all).
+    // Mixed-precision list slots keep a neighbour's cell relative to i's in code_bits bits per
+    // axis (2 for reach 1, else 3) above bit code_shift = 32 - 3 code_bits.
+    int reach;
+    int code_bits;
+    int code_shift;
     // Launch shape of the neighbour kernels (host side): threads per block (multiple of 32, at
     // most 256) and particles per thread.
     int threads;
@@ -128,7 +135,7 @@ __device__ __forceinline__ void cell_origin(const KParamsT<KT>& k, unsigned key,
                                             double& oy, double& oz) {
     int cx, cy, cz;
     cell_of_key(k.gx, k.gy, key, cx, cy, cz);
-    if (k.inst_cells) cz %= k.gz_local + 1;
+    if (k.inst_cells) cz %= k.gz_local + k.reach;
     ox = (double)k.gmin_x + (double)cx * (double)k.cell;
     oy = (double)k.gmin_y + (double)cy * (double)k.cell;
     oz = (double)k.gmin_z + (double)cz * (double)k.cell;

@@ -203,21 +203,26 @@ bool params_ok(const sph_params* p) {
 
 constexpr int EV_PER_HALF = PH_COUNT + 1;
 
+// Bits of a mixed-precision list slot that hold the neighbour's index (the rest hold its cell
+// relative to the particle's: 2 bits per axis with one cell walked on each side, 3 with more).
+int mixed_index_bits(const sph_ctx* c) { return c->opt_reach > 1 ? 23 : 26; }
+
 // The neighbour list to use this half step, or NULL to walk the cells in every pass.
 const NbrList* list_for(sph_ctx* c) {
     c->nl.fluid_cells = c->fluid_cells;
     return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr;
 }
 
-// The resident solver's own grid: the caller's grid box with cells of kh (1 + skin), so a walk
-// of the 27 cells around a particle's cell at the last rebuild still finds every particle
-// within kh of it while no particle has moved more than skin/2.  skin = 0 keeps the caller's
-// grid exactly (cells of kh).
-sph_params internal_params(const sph_params& P, double skin) {
-    if (!(skin > 0.0)) return P;
+// The resident solver's own grid: the caller's grid box with cells of kh (1 + skin) / reach,
+// so a walk of the reach cells on each side of a particle's cell at the last rebuild still
+// finds every particle within kh of it while no particle has moved more than skin/2.  skin = 0
+// and reach 1 keep the caller's grid exactly (cells of kh).
+sph_params internal_params(const sph_params& P, double skin, int reach) {
+    if (!(skin > 0.0) && reach <= 1) return P;
     sph_params Q = P;
-    Q.cell_size = (float)((double)P.kh * (1.0 + skin));
-    if (Q.cell_size < P.cell_size) Q.cell_size = P.cell_size;
+    float base = skin > 0.0 ? (float)((double)P.kh * (1.0 + skin)) : P.cell_size;
+    if (base < P.cell_size) base = P.cell_size;
+    Q.cell_size = reach > 1 ? (float)((double)base / (double)reach) : base;
     for (int c = 0; c < 3; c++) {
         float span = (Q.grid_max[c] - Q.grid_min[c]) / Q.cell_size;
         Q.grid_dim[c] = (int)ceilf(span);
@@ -227,15 +232,16 @@ sph_params internal_params(const sph_params& P, double skin) {
     return Q;
 }
 
-// The solver's grid for n_inst batched instances: the instances' grids stacked along z, one
-// empty cell layer between consecutive instances, so no 27-cell walk reaches another instance.
+// The solver's grid for n_inst batched instances: the instances' grids stacked along z, `reach`
+// empty cell layers between consecutive instances, so no cell walk reaches another instance.
 // *gz_local receives the height of one instance's grid.  Returns false when the stacked grid
 // does not fit the key range.
-bool stacked_params(const sph_params& P, double skin, int n_inst, sph_params* out, int* gz_local) {
-    sph_params Q = internal_params(P, skin);
+bool stacked_params(const sph_params& P, double skin, int reach, int n_inst, sph_params* out,
+                    int* gz_local) {
+    sph_params Q = internal_params(P, skin, reach);
     *gz_local = Q.grid_dim[2];
     if (n_inst > 1) {
-        const long long gz = (long long)n_inst * (Q.grid_dim[2] + 1);
+        const long long gz = (long long)n_inst * (Q.grid_dim[2] + reach);
         const long long cells = (long long)Q.grid_dim[0] * Q.grid_dim[1] * gz;
         if (cells >= (1LL << 30)) return false;
         Q.grid_dim[2] = (int)gz;
@@ -277,7 +283,11 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     const bool groups = c->opt_nbr_list && c->nl.idx;
     k.lanes = groups ? pass1_lanes(c) : 1;
     k.list_win = k.lanes > 1;
-    k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + 1) : 0;
+    k.reach = c->opt_reach;
+    k.code_bits = c->opt_reach > 1 ? 3 : 2;
+    k.code_shift = 32 - 3 * k.code_bits;
+    k.inst_cells =
+        c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + c->opt_reach) : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
@@ -557,7 +567,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     sph_ctx* c = new (std::nothrow) sph_ctx();
     if (!c) return SPH_ERR_NOMEM;
     c->P = *p;
-    stacked_params(*p, c->skin, 1, &c->Pi, &c->gz_inst);
+    stacked_params(*p, c->skin, c->opt_reach, 1, &c->Pi, &c->gz_inst);
     c->capacity = capacity;
     cudaGetDevice(&c->device);
     cudaError_t e = cudaSuccess;
@@ -634,7 +644,7 @@ extern "C" int sph_set_params(sph_ctx* c, const sph_params* p) {
     if (!c || !params_ok(p)) return SPH_ERR_ARG;
     sph_params pi;
     int gz_local;
-    if (!stacked_params(*p, c->skin, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
+    if (!stacked_params(*p, c->skin, c->opt_reach, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
     if (ensure_cells(c, std::max(p->num_cells, pi.num_cells)) != cudaSuccess) return SPH_ERR_NOMEM;
     c->P = *p;
     c->Pi = pi;
@@ -692,6 +702,21 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             break;  // the slot order of the lists changed: rebuild
         }
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
+        case SPH_OPT_CELL_DIVISIONS: {
+            if (value < 1 || value > 3) return SPH_ERR_ARG;
+            if (value == c->opt_reach) return SPH_OK;
+            if (prec_is_mixed(c->prec) && c->n >= (1 << (value > 1 ? 23 : 26))) return SPH_ERR_ARG;
+            sph_params pi;
+            int gz_local;
+            if (!stacked_params(c->P, c->skin, value, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
+            if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
+            c->opt_reach = value;
+            c->Pi = pi;
+            c->gz_inst = gz_local;
+            c->rehash = c->loaded;  // the keys pass 2 wrote index the old grid
+            drop_graph(c);
+            break;
+        }
         case SPH_OPT_PRECISION: {
             if (value != SPH_PREC_FP32 && value != SPH_PREC_FP64 && !prec_is_mixed(value))
                 return SPH_ERR_ARG;
@@ -726,7 +751,7 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
                 if (c->P.num_cells <= 0) return SPH_ERR_STATE;
                 sph_params pi;
                 int gz_local;
-                if (!stacked_params(c->P, value / 1000.0, c->n_inst, &pi, &gz_local))
+                if (!stacked_params(c->P, value / 1000.0, c->opt_reach, c->n_inst, &pi, &gz_local))
                     return SPH_ERR_ARG;
                 if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
                 c->skin = value / 1000.0;
@@ -762,6 +787,7 @@ extern "C" int sph_ctx_get_option(const sph_ctx* c, int option, int* value) {
         case SPH_OPT_BLOCK_THREADS: *value = block_threads(c); break;
         case SPH_OPT_PARTICLES_PER_THREAD: *value = c->opt_ppt; break;
         case SPH_OPT_ADAPTIVE_SKIN: *value = c->opt_adaptive_skin; break;
+        case SPH_OPT_CELL_DIVISIONS: *value = c->opt_reach; break;
         case SPH_OPT_LANES_PER_PARTICLE:
         case SPH_OPT_PASS1_LANES: *value = pass1_lanes(c); break;
         default: return SPH_ERR_ARG;
@@ -775,8 +801,9 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
                        int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
-    // mixed-precision list slots keep the neighbour index in 26 bits
-    if (prec_is_mixed(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
+    // mixed-precision list slots keep the neighbour index in 26 bits (23 with cells smaller
+    // than the cutoff)
+    if (prec_is_mixed(c->prec) && n >= (1 << mixed_index_bits(c))) return SPH_ERR_ARG;
     if (n_inst < 1 || n_inst > SPH_MAX_INSTANCES) return SPH_ERR_ARG;
     if (n_inst > 1) {
         if (!offsets || offsets[0] != 0 || offsets[n_inst] != n) return SPH_ERR_ARG;
@@ -793,7 +820,7 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
     if (n_inst != c->n_inst) {
         sph_params pi;
         int gz_local;
-        if (!stacked_params(c->P, c->skin, n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
+        if (!stacked_params(c->P, c->skin, c->opt_reach, n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
         if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
         c->Pi = pi;
         c->gz_inst = gz_local;

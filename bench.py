@@ -410,16 +410,20 @@ def configured_run(sol, stream, st, n: int, n_fluid: int, run_steps: int, steps:
 
 
 def set_lanes(sol, args) -> None:
-    """Lanes per particle of list pass 1 (--pass1-lanes; 0: the precision's default)."""
+    """Lanes per particle of list pass 1 (--pass1-lanes; 0: the precision's default) and the
+    cell size (--divisions; 0: the library's default)."""
     from tmp_sph_gb300 import api
     sol.set_option(api.SPH_OPT_PASS1_LANES, args.pass1_lanes)
+    if args.divisions:
+        sol.set_option(api.SPH_OPT_CELL_DIVISIONS, args.divisions)
 
 
 def lanes_in_effect(sol) -> dict:
     """Launch shape of the neighbour kernels in effect (defaults resolved)."""
     from tmp_sph_gb300 import api
     return {"lanes_per_particle_pass1_pass2": [sol.get_option(api.SPH_OPT_PASS1_LANES), 1],
-            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS)}
+            "block_threads": sol.get_option(api.SPH_OPT_BLOCK_THREADS),
+            "cell_divisions": sol.get_option(api.SPH_OPT_CELL_DIVISIONS)}
 
 
 def config_block(args, p, n, lanes=None):
@@ -589,7 +593,8 @@ def sol_cells_batch(p, n_inst: int, skin: int, divisions: int = 1) -> int:
     import math
     cell = max(float(p.kh) * (1.0 + skin / 1000.0), float(p.cell_size)) / divisions
     dims = [max(1, math.ceil((p.grid_max[c] - p.grid_min[c]) / cell)) for c in range(3)]
-    return dims[0] * dims[1] * n_inst * (dims[2] + divisions)
+    stride = (dims[2] + 2 * divisions - 1) // divisions * divisions
+    return dims[0] * dims[1] * n_inst * stride
 
 
 # ---------------------------------------------------------------- --components
@@ -763,6 +768,9 @@ def main():
                          "autotuner first (overrides --skin)")
     ap.add_argument("--pass1-lanes", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
                     help="lanes per particle in list pass 1 (0: 2 in FP32 with a skin, else 1)")
+    ap.add_argument("--divisions", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="cells per list cutoff (SPH_OPT_CELL_DIVISIONS; 0: the library's "
+                         "default)")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
     ap.add_argument("--skin", type=int, default=100,
@@ -897,7 +905,8 @@ def main():
     dom_ms = phases[dom]["ms_per_launch"]
     workload = f"dam_break_{args.case}_{args.precision}"
     shape = {"block_threads": lanes["block_threads"],
-             "lanes_pass1": lanes["lanes_per_particle_pass1_pass2"][0]}
+             "lanes_pass1": lanes["lanes_per_particle_pass1_pass2"][0],
+             "cell_divisions": lanes["cell_divisions"]}
     cap = ncu_capture(dom, workload, shape)
     traffic = cap.get("dram_bytes_per_launch")
     roof = {"bound": "hbm", "kernel": PHASE_KERNEL[dom],

@@ -281,13 +281,14 @@ typedef struct sph_ctx sph_ctx;
                              per particle (groups were slower there at every size measured) */
 #define SPH_OPT_PASS1_LANES 14  /* the same as SPH_OPT_LANES_PER_PARTICLE */
 /* 15 is not used (it selected lane groups in pass 2, removed) */
-#define SPH_OPT_CELL_DIVISIONS 16  /* cells per list cutoff of the resident grid: 1 (default:
-                             cells of kh (1 + skin), the 27 around a particle's cell walked), 2
-                             (cells of half that, 125 walked) or 3 (a third, about dx at
-                             h = 1.3 dx: 343 walked, the reference's gridSize = dx of
-                             opt_src_v4/sph/sph_run.cu:73).  Smaller cells give the list build
-                             fewer candidates for more cell lookups.  Mixed precision with 2 or
-                             3 holds at most 2^23 - 1 particles (2^26 - 1 with 1) */
+#define SPH_OPT_CELL_DIVISIONS 16  /* cells per list cutoff of the resident grid: 1 (cells
+                             of kh (1 + skin), the 27 around a particle's cell walked), 2 (cells
+                             of half that, 125 walked) or 3 (a third, about dx at h = 1.3 dx:
+                             343 walked, the reference's gridSize = dx of
+                             opt_src_v4/sph/sph_run.cu:73); 0 (default): 3 in FP32, 1 in the
+                             other precisions.  Smaller cells give the list build
+                             fewer candidates for more cell lookups, and order the particles of
+                             the cell-sorted state along finer x rows */
 
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */

@@ -3,9 +3,9 @@ a half or a third of the list cutoff and the cell walks cover 125 or 343 cells. 
 finds the same pairs in another order, so the fields follow the oracle to FP32 rounding; with
 one lane per particle the neighbour-list passes and the passes that walk the cells themselves
 still visit the same pairs in the same order (bitwise); batched instances stay apart (the
-stacked grid keeps as many empty layers between instances as cells are walked on each side),
-so each instance of a batch equals its solo run bit for bit with the lists rebuilt every half
-step."""
+stacked grid keeps at least as many empty layers between instances as cells are walked on each
+side), so each instance of a batch equals its solo run bit for bit with the lists rebuilt every
+half step."""
 from __future__ import annotations
 
 import numpy as np
@@ -28,8 +28,8 @@ def run(st, p, nsteps, precision="fp32", opts=None):
         out = sol.download(stream=s)
         out["flags"] = sol.error_flags(stream=s)
         out["rebuilds"] = sol.rebuild_count(stream=s)
-        assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == (opts or {}).get(
-            api.SPH_OPT_CELL_DIVISIONS, 1)
+        if api.SPH_OPT_CELL_DIVISIONS in (opts or {}):
+            assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == opts[api.SPH_OPT_CELL_DIVISIONS]
     return out
 
 
@@ -65,14 +65,18 @@ def test_divisions_list_equals_walk(sphlib, cuda, div):
 
 
 @pytest.mark.parametrize("div", [2, 3])
-def test_divisions_batch_equals_solo(sphlib, cuda, div):
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_divisions_batch_equals_solo(sphlib, cuda, div, precision):
+    """Mixed precision anchors a particle's offsets at a cell whose coordinates are multiples of
+    the reach; the instances are stacked every multiple of the reach, so an instance's anchors,
+    offsets and sums are those of its solo run."""
     import torch
     from tmp_sph_gb300 import api, cases, solver as S
     states, p = cases.batch(3, dx=0.02, seed=5)
     n = sum(len(st["rho"]) for st in states)
     opts = {api.SPH_OPT_CELL_DIVISIONS: div, api.SPH_OPT_SKIN_PERMILLE: 0}
     s = torch.cuda.Stream()
-    with S.Solver(p, n) as sol:
+    with S.Solver(p, n, precision=precision) as sol:
         for k, v in opts.items():
             sol.set_option(k, v)
         off = sol.upload_instances(states, stream=s)
@@ -80,7 +84,7 @@ def test_divisions_batch_equals_solo(sphlib, cuda, div):
         out = sol.download(stream=s)
         assert sol.error_flags(stream=s) == 0
     for b, st in enumerate(states):
-        ref = run(st, p, 5, opts=opts)
+        ref = run(st, p, 5, precision, opts=opts)
         sl = slice(int(off[b]), int(off[b + 1]))
         for k in ("pos", "vel", "rho", "p"):
             assert np.array_equal(out[k][sl], ref[k]), (b, k)
@@ -95,9 +99,11 @@ def test_divisions_switch_and_checks(sphlib, cuda):
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
     s = torch.cuda.Stream()
     with S.Solver(p, len(st["rho"])) as sol:
-        for bad in (0, 4, -1):
+        assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == 3  # the FP32 default
+        for bad in (4, -1):
             with pytest.raises(api.SphError):
                 sol.set_option(api.SPH_OPT_CELL_DIVISIONS, bad)
+        sol.set_option(api.SPH_OPT_CELL_DIVISIONS, 1)
         sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
         sol.step(3, stream=s)
         r0 = sol.rebuild_count(stream=s)
@@ -111,3 +117,19 @@ def test_divisions_switch_and_checks(sphlib, cuda):
     fl = st["type"] == 1
     e = rel_l2(out["vel"][fl], ref["vel"][fl], floor=1e-3 * np.sqrt(fl.sum()))
     assert e < 1e-5, e
+
+
+def test_divisions_defaults(sphlib, cuda):
+    """Cells of a third of the list cutoff in FP32, of the cutoff in the other precisions; a
+    precision change moves the default along unless the caller set the cell size."""
+    from tmp_sph_gb300 import api, cases, solver as S
+    _, p = cases.build("small", physics="config", dx=0.04)
+    for prec, want in (("fp32", 3), ("mixed", 1), ("mixed_comp", 1), ("fp64", 1)):
+        with S.Solver(p, 1000, precision=prec) as sol:
+            assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == want, prec
+    with S.Solver(p, 1000) as sol:
+        sol.set_option(api.SPH_OPT_CELL_DIVISIONS, 2)
+        sol.set_option(api.SPH_OPT_PRECISION, api.PRECISIONS["mixed"])
+        assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == 2
+        sol.set_option(api.SPH_OPT_CELL_DIVISIONS, 0)
+        assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == 1

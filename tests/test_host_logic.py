@@ -45,7 +45,7 @@ def test_autotune_cost_model():
     assert math.isclose(autotune.surge_speed([st], -9.81), 2 * math.sqrt(9.81 * 0.3))
     # the default the confirmation runs compare against
     assert autotune.default_choice("fp32") == {"threads": 256, "ppt": 1, "lanes": 2,
-                                               "skin_permille": 100, "divisions": 1}
+                                               "skin_permille": 100, "divisions": 3}
     assert autotune.default_choice("mixed")["threads"] == 128
 
 

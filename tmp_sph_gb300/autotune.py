@@ -64,14 +64,19 @@ def _upload(sol, states, stream):
 
 
 def measure(sol, stream, threads: int, ppt: int, skin: int, lanes: int = 1,
-            divisions: int = 1) -> dict:
+            divisions: int = 1) -> dict | None:
     """Rebuild and pass costs (ms) of one candidate on the loaded state, from two profiled
-    steps (setting the skin forces the next half step to rebuild; the state advances)."""
-    sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
-    sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
-    sol.set_option(api.SPH_OPT_PASS1_LANES, lanes)
-    sol.set_option(api.SPH_OPT_CELL_DIVISIONS, divisions)
-    sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+    steps (setting the skin forces the next half step to rebuild; the state advances).  None
+    when the solver refuses the candidate (e.g. a cell size whose stacked grid of many
+    instances would not fit the key range)."""
+    try:
+        sol.set_option(api.SPH_OPT_BLOCK_THREADS, threads)
+        sol.set_option(api.SPH_OPT_PARTICLES_PER_THREAD, ppt)
+        sol.set_option(api.SPH_OPT_PASS1_LANES, lanes)
+        sol.set_option(api.SPH_OPT_CELL_DIVISIONS, divisions)
+        sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+    except api.SphError:
+        return None
     sol.step(1, stream=stream)  # warm: first launches of this shape
     sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)  # force one rebuild in the profiled steps
     r0 = sol.rebuild_count(stream=stream)
@@ -97,11 +102,12 @@ def step_cost(m: dict, p, v: float) -> float:
 
 
 def default_choice(precision: str) -> dict:
-    """The library's default: in FP32 256 threads and two pass-1 lanes, otherwise 128 threads
-    and one lane; one particle per thread, skin 0.1 kh, cells of the list cutoff."""
+    """The library's default: in FP32 256 threads, two pass-1 lanes and cells of a third of
+    the list cutoff, otherwise 128 threads, one lane and cells of the cutoff; one particle per
+    thread and skin 0.1 kh in all."""
     fp32 = precision == "fp32"
     return {"threads": 256 if fp32 else 128, "ppt": 1, "lanes": 2 if fp32 else 1,
-            "skin_permille": DEFAULT_SKIN, "divisions": 1}
+            "skin_permille": DEFAULT_SKIN, "divisions": 3 if fp32 else 1}
 
 
 def _key(m: dict) -> tuple:
@@ -140,22 +146,27 @@ def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=
     table = []
     dflt = default_choice(precision)
     skin0 = dflt["skin_permille"] if dflt["skin_permille"] in skins else skins[0]
+    div0 = dflt["divisions"] if dflt["divisions"] in divisions else divisions[0]
     with S.Solver(p, n, precision=precision) as sol:
         # every candidate's lists at its own skin (no adaptive skin while measuring)
         sol.set_option(api.SPH_OPT_ADAPTIVE_SKIN, 0)
         _upload(sol, states, stream)
         # stage 1: launch shape at the default skin and cell size
         for t, k, g in itertools.product(threads, ppt, lanes):
-            m = measure(sol, stream, t, k, skin0, g, 1)
+            m = measure(sol, stream, t, k, skin0, g, div0)
+            if m is None:
+                continue
             m["step_ms_estimate"] = step_cost(m, p, v)
             table.append(m)
         ok = [m for m in table if m["flags"] == 0] or table
         shape = min(ok, key=lambda m: m["step_ms_estimate"])
         # stage 2: skin and cell size for that shape
         for s_, d in itertools.product(skins, divisions):
-            if s_ == skin0 and d == 1:
+            if s_ == skin0 and d == div0:
                 continue
             m = measure(sol, stream, shape["threads"], shape["ppt"], s_, shape["lanes"], d)
+            if m is None:
+                continue
             m["step_ms_estimate"] = step_cost(m, p, v)
             table.append(m)
     ok = [m for m in table if m["flags"] == 0] or table

@@ -152,11 +152,11 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             auto one = [&](int e) {
-                const int j = P::kMixed ? slot_index(k, e) : e;
+                const int j = P::kMixed ? slot_index(e) : e;
                 V a, b;
                 ld_rec(R, j, a, b);
                 T dx, dy, dz;
-                rel_pos<P>(k, pi, a, P::kMixed ? slot_code(k, e) : 0u, dx, dy, dz);
+                rel_pos<P>(k, pi, a, P::kMixed ? slot_code(e) : 0u, dx, dy, dz);
                 const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
             };
@@ -208,7 +208,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
         if (keep_all || fluid_rec(pj.w))
-            w.put(P::kMixed ? make_slot(k, j, code) : j);
+            w.put(P::kMixed ? make_slot(j, code) : j);
     });
     w.flush();
     nl.count[i] = w.cnt;

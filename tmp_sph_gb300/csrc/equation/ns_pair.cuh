@@ -18,25 +18,26 @@ namespace {
 // are picked by the autotuner.  ppt > 1 runs the grid-stride instantiation (GS), which holds
 // its loop state in registers (pass 2: 64 instead of 48), so ppt = 1 has its own.
 constexpr int NS_MAX_THREADS = 256;
-// Mixed precision: a list slot is j | code << k.code_shift (j < 2^code_shift), code the
-// neighbour's cell relative to i's (cell_code).
-template <class KP>
-__device__ __forceinline__ int slot_index(const KP& k, int e) {
-    return (int)((unsigned)e & ((1u << k.code_shift) - 1u));
+// Mixed precision: a list slot is j | code << CODE_SHIFT (j < 2^26), code the neighbour's
+// anchor cell relative to i's (cell_code).
+constexpr int CODE_SHIFT = 26;
+constexpr unsigned IDX_MASK = (1u << CODE_SHIFT) - 1u;
+__device__ __forceinline__ int slot_index(int e) { return (int)((unsigned)e & IDX_MASK); }
+__device__ __forceinline__ unsigned slot_code(int e) { return (unsigned)e >> CODE_SHIFT; }
+__device__ __forceinline__ int make_slot(int j, unsigned code) {
+    return (int)((unsigned)j | (code << CODE_SHIFT));
 }
+// Code of a neighbour cell (xj, yj, zj) seen from cell (xi, yi, zi), both within one walk:
+// the difference of their anchors (anchor_of) in anchor steps, each in {-1, 0, 1}, two bits
+// per axis, (dz+1) << 4 | (dy+1) << 2 | (dx+1).
 template <class KP>
-__device__ __forceinline__ unsigned slot_code(const KP& k, int e) {
-    return (unsigned)e >> k.code_shift;
-}
-template <class KP>
-__device__ __forceinline__ int make_slot(const KP& k, int j, unsigned code) {
-    return (int)((unsigned)j | (code << k.code_shift));
-}
-// Cell (dx, dy, dz) relative to i's, each in [-reach, reach], as code_bits bits per axis.
-template <class KP>
-__device__ __forceinline__ unsigned cell_code(const KP& k, int dx, int dy, int dz) {
-    const int r = k.reach, b = k.code_bits;
-    return (unsigned)(((dz + r) << (2 * b)) | ((dy + r) << b) | (dx + r));
+__device__ __forceinline__ unsigned cell_code(const KP& k, int xi, int yi, int zi, int xj, int yj,
+                                              int zj) {
+    const int r = k.reach;
+    const int dx = (anchor_of(xj, r) - anchor_of(xi, r)) / r;
+    const int dy = (anchor_of(yj, r) - anchor_of(yi, r)) / r;
+    const int dz = (anchor_of(zj, r) - anchor_of(zi, r)) / r;
+    return (unsigned)(((dz + 1) << 4) | ((dy + 1) << 2) | (dx + 1));
 }
 
 // Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
@@ -148,7 +149,7 @@ struct Sum {
 
 // Visit every candidate slot j of the (2 reach + 1)^3 cells around (cx, cy, cz): f(j, code).
 // Without CODES each x-strip is one range and code is 0; with CODES the strip's cells are
-// visited one by one and code = cell_code(j's cell relative to (cx, cy, cz)).  Both visit the
+// visited one by one and code = cell_code of j's cell seen from (cx, cy, cz).  Both visit the
 // same slots in the same order.
 template <bool CODES, class KP, class F>
 __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
@@ -166,12 +167,15 @@ __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __res
             if ((unsigned)y >= (unsigned)k.gy) continue;
             const int row = (z * k.gy + y) * k.gx;
             if constexpr (CODES) {
+                // the strip in runs of cells that share an anchor column (one code per run)
 #pragma unroll 1
-                for (int xc = xl; xc <= xh; xc++) {
-                    const unsigned code = cell_code(k, xc - cx, dy, dz);
-                    const int j0 = max(__ldg(cs + row + xc), 0);
-                    const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
+                for (int xa = xl; xa <= xh;) {
+                    const int xb = min(anchor_of(xa, r) + r - 1, xh);
+                    const unsigned code = cell_code(k, cx, cy, cz, xa, y, z);
+                    const int j0 = max(__ldg(cs + row + xa), 0);
+                    const int j1 = min(__ldg(cs + row + xb + 1), k.n);  // bounds guard only
                     for (int j = j0; j < j1; j++) f(j, code);
+                    xa = xb + 1;
                 }
             } else {
                 const int j0 = max(__ldg(cs + row + xl), 0);
@@ -214,20 +218,22 @@ __device__ __forceinline__ dvec4 ld_pos(const dvec4* __restrict__ X, size_t j) {
 }
 
 // Relative position r = x_i - x_j of a pair: from absolute positions, or (mixed precision)
-// from cell-local offsets and j's cell relative to i's.
+// from the offsets from their anchor cells and j's anchor relative to i's (anchor steps of
+// reach cells).
 template <class P, class V>
 __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const V& pi,
                                         const V& pj, unsigned code, typename P::T& dx,
                                         typename P::T& dy, typename P::T& dz) {
     using T = typename P::T;
     if constexpr (P::kMixed) {
-        const unsigned b = (unsigned)k.code_bits, m = (1u << b) - 1u;
-        const int rz = (int)(code >> (2u * b)) - k.reach;
-        const int ry = (int)((code >> b) & m) - k.reach;
-        const int rx = (int)(code & m) - k.reach;
-        dx = (pi.x - pj.x) - (T)rx * k.cell;
-        dy = (pi.y - pj.y) - (T)ry * k.cell;
-        dz = (pi.z - pj.z) - (T)rz * k.cell;
+        // one explicitly rounded difference and one fused multiply-add per axis, so every
+        // caller (list, cell walk, list build) gets the same bits whatever the compiler hoists
+        const int rz = ((int)(code >> 4) - 1) * k.reach;
+        const int ry = ((int)((code >> 2) & 3u) - 1) * k.reach;
+        const int rx = ((int)(code & 3u) - 1) * k.reach;
+        dx = __fmaf_rn(-(float)rx, k.cell, __fsub_rn(pi.x, pj.x));
+        dy = __fmaf_rn(-(float)ry, k.cell, __fsub_rn(pi.y, pj.y));
+        dz = __fmaf_rn(-(float)rz, k.cell, __fsub_rn(pi.z, pj.z));
     } else {
         (void)k;
         (void)code;

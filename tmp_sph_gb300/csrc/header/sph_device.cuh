@@ -41,18 +41,20 @@ struct KParamsT {
     int n;
     int gx, gy, gz;      // grid dimensions
     int num_cells;
-    // Batched instances are stacked along z, each gz_local cells high plus `reach` empty
-    // layers, so the resident key of a particle of instance b is b * inst_cells + its cell in
-    // its own grid.  A single simulation has gz_local = gz and inst_cells = 0.
+    // Batched instances are stacked along z every gz_stride cell layers: each gz_local cells
+    // high, then at least `reach` empty layers (gz_stride is a multiple of reach, so the
+    // anchor cells of mixed precision fall alike in every instance); the resident key of a
+    // particle of instance b is b * inst_cells + its cell in its own grid.  A single simulation
+    // has gz_local = gz and inst_cells = 0.
     int gz_local;
+    int gz_stride;
     int inst_cells;
     // Cells walked on each side of a particle's cell: 1 (27 cells of at least the list cutoff),
     // 2 or 3 (cells of a half or a third of it: 125 or 343 cells, fewer candidates in all).
-    // Mixed-precision list slots keep a neighbour's cell relative to i's in code_bits bits per
-    // axis (2 for reach 1, else 3) above bit code_shift = 32 - 3 code_bits.
+    // Mixed precision anchors a particle's offsets at the cell whose coordinates are its own
+    // rounded down to multiples of `reach` (anchor_of), so two particles within the walk have
+    // anchors at most one anchor step apart on each axis.
     int reach;
-    int code_bits;
-    int code_shift;
     // Launch shape of the neighbour kernels (host side): threads per block (multiple of 32, at
     // most 256) and particles per thread.
     int threads;
@@ -128,17 +130,22 @@ __device__ __forceinline__ void cell_of_key(int gx, int gy, unsigned key, int& c
     cy = (int)(t - (unsigned)cz * (unsigned)gy);
 }
 
-// Origin of a cell of the (float) grid, in double: the frame of the mixed-precision offsets.
-// `key` is a resident key; the origin is in the coordinates of the particle's own instance.
+// Anchor of a cell coordinate: rounded down to a multiple of the walk reach (the coordinate
+// itself with reach 1).
+__device__ __forceinline__ int anchor_of(int c, int reach) { return reach > 1 ? c - c % reach : c; }
+
+// Origin of the anchor cell of a cell of the (float) grid, in double: the frame of the
+// mixed-precision offsets.  `key` is a resident key; the origin is in the coordinates of the
+// particle's own instance.
 template <class KT>
 __device__ __forceinline__ void cell_origin(const KParamsT<KT>& k, unsigned key, double& ox,
                                             double& oy, double& oz) {
     int cx, cy, cz;
     cell_of_key(k.gx, k.gy, key, cx, cy, cz);
-    if (k.inst_cells) cz %= k.gz_local + k.reach;
-    ox = (double)k.gmin_x + (double)cx * (double)k.cell;
-    oy = (double)k.gmin_y + (double)cy * (double)k.cell;
-    oz = (double)k.gmin_z + (double)cz * (double)k.cell;
+    if (k.inst_cells) cz %= k.gz_stride;
+    ox = (double)k.gmin_x + (double)anchor_of(cx, k.reach) * (double)k.cell;
+    oy = (double)k.gmin_y + (double)anchor_of(cy, k.reach) * (double)k.cell;
+    oz = (double)k.gmin_z + (double)anchor_of(cz, k.reach) * (double)k.cell;
 }
 
 // Position along one axis in units of the cell edge, measured from the grid origin: the

@@ -304,6 +304,7 @@ struct sph_ctx {
     int opt_lanes = 0;       // list pass 1: lanes per particle (0: the precision's default)
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
     int opt_reach = 1;       // cells per list cutoff (SPH_OPT_CELL_DIVISIONS): walk reach
+    bool opt_reach_set = false;  // set by the caller (else the precision's default)
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

@@ -33,10 +33,9 @@ KParams make_kparams(const sph_params& p, int n) {
     k.gz = p.grid_dim[2];
     k.num_cells = p.num_cells;
     k.gz_local = p.grid_dim[2];
+    k.gz_stride = p.grid_dim[2];
     k.inst_cells = 0;
     k.reach = 1;
-    k.code_bits = 2;
-    k.code_shift = 26;
     k.threads = 128;
     k.ppt = 1;
     k.lanes = 1;
@@ -99,10 +98,9 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.gz = p.grid_dim[2];
     k.num_cells = p.num_cells;
     k.gz_local = p.grid_dim[2];
+    k.gz_stride = p.grid_dim[2];
     k.inst_cells = 0;
     k.reach = 1;
-    k.code_bits = 2;
-    k.code_shift = 26;
     k.threads = 128;
     k.ppt = 1;
     k.lanes = 1;

@@ -203,9 +203,6 @@ bool params_ok(const sph_params* p) {
 
 constexpr int EV_PER_HALF = PH_COUNT + 1;
 
-// Bits of a mixed-precision list slot that hold the neighbour's index (the rest hold its cell
-// relative to the particle's: 2 bits per axis with one cell walked on each side, 3 with more).
-int mixed_index_bits(const sph_ctx* c) { return c->opt_reach > 1 ? 23 : 26; }
 
 // The neighbour list to use this half step, or NULL to walk the cells in every pass.
 const NbrList* list_for(sph_ctx* c) {
@@ -236,12 +233,19 @@ sph_params internal_params(const sph_params& P, double skin, int reach) {
 // empty cell layers between consecutive instances, so no cell walk reaches another instance.
 // *gz_local receives the height of one instance's grid.  Returns false when the stacked grid
 // does not fit the key range.
+// Height of one instance in the stacked grid: its own layers and at least `reach` empty ones,
+// rounded up to a multiple of reach.
+int instance_stride(int gz_local, int reach) {
+    const int r = reach > 1 ? reach : 1;
+    return (gz_local + r + r - 1) / r * r;
+}
+
 bool stacked_params(const sph_params& P, double skin, int reach, int n_inst, sph_params* out,
                     int* gz_local) {
     sph_params Q = internal_params(P, skin, reach);
     *gz_local = Q.grid_dim[2];
     if (n_inst > 1) {
-        const long long gz = (long long)n_inst * (Q.grid_dim[2] + reach);
+        const long long gz = (long long)n_inst * instance_stride(Q.grid_dim[2], reach);
         const long long cells = (long long)Q.grid_dim[0] * Q.grid_dim[1] * gz;
         if (cells >= (1LL << 30)) return false;
         Q.grid_dim[2] = (int)gz;
@@ -270,6 +274,13 @@ static int block_threads(const sph_ctx* c) {
     return c->prec == SPH_PREC_FP32 ? 256 : 128;
 }
 
+// Cells per list cutoff by default: 3 in FP32 (cells of about dx at h = 1.3 dx: the
+// cell-sorted state is ordered along rows of single particles, so the lanes of a warp hold
+// neighbours whose lists are shifted copies of each other and gather common lines; 4.96M dam
+// break 2.85 against 3.28 ms per step), 1 in the other precisions (mixed precision's passes
+// gain less and its list build walks the finer cells in more runs).
+static int default_reach(int prec) { return prec == SPH_PREC_FP32 ? 3 : 1; }
+
 // Lane groups read interleaved list windows, one lane per particle plain ones.
 static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1; }
 
@@ -284,10 +295,8 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.lanes = groups ? pass1_lanes(c) : 1;
     k.list_win = k.lanes > 1;
     k.reach = c->opt_reach;
-    k.code_bits = c->opt_reach > 1 ? 3 : 2;
-    k.code_shift = 32 - 3 * k.code_bits;
-    k.inst_cells =
-        c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * (c->gz_inst + c->opt_reach) : 0;
+    k.gz_stride = c->n_inst > 1 ? instance_stride(c->gz_inst, c->opt_reach) : c->gz_inst;
+    k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * k.gz_stride : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
     if (k.kh2_list < k.kh2) k.kh2_list = k.kh2;
@@ -567,6 +576,7 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     sph_ctx* c = new (std::nothrow) sph_ctx();
     if (!c) return SPH_ERR_NOMEM;
     c->P = *p;
+    c->opt_reach = default_reach(c->prec);
     stacked_params(*p, c->skin, c->opt_reach, 1, &c->Pi, &c->gz_inst);
     c->capacity = capacity;
     cudaGetDevice(&c->device);
@@ -667,6 +677,22 @@ extern "C" int sph_get_params(const sph_ctx* c, sph_params* out) {
     return SPH_OK;
 }
 
+// A new cell size: the solver's grid and the cell arrays for it, the keys recomputed and the
+// lists rebuilt at the next half step.
+static int set_reach(sph_ctx* c, int reach) {
+    sph_params pi;
+    int gz_local;
+    if (!stacked_params(c->P, c->skin, reach, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
+    if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
+    c->opt_reach = reach;
+    c->Pi = pi;
+    c->gz_inst = gz_local;
+    c->rehash = c->loaded;  // the keys pass 2 wrote index the old grid
+    c->sorted = false;
+    drop_graph(c);
+    return cudaMemset(c->rb + 2, 1, sizeof(unsigned)) == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+}
+
 extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
     if (!c) return SPH_ERR_ARG;
     switch (option) {
@@ -703,18 +729,13 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
         }
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
         case SPH_OPT_CELL_DIVISIONS: {
-            if (value < 1 || value > 3) return SPH_ERR_ARG;
-            if (value == c->opt_reach) return SPH_OK;
-            if (prec_is_mixed(c->prec) && c->n >= (1 << (value > 1 ? 23 : 26))) return SPH_ERR_ARG;
-            sph_params pi;
-            int gz_local;
-            if (!stacked_params(c->P, c->skin, value, c->n_inst, &pi, &gz_local)) return SPH_ERR_ARG;
-            if (ensure_cells(c, pi.num_cells) != cudaSuccess) return SPH_ERR_NOMEM;
-            c->opt_reach = value;
-            c->Pi = pi;
-            c->gz_inst = gz_local;
-            c->rehash = c->loaded;  // the keys pass 2 wrote index the old grid
-            drop_graph(c);
+            // 0: the precision's default
+            if (value < 0 || value > 3) return SPH_ERR_ARG;
+            const int reach = value > 0 ? value : default_reach(c->prec);
+            c->opt_reach_set = value > 0;
+            if (reach == c->opt_reach) return SPH_OK;
+            const int st = set_reach(c, reach);
+            if (st != SPH_OK) return st;
             break;
         }
         case SPH_OPT_PRECISION: {
@@ -734,6 +755,11 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
                 alloc_state(c);
                 cudaGetLastError();
                 return SPH_ERR_NOMEM;
+            }
+            // the cell size follows the precision unless it was set
+            if (!c->opt_reach_set && default_reach(c->prec) != c->opt_reach) {
+                const int st = set_reach(c, default_reach(c->prec));
+                if (st != SPH_OK) return st;
             }
             return SPH_OK;
         }
@@ -801,9 +827,8 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
                        int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
-    // mixed-precision list slots keep the neighbour index in 26 bits (23 with cells smaller
-    // than the cutoff)
-    if (prec_is_mixed(c->prec) && n >= (1 << mixed_index_bits(c))) return SPH_ERR_ARG;
+    // mixed-precision list slots keep the neighbour index in 26 bits
+    if (prec_is_mixed(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
     if (n_inst < 1 || n_inst > SPH_MAX_INSTANCES) return SPH_ERR_ARG;
     if (n_inst > 1) {
         if (!offsets || offsets[0] != 0 || offsets[n_inst] != n) return SPH_ERR_ARG;

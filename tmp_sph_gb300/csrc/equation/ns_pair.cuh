@@ -122,13 +122,11 @@ __device__ __forceinline__ float pair_rcp(float x) {
 __device__ __forceinline__ double pair_rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ float dabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }
-__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
-[[maybe_unused]] __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
-[[maybe_unused]] __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 
-// A neighbour sum: plain, or compensated (Neumaier) when COMP.  The compensated form uses
-// explicitly rounded adds so no contraction folds the error terms away.
+// A neighbour sum: plain, or compensated (Neumaier) when COMP, with explicitly rounded
+// arithmetic (no contraction folds the error terms away, and every kernel sums alike).
+// add_prod(a, b) adds a b: one fused multiply-add into a plain sum, the rounded product into
+// a compensated one.
 template <class T, bool COMP>
 struct Sum {
     T s = T(0), c = T(0);
@@ -138,7 +136,14 @@ struct Sum {
             c = add_rn(c, dabs(s) >= dabs(v) ? add_rn(sub_rn(s, t), v) : add_rn(sub_rn(v, t), s));
             s = t;
         } else {
-            s += v;
+            s = add_rn(s, v);
+        }
+    }
+    __device__ __forceinline__ void add_prod(T a, T b) {
+        if constexpr (COMP) {
+            add(mul_rn(a, b));
+        } else {
+            s = fma_rn(a, b, s);
         }
     }
     __device__ __forceinline__ T get() const {
@@ -231,15 +236,15 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
         const int rz = ((int)(code >> 4) - 1) * k.reach;
         const int ry = ((int)((code >> 2) & 3u) - 1) * k.reach;
         const int rx = ((int)(code & 3u) - 1) * k.reach;
-        dx = __fmaf_rn(-(float)rx, k.cell, __fsub_rn(pi.x, pj.x));
-        dy = __fmaf_rn(-(float)ry, k.cell, __fsub_rn(pi.y, pj.y));
-        dz = __fmaf_rn(-(float)rz, k.cell, __fsub_rn(pi.z, pj.z));
+        dx = fma_rn(-(float)rx, k.cell, sub_rn(pi.x, pj.x));
+        dy = fma_rn(-(float)ry, k.cell, sub_rn(pi.y, pj.y));
+        dz = fma_rn(-(float)rz, k.cell, sub_rn(pi.z, pj.z));
     } else {
         (void)k;
         (void)code;
-        dx = pi.x - pj.x;
-        dy = pi.y - pj.y;
-        dz = pi.z - pj.z;
+        dx = sub_rn(pi.x, pj.x);
+        dy = sub_rn(pi.y, pj.y);
+        dz = sub_rn(pi.z, pj.z);
     }
 }
 
@@ -280,6 +285,13 @@ __device__ __forceinline__ float4 as_float4(const dvec4& v) {
 // Pass 1: boundary pressure extrapolation (Adami-style, over fluid neighbours) for boundary
 // particles; velocity divergence over fluid neighbours for fluid particles.  Writes the pass-2
 // neighbour record and the particle's own (p', rho', dofv).
+// (v_i - v_j) . r with explicit rounding: x, then y and z fused in.
+template <class V, class T>
+__device__ __forceinline__ T dot_rn(const V& vi, const V& vj, T dx, T dy, T dz) {
+    return fma_rn(sub_rn(vi.z, vj.z), dz,
+                  fma_rn(sub_rn(vi.y, vj.y), dy, mul_rn(sub_rn(vi.x, vj.x), dx)));
+}
+
 // Pass-1 state of one particle: its own record and the three neighbour sums.
 template <class P>
 struct Pass1Acc {
@@ -299,17 +311,17 @@ struct Pass1Acc {
                                          T dy, T dz, T r2) {
         if (!fluid_rec(vj.w)) return;
         const T rr = pair_sqrt(r2);
-        const T q = rr * k.inv_h;
-        const T t = T(1) - T(0.5) * q;
-        const T t2 = t * t;
+        const T q = mul_rn(rr, k.inv_h);
+        const T t = fma_rn(T(-0.5), q, T(1));
+        const T t2 = mul_rn(t, t);
         if (!fi) {
-            const T w = k.adh * t2 * t2 * (T(2) * q + T(1));
-            rs.add((aj.w + vj.w * k.g * dz) * w);
+            const T w = mul_rn(mul_rn(mul_rn(k.adh, t2), t2), fma_rn(T(2), q, T(1)));
+            rs.add_prod(fma_rn(mul_rn(vj.w, k.g), dz, aj.w), w);
             ws.add(w);
         } else {
-            const T fr = k.c_fr * t2 * t;
-            const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            dofv.add(-(fr * vdotr * (k.mass * pair_rcp(vj.w))));
+            const T fr = mul_rn(mul_rn(k.c_fr, t2), t);
+            const T vdotr = dot_rn(vi, vj, dx, dy, dz);
+            dofv.add_prod(-mul_rn(fr, vdotr), mul_rn(k.mass, pair_rcp(vj.w)));
         }
     }
     template <bool WRITE_SUMS>
@@ -326,7 +338,7 @@ struct Pass1Acc {
             if (p < T(0)) p = T(0);
             rho = eos_density(k, p);
         }
-        const T qv = fi ? p - k.damper * dv : p;
+        const T qv = fi ? fma_rn(-k.damper, dv, p) : p;
         out.nrec[2 * (size_t)i] = make4<T>(pi.x, pi.y, pi.z, qv);
         out.nrec[2 * (size_t)i + 1] = make4<T>(vi.x, vi.y, vi.z, fi ? rho : -rho);
         out.self[i] = make4<T>(p, rho, dv, T(0));
@@ -378,23 +390,24 @@ struct Pass2Acc {
         const bool fj = fluid_rec(vj.w);
         const T rhoj = dabs(vj.w);
         const T rr = pair_sqrt(r2);
-        const T t = T(1) - T(0.5) * k.inv_h * rr;
+        const T t = fma_rn(mul_rn(T(-0.5), k.inv_h), rr, T(1));
         // m / rho_j grad W / r in one factor: c_fr m t^3 / rho_j
-        const T w = k.c_fr_mass * (t * t) * t * pair_rcp(rhoj);
-        const T vdotr = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-        const T inv_r2e = pair_rcp(r2 + k.eta2);
-        sd.add(w * (rhoi * vdotr + (rhoi - rhoj) * k.delta_h_cs * r2 * inv_r2e));
+        const T w = mul_rn(mul_rn(mul_rn(k.c_fr_mass, mul_rn(t, t)), t), pair_rcp(rhoj));
+        const T vdotr = dot_rn(vi, vj, dx, dy, dz);
+        const T inv_r2e = pair_rcp(add_rn(r2, k.eta2));
+        const T diff = mul_rn(mul_rn(mul_rn(sub_rn(rhoi, rhoj), k.delta_h_cs), r2), inv_r2e);
+        sd.add_prod(w, fma_rn(rhoi, vdotr, diff));
         T S;
         if (MODE != MODE_RATES || fi) {  // the integrating passes only visit fluid rows
-            S = -presi - aj.w;
-            if (fj) S += damp_i + k.visc * vdotr * inv_r2e;
+            S = sub_rn(-presi, aj.w);
+            if (fj) S = add_rn(S, fma_rn(mul_rn(k.visc, vdotr), inv_r2e, damp_i));
         } else {
-            S = -(presi + __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
+            S = -add_rn(presi, __ldg(&p1.self[j].x));  // boundary rows (wall_rates): plain pressures
         }
-        const T c = w * S;
-        sx.add(c * dx);
-        sy.add(c * dy);
-        sz.add(c * dz);
+        const T c = mul_rn(w, S);
+        sx.add_prod(c, dx);
+        sy.add_prod(c, dy);
+        sz.add_prod(c, dz);
     }
 };
 
@@ -422,11 +435,11 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
     if (acc.active) {
         drho = acc.sd.get();
         const T inv_rhoi = T(1) / rhoi;
-        ax = acc.sx.get() * inv_rhoi;
-        ay = acc.sy.get() * inv_rhoi;
-        az = acc.sz.get() * inv_rhoi;
+        ax = mul_rn(acc.sx.get(), inv_rhoi);
+        ay = mul_rn(acc.sy.get(), inv_rhoi);
+        az = mul_rn(acc.sz.get(), inv_rhoi);
     }
-    az += k.g;
+    az = add_rn(az, k.g);
 
     if constexpr (MODE == MODE_RATES) {
         const bool have = fi || wall_rates;
@@ -450,31 +463,32 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
                 tv = nv;
             } else if (MODE == MODE_PRED) {
                 tv = make_float4(vi.x, vi.y, vi.z, 0.f);
-                double d = xm.w + (double)drho * hdt;
+                double d = fma_rn((double)drho, hdt, xm.w);
                 if (k.clamp_density && d < 0.0) d = 0.0;
-                nxm.x = xm.x + (double)vi.x * hdt;
-                nxm.y = xm.y + (double)vi.y * hdt;
-                nxm.z = xm.z + (double)vi.z * hdt;
+                nxm.x = fma_rn((double)vi.x, hdt, xm.x);
+                nxm.y = fma_rn((double)vi.y, hdt, xm.y);
+                nxm.z = fma_rn((double)vi.z, hdt, xm.z);
                 nxm.w = d;
-                nv = make_float4(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
-                                 0.f);
+                nv = make_float4(fma_rn(ax, k.half_dt, vi.x), fma_rn(ay, k.half_dt, vi.y),
+                                 fma_rn(az, k.half_dt, vi.z), 0.f);
             } else {
                 txm = in.txm[i];
                 tv = in.tvel[i];
-                double ds = txm.w + (double)drho * hdt;
+                double ds = fma_rn((double)drho, hdt, txm.w);
                 if (k.clamp_density && ds < 0.0) ds = 0.0;
-                double d = 2.0 * ds - txm.w;
+                double d = fma_rn(2.0, ds, -txm.w);
                 if (k.clamp_density && d < 0.0) d = 0.0;
-                nxm.x = 2.0 * (txm.x + (double)vi.x * hdt) - txm.x;
-                nxm.y = 2.0 * (txm.y + (double)vi.y * hdt) - txm.y;
-                nxm.z = 2.0 * (txm.z + (double)vi.z * hdt) - txm.z;
+                nxm.x = fma_rn(2.0, fma_rn((double)vi.x, hdt, txm.x), -txm.x);
+                nxm.y = fma_rn(2.0, fma_rn((double)vi.y, hdt, txm.y), -txm.y);
+                nxm.z = fma_rn(2.0, fma_rn((double)vi.z, hdt, txm.z), -txm.z);
                 nxm.w = d;
-                const float uxs = tv.x + ax * k.half_dt;
-                const float uys = tv.y + ay * k.half_dt;
-                const float uzs = tv.z + az * k.half_dt;
-                nv = make_float4(2.f * uxs - tv.x, 2.f * uys - tv.y, 2.f * uzs - tv.z, 0.f);
+                const float uxs = fma_rn(ax, k.half_dt, tv.x);
+                const float uys = fma_rn(ay, k.half_dt, tv.y);
+                const float uzs = fma_rn(az, k.half_dt, tv.z);
+                nv = make_float4(fma_rn(2.f, uxs, -tv.x), fma_rn(2.f, uys, -tv.y),
+                                 fma_rn(2.f, uzs, -tv.z), 0.f);
             }
-            nrho = k.rho0 + (float)nxm.w;
+            nrho = add_rn(k.rho0, (float)nxm.w);
             npres = eos_pressure_d(k, (float)nxm.w);
         } else {
             // boundary particles do not move; they keep the extrapolated pressure and density
@@ -532,32 +546,33 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
             } else if (MODE == MODE_PRED) {
                 tp = make4<T>(pi.x, pi.y, pi.z, rhoi);
                 tv = make4<T>(vi.x, vi.y, vi.z, T(0));
-                T rho = rhoi + drho * k.half_dt;
+                T rho = fma_rn(drho, k.half_dt, rhoi);
                 if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-                np.x = pi.x + vi.x * k.half_dt;
-                np.y = pi.y + vi.y * k.half_dt;
-                np.z = pi.z + vi.z * k.half_dt;
-                nv = make4<T>(vi.x + ax * k.half_dt, vi.y + ay * k.half_dt, vi.z + az * k.half_dt,
-                              T(0));
+                np.x = fma_rn(vi.x, k.half_dt, pi.x);
+                np.y = fma_rn(vi.y, k.half_dt, pi.y);
+                np.z = fma_rn(vi.z, k.half_dt, pi.z);
+                nv = make4<T>(fma_rn(ax, k.half_dt, vi.x), fma_rn(ay, k.half_dt, vi.y),
+                              fma_rn(az, k.half_dt, vi.z), T(0));
                 nrho = rho;
                 npres = eos_pressure(k, rho);
             } else {
                 tp = in.tpos[i];
                 tv = in.tvel[i];
-                T rho = tp.w + drho * k.half_dt;
+                T rho = fma_rn(drho, k.half_dt, tp.w);
                 if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-                const T xs = tp.x + vi.x * k.half_dt;
-                const T ys = tp.y + vi.y * k.half_dt;
-                const T zs = tp.z + vi.z * k.half_dt;
-                const T uxs = tv.x + ax * k.half_dt;
-                const T uys = tv.y + ay * k.half_dt;
-                const T uzs = tv.z + az * k.half_dt;
-                rho = T(2) * rho - tp.w;
+                const T xs = fma_rn(vi.x, k.half_dt, tp.x);
+                const T ys = fma_rn(vi.y, k.half_dt, tp.y);
+                const T zs = fma_rn(vi.z, k.half_dt, tp.z);
+                const T uxs = fma_rn(ax, k.half_dt, tv.x);
+                const T uys = fma_rn(ay, k.half_dt, tv.y);
+                const T uzs = fma_rn(az, k.half_dt, tv.z);
+                rho = fma_rn(T(2), rho, -tp.w);
                 if (k.clamp_density && rho < k.rho0) rho = k.rho0;
-                np.x = T(2) * xs - tp.x;
-                np.y = T(2) * ys - tp.y;
-                np.z = T(2) * zs - tp.z;
-                nv = make4<T>(T(2) * uxs - tv.x, T(2) * uys - tv.y, T(2) * uzs - tv.z, T(0));
+                np.x = fma_rn(T(2), xs, -tp.x);
+                np.y = fma_rn(T(2), ys, -tp.y);
+                np.z = fma_rn(T(2), zs, -tp.z);
+                nv = make4<T>(fma_rn(T(2), uxs, -tv.x), fma_rn(T(2), uys, -tv.y),
+                              fma_rn(T(2), uzs, -tv.z), T(0));
                 nrho = rho;
                 npres = eos_pressure(k, rho);
             }

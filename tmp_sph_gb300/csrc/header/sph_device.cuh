@@ -199,6 +199,21 @@ __device__ __forceinline__ unsigned resident_key(const KParamsT<KT>& k, int inst
     return (unsigned)cell_hash_clamped(k, x, y, z, flag) + (unsigned)inst * (unsigned)k.inst_cells;
 }
 
+// ---------------------------------------------------------------- explicit rounding
+// Arithmetic with its rounding spelled out.  The compiler fuses a product into a following add
+// (fma contraction) where it sees fit, and an inlined expression can be fused one way in one
+// kernel and another way in the next; the neighbour passes are written with these wherever a
+// product meets a sum, so the list passes, the cell-walking passes and the batched runs get the
+// same bits from the same pairs.
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
 // ---------------------------------------------------------------- equation of state
 __device__ __forceinline__ float dexpm1(float x) { return expm1f(x); }
 __device__ __forceinline__ double dexpm1(double x) { return expm1(x); }
@@ -224,7 +239,7 @@ __device__ __forceinline__ T eos_pressure(const KParamsT<T>& k, T rho) {
 template <class T>
 __device__ __forceinline__ T eos_density(const KParamsT<T>& k, T p) {
     if (k.eos == SPH_EOS_TAIT)
-        return k.rho0 + k.rho0 * dexpm1(k.inv_gamma * dlog1p(p * k.inv_tait_b));
+        return fma_rn(k.rho0, dexpm1(k.inv_gamma * dlog1p(p * k.inv_tait_b)), k.rho0);
     return p / k.cs / k.cs + k.rho0;
 }
 

@@ -175,8 +175,10 @@ def build_case(name: str):
     return cases.build(name, physics="config")
 
 
-def count_launches(num_cells: int, half_steps: int, rebuilds: int, mode: str) -> int:
-    """Kernels launched over `half_steps` half steps with `rebuilds` list rebuilds."""
+def count_launches(num_cells: int, half_steps: int, rebuilds: int, mode: str,
+                   keep_keys: bool = False) -> int:
+    """Kernels launched over `half_steps` half steps with `rebuilds` list rebuilds
+    (keep_keys: a batch with per-instance decisions, one more kernel per rebuild)."""
     bits = 1
     while bits < 31 and (1 << bits) < num_cells:
         bits += 1
@@ -185,7 +187,7 @@ def count_launches(num_cells: int, half_steps: int, rebuilds: int, mode: str) ->
     # clear, 3 kernels per radix pass, gather + copy back, cell-start clear, mark and fill,
     # and the neighbour-list build.  In gated mode the rebuild kernels are launched every
     # half step (and return at once when the lists are kept).
-    rebuild_kernels = 3 * passes + 7
+    rebuild_kernels = 3 * passes + 7 + (1 if keep_keys else 0)
     if mode == "gated":
         return half_steps * (3 + rebuild_kernels)
     return 3 * half_steps + rebuilds * rebuild_kernels
@@ -469,10 +471,15 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
         v.set_option(api.SPH_OPT_CONDITIONAL_GRAPH, int(args.graph_mode == "conditional"))
         set_lanes(v, args)
         v.set_option(api.SPH_OPT_ADAPTIVE_SKIN, args.adaptive_skin)
+        v.set_option(api.SPH_OPT_INSTANCE_DECISIONS, args.instance_decisions)
         if tuned:
             from tmp_sph_gb300 import autotune
             autotune.apply(v, tuned)
         return v
+
+    def instance_rebuilds(v) -> dict:
+        c = v.instance_rebuild_counts(hi - lo, stream=stream)
+        return {"min": int(c.min()), "mean": float(c.mean()), "max": int(c.max())}
 
     sol = make_solver()
     lanes = lanes_in_effect(sol)
@@ -492,6 +499,7 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
         replicas.barrier()
     ms = replicas.reduce_max(ev0.elapsed_time(ev1))
     rebuilds = sol.rebuild_count(stream=stream) - r0
+    own = bool(sol.get_option(api.SPH_OPT_INSTANCE_DECISIONS)) and hi - lo > 1
     out = {"value": n_all * steps / (ms / 1e3), "unit": UNIT,
            "fluid_value": n_fluid_all * steps / (ms / 1e3), "ms_per_step": ms / steps,
            "steps": steps, "warmup": warmup,
@@ -505,11 +513,11 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
                                       if ws > 1 else "one batched solver"),
                       "dx_m": p.dx, "dt_s": p.dt, "cs": p.cs,
                       "neighbour_list_skin_over_kh": skin / 1000.0,
-                      "graph_mode": args.graph_mode, **lanes},
+                      "graph_mode": args.graph_mode, "instance_decisions": int(own), **lanes},
            "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * steps},
            "gpu_launches": count_launches(
-               sol_cells_batch(p, n_inst, skin, tuned["divisions"] if tuned else 1), 2 * steps,
-               rebuilds, args.graph_mode),
+               sol_cells_batch(p, n_inst, skin, lanes["cell_divisions"]), 2 * steps,
+               rebuilds, args.graph_mode, own),
            "autotune": None}
     if tuned:
         from tmp_sph_gb300 import autotune
@@ -533,11 +541,13 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
         sol.upload_instances(mine, stream=stream)
         ms_run, rb_run = time_run(sol, stream, run_steps)
         ms_run = replicas.reduce_max(ms_run)
+        inst_rb = instance_rebuilds(sol)
         ms_dev, rb_dev = time_run(sol, stream, steps)
         ms_dev = replicas.reduce_max(ms_dev)
         out["configured_run"] = {"steps": run_steps, "ms_per_step": ms_run / run_steps,
                                  "value": n_all * run_steps / (ms_run / 1e3),
-                                 "list_rebuilds": rb_run, "half_steps": 2 * run_steps}
+                                 "list_rebuilds": rb_run, "half_steps": 2 * run_steps,
+                                 "instance_rebuilds": inst_rb}
         out["developed_flow"] = {"after_steps": run_steps, "steps": steps,
                                  "ms_per_step": ms_dev / steps,
                                  "value": n_all * steps / (ms_dev / 1e3),
@@ -771,6 +781,9 @@ def main():
     ap.add_argument("--divisions", type=int, default=0, choices=[0, 1, 2, 3],
                     help="cells per list cutoff (SPH_OPT_CELL_DIVISIONS; 0: the library's "
                          "default)")
+    ap.add_argument("--instance-decisions", type=int, default=1, choices=[0, 1],
+                    help="batches: each instance rebuilds its lists on its own displacement "
+                         "box and skin (SPH_OPT_INSTANCE_DECISIONS; 0: one decision for all)")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
     ap.add_argument("--skin", type=int, default=100,

@@ -289,6 +289,16 @@ typedef struct sph_ctx sph_ctx;
                              other precisions.  Smaller cells give the list build
                              fewer candidates for more cell lookups, and order the particles of
                              the cell-sorted state along finer x rows */
+#define SPH_OPT_INSTANCE_DECISIONS 17  /* batched instances (sph_upload_instances) with a
+                             neighbour list: 1 (default): each instance keeps its own
+                             displacement box, list skin and rebuild decision, so its lists are
+                             rebuilt in the same half steps, with the same skins, as in a run of
+                             it alone (the slots of the instances that keep their lists stay in
+                             place through the sort, and their lists are not rebuilt); 0: one box
+                             and one decision for the whole batch, so the fastest instance
+                             rebuilds all.  With park_inactive, a particle that leaves or
+                             rejoins the neighbour search moves the slots after it and every
+                             instance rebuilds */
 
 
 /* Precision of the resident solver (SPH_OPT_PRECISION); none has a reference counterpart. */
@@ -380,6 +390,10 @@ int sph_steps_taken(const sph_ctx* ctx, long long* steps);
 int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
 /* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream). */
 int sph_read_rebuild_count(sph_ctx* ctx, unsigned* count, void* stream);
+/* List rebuilds of each of the first n instances of a batch since the upload (host array of n;
+ * synchronises the stream).  Without per-instance decisions every instance reports the count
+ * of sph_read_rebuild_count. */
+int sph_read_instance_rebuild_counts(sph_ctx* ctx, unsigned* counts, int n, void* stream);
 /* Skin of the current neighbour lists as a fraction of kh (synchronises the stream). */
 int sph_read_list_skin(sph_ctx* ctx, float* skin, void* stream);
 

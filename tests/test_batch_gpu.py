@@ -1,10 +1,12 @@
 """GPU tests of batched instances (sph_upload_instances): several independent dam breaks
-advanced by the same launches.  The instances are stacked in one grid with an empty cell layer
+advanced by the same launches.  The instances are stacked in one grid with empty cell layers
 between them, so every instance sees exactly the neighbours, in exactly the order, it would see
-alone when the lists are rebuilt on the same schedule: with the skin off (rebuild every half
-step) each instance of a batched run equals its solo run bit for bit.  With the skin on, the
-batch rebuilds when any instance needs it, so summation orders — not the pairs — can differ
-from a solo run: agreement to FP32 rounding."""
+alone when its lists are rebuilt on the same schedule.  With per-instance decisions (the
+default) each instance keeps its own displacement box and skin and rebuilds exactly when it
+would alone, so each instance of a batched run equals its solo run bit for bit, with the skin
+on or off.  With one decision for the batch (SPH_OPT_INSTANCE_DECISIONS 0) the batch rebuilds
+when any instance needs it, so summation orders — not the pairs — can differ from a solo run:
+agreement to FP32 rounding."""
 from __future__ import annotations
 
 import ctypes
@@ -25,12 +27,14 @@ def solo(st, p, nsteps, precision, skin=100):
         sol.step(nsteps, stream=s)
         out = sol.download(stream=s)
         out["flags"] = sol.error_flags(stream=s)
+        out["rebuilds"] = sol.rebuild_count(stream=s)
         _, out["stats"] = sol.probe(stream=s)
     return out
 
 
-@pytest.mark.parametrize("precision,skin", [("fp32", 0), ("mixed", 0), ("fp32", 100)])
-def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin):
+@pytest.mark.parametrize("precision,skin,own", [("fp32", 0, 1), ("mixed", 0, 1), ("fp32", 100, 1),
+                                                ("mixed", 100, 1), ("fp32", 100, 0)])
+def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin, own):
     import torch
     from tmp_sph_gb300 import api, cases, solver as S
     from gpu_util import perturbed
@@ -42,6 +46,7 @@ def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin
     s = torch.cuda.Stream()
     with S.Solver(p, n, precision=precision) as sol:
         sol.set_option(api.SPH_OPT_SKIN_PERMILLE, skin)
+        sol.set_option(api.SPH_OPT_INSTANCE_DECISIONS, own)
         off = sol.upload_instances(states, stream=s)
         ni = ctypes.c_int(0)
         api.lib().sph_instances(sol.handle, ctypes.byref(ni))
@@ -51,16 +56,19 @@ def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin
         flags = sol.error_flags(stream=s)
         _, stats = sol.probe(stream=s)
         rebuilds = sol.rebuild_count(stream=s)
+        per_inst = sol.instance_rebuild_counts(3, stream=s)
     assert flags == 0
     assert rebuilds >= 2
     report(f"batched {precision} skin {skin} rebuilds", rebuilds)
     fluid = 0
+    solo_rebuilds = []
     for b, st in enumerate(states):
         ref = solo(st, p, steps, precision, skin)
         assert ref["flags"] == 0
+        solo_rebuilds.append(ref["rebuilds"])
         sl = slice(int(off[b]), int(off[b + 1]))
         fl = st["type"] == 1
-        if skin == 0:
+        if skin == 0 or own:
             for k in ("pos", "vel", "rho", "p", "type"):
                 assert np.array_equal(out[k][sl], ref[k]), (b, k)
         else:
@@ -70,6 +78,14 @@ def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin
             assert np.array_equal(out["type"][sl], ref["type"])
         fluid += ref["stats"]["fluid"]
     assert stats["fluid"] == fluid
+    if own:
+        # each instance rebuilt exactly when it did alone; the batch when any did
+        assert per_inst.tolist() == solo_rebuilds
+        assert max(solo_rebuilds) <= rebuilds <= sum(solo_rebuilds)
+        if skin:
+            assert len(set(solo_rebuilds)) > 1, solo_rebuilds  # the instances' schedules differ
+    else:
+        assert per_inst.tolist() == [rebuilds] * 3
 
 
 def test_batched_then_single_upload(sphlib, cuda):

@@ -47,6 +47,7 @@ SPH_OPT_LANES_PER_PARTICLE = 12
 SPH_OPT_PASS1_LANES = 14
 SPH_OPT_ADAPTIVE_SKIN = 13
 SPH_OPT_CELL_DIVISIONS = 16
+SPH_OPT_INSTANCE_DECISIONS = 17
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
               "mixed_comp": SPH_PREC_MIXED_COMP}
@@ -180,6 +181,7 @@ _PROTOS = {
     "sph_step_host": (_I, [_P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "sph_ctx_sorted_view": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I)]),
     "sph_read_rebuild_count": (_I, [_P, C.POINTER(C.c_uint), _P]),
+    "sph_read_instance_rebuild_counts": (_I, [_P, _P, _I, _P]),
     "sph_read_list_skin": (_I, [_P, C.POINTER(C.c_float), _P]),
     "sph_snapshot_begin": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "sph_snapshot_wait": (_I, [_P]),

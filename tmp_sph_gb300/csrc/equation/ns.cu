@@ -183,6 +183,14 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
                                               const int* __restrict__ cs, const NbrList& nl,
                                               int walls_all, unsigned* err, int4* stage, int i) {
     using T = typename P::T;
+    T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
+    if (nl.iw) {
+        // per-instance decisions: the particles of the instances that rebuild, each at its
+        // instance's list cutoff; the others keep their lists
+        const unsigned* w = nl.iw + IW_STRIDE * (__ldg(nl.inst + i) + 1);
+        if (!w[IW_REBUILD]) return;
+        cut2 = (T)__uint_as_float(w[IW_CUT2]);
+    }
     const vec4_t<T> pi = X[i];
     if (nl.xb) nl.xb[i] = as_float4(pi);
     const bool keep_all = fluid_rec(pi.w) || walls_all;
@@ -204,7 +212,6 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
         }
     }
     SlotWriter<WIN> w(nl.idx + nbr_col(nl, i), nl.cap, stage);
-    const T cut2 = nl.cut2 ? (T)__ldg(nl.cut2) : k.kh2_list;
     walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
                      [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
         if (keep_all || fluid_rec(pj.w))
@@ -273,7 +280,7 @@ __device__ __forceinline__ void pass2_one(const KParamsT<typename P::T>& k, int 
                                           float* __restrict__ rho_dt, float* __restrict__ vel_dt,
                                           int wall_rates, const ParticleSetT<typename P::T>& out,
                                           unsigned* __restrict__ out_hash, unsigned* err,
-                                          DispBox& box) {
+                                          DispBox& box, unsigned* disp) {
     using T = typename P::T;
     using V = vec4_t<T>;
     Pass2Acc<P, MODE> acc;
@@ -284,7 +291,7 @@ __device__ __forceinline__ void pass2_one(const KParamsT<typename P::T>& k, int 
             acc.pair(k, p1, j, aj, vj, dx, dy, dz, r2);
         });
     pass2_finish<P, MODE>(k, i, acc, in, keys, nl, rho_dt, vel_dt, wall_rates, out, out_hash,
-                          err, box);
+                          err, box, disp);
 }
 
 
@@ -300,15 +307,16 @@ k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
             pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                     out_hash, err, box);
+                                     out_hash, err, box, disp);
     } else if (i0 < k.n) {
         pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                 out_hash, err, box);
+                                 out_hash, err, box, disp);
     }
     if (MODE == MODE_RATES || disp == nullptr) return;
     // the block's displacement box; blockDim is a multiple of 32, every thread gets here
     __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
-    reduce_disp_box(box, disp, s_box);
+    __shared__ int s_inst[NS_MAX_THREADS / 32];
+    reduce_disp(k, box, disp, s_box, s_inst);
 }
 
 // The same kernel held to CAP registers (one particle per thread): the FP32 step kernel fits
@@ -326,15 +334,16 @@ k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     if constexpr (GS) {
         for (int i = i0; i < k.n; i += gridDim.x * blockDim.x)
             pass2_one<P, MODE, LIST>(k, i, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                     out_hash, err, box);
+                                     out_hash, err, box, disp);
     } else if (i0 < k.n) {
         pass2_one<P, MODE, LIST>(k, i0, in, keys, cs, nl, p1, rho_dt, vel_dt, wall_rates, out,
-                                 out_hash, err, box);
+                                 out_hash, err, box, disp);
     }
     if (MODE == MODE_RATES || disp == nullptr) return;
     // the block's displacement box; blockDim is a multiple of 32, every thread gets here
     __shared__ unsigned s_box[6 * (NS_MAX_THREADS / 32)];
-    reduce_disp_box(box, disp, s_box);
+    __shared__ int s_inst[NS_MAX_THREADS / 32];
+    reduce_disp(k, box, disp, s_box, s_inst);
 }
 
 // Launch shape of a neighbour kernel: KParams::threads per block, KParams::ppt particles per

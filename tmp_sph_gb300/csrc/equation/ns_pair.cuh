@@ -424,9 +424,11 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
                                               float* __restrict__ vel_dt, int wall_rates,
                                               const ParticleSetT<typename P::T>& out,
                                               unsigned* __restrict__ out_hash, unsigned* err,
-                                              DispBox& box) {
+                                              DispBox& box, unsigned* disp) {
     using T = typename P::T;
     using V = vec4_t<T>;
+    // per-instance boxes: disp holds the instance words
+    unsigned* const iw = k.inst_boxes ? disp : nullptr;
     const V& pi = acc.pi;
     const V& vi = acc.vi;
     const bool fi = acc.fi;
@@ -522,15 +524,17 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
             // outside it is in no list, so its moves do not count
             const bool now = inactive_key(k, nk);
             if (now != inactive_key(k, keys[i])) {
-                box.add(3.0e38f, 3.0e38f, 3.0e38f);
-                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+                // every slot after it moves: with per-instance boxes all instances rebuild
+                if (iw) atomicOr(iw + IW_ALL, 1u);
+                box.add_at(iw, inst, 3.0e38f, 3.0e38f, 3.0e38f);
+                box.add_at(iw, inst, -3.0e38f, -3.0e38f, -3.0e38f);
                 return;
             }
             if (now) return;
         }
         if (!nl.xb) return;
         const float4 xb = nl.xb[i];
-        box.add(px - xb.x, py - xb.y, pz - xb.z);
+        box.add_at(iw, inst, px - xb.x, py - xb.y, pz - xb.z);
     } else {
         V np = pi, nv;
         T npres, nrho;
@@ -605,15 +609,18 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
             // outside it is in no list, so its moves do not count
             const bool now = inactive_key(k, nk);
             if (now != inactive_key(k, keys[i])) {
-                box.add(3.0e38f, 3.0e38f, 3.0e38f);
-                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+                // every slot after it moves: with per-instance boxes all instances rebuild
+                if (iw) atomicOr(iw + IW_ALL, 1u);
+                box.add_at(iw, inst, 3.0e38f, 3.0e38f, 3.0e38f);
+                box.add_at(iw, inst, -3.0e38f, -3.0e38f, -3.0e38f);
                 return;
             }
             if (now) return;
         }
         if (!nl.xb) return;
         const float4 xb = nl.xb[i];
-        box.add((float)(np.x - (T)xb.x), (float)(np.y - (T)xb.y), (float)(np.z - (T)xb.z));
+        box.add_at(iw, inst, (float)(np.x - (T)xb.x), (float)(np.y - (T)xb.y),
+                   (float)(np.z - (T)xb.z));
     }
 }
 

@@ -83,6 +83,9 @@ struct KParamsT {
     // 1: a fluid particle outside the escape box takes key num_cells (sorted after every cell,
     // outside the neighbour search); 0: it is parked and stays in the search (reference)
     int park_inactive;
+    // 1: batched instances keep a displacement box each and rebuild their lists on their own
+    // decisions (IW_* words below); 0: one box and one decision for all particles
+    int inst_boxes;
 };
 using KParams = KParamsT<float>;
 
@@ -304,10 +307,39 @@ __device__ __forceinline__ float ord_value(unsigned key) {
     return __uint_as_float((key & 0x80000000u) ? (key & 0x7fffffffu) : ~key);
 }
 
+// Per-instance rebuild decisions (batched instances, KParams::inst_boxes): every instance keeps
+// its own displacement box, list skin and rebuild decision, in IW_STRIDE words at
+// iw + IW_STRIDE (b + 1) after a header of IW_STRIDE words.  An instance rebuilds when its own
+// box says so, so it rebuilds in the same half steps, with the same skins, as it would alone.
+constexpr int IW_STRIDE = 16;
+constexpr int IW_ALL = 0;      // header: every instance rebuilds at the next decision
+constexpr int IW_REBUILD = 0;  // the instance's lists are rebuilt in this half step
+constexpr int IW_SKIN = 1;     // skin of its lists (float bits)
+constexpr int IW_CUT2 = 2;     // squared list cutoff (float bits)
+constexpr int IW_THR = 3;      // rebuild threshold on its box (float bits)
+constexpr int IW_HS = 4;       // half steps since its last build
+constexpr int IW_COUNT = 5;    // its rebuilds since the upload
+constexpr int IW_HD2 = 6;      // squared half-diagonal of its last box (float bits)
+constexpr int IW_BOX = 8;      // lo x, y, z, hi x, y, z
+__device__ __forceinline__ unsigned* inst_words(unsigned* iw, int b) {
+    return iw + IW_STRIDE * (b + 1);
+}
+
+// Lower (c < 3) or raise a corner word of a box to v, with an atomic only when v improves on
+// the value already there.
+__device__ __forceinline__ void fold_corner(unsigned* word, int c, unsigned v) {
+    if (c < 3) {
+        if (v < *(volatile unsigned*)word) atomicMin(word, v);
+    } else {
+        if (v > *(volatile unsigned*)word) atomicMax(word, v);
+    }
+}
+
 // A thread's box of displacements (empty until the first add).
 struct DispBox {
     unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu};
     unsigned hi[3] = {0u, 0u, 0u};
+    int inst = -1;  // instance of the displacements added (per-instance boxes), -1: none yet
     // a displacement that is not a number counts as a huge one (the lists are rebuilt)
     __device__ __forceinline__ void add(float x, float y, float z) {
         const float v[3] = {x == x ? x : 3.0e38f, y == y ? y : 3.0e38f, z == z ? z : 3.0e38f};
@@ -316,6 +348,33 @@ struct DispBox {
             const unsigned kc = ord_key(v[c]);
             lo[c] = min(lo[c], kc);
             hi[c] = max(hi[c], kc);
+        }
+    }
+    // The displacement of a particle of instance b: with per-instance boxes (iw != NULL) a
+    // thread that moves on to another instance (particles per thread > 1) first folds what it
+    // holds into the previous instance's box.
+    __device__ __forceinline__ void add_at(unsigned* iw, int b, float x, float y, float z) {
+        if (iw) {
+            if (inst >= 0 && b != inst) {
+                flush(iw);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    lo[c] = 0xffffffffu;
+                    hi[c] = 0u;
+                }
+            }
+            inst = b;
+        }
+        add(x, y, z);
+    }
+    // This thread's box into its instance's words.
+    __device__ __forceinline__ void flush(unsigned* iw) const {
+        if (inst < 0) return;
+        unsigned* w = inst_words(iw, inst) + IW_BOX;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            fold_corner(w + c, c, lo[c]);
+            fold_corner(w + 3 + c, 3 + c, hi[c]);
         }
     }
 };
@@ -341,13 +400,60 @@ __device__ __forceinline__ void reduce_disp_box(const DispBox& b, unsigned* disp
         unsigned v = s_box[c * warps];
         for (int q = 1; q < warps; q++)
             v = c < 3 ? min(v, s_box[c * warps + q]) : max(v, s_box[c * warps + q]);
-        unsigned* word = disp + c * DISP_STRIDE;
-        if (c < 3) {
-            if (v < *(volatile unsigned*)word) atomicMin(word, v);
-        } else {
-            if (v > *(volatile unsigned*)word) atomicMax(word, v);
+        fold_corner(disp + c * DISP_STRIDE, c, v);
+    }
+}
+
+// The same with a box per instance (iw: the instance words).  The particles of a block are
+// consecutive slots, so they belong to one instance or, next to an instance boundary, to a
+// few: each warp whose lanes hold one instance folds its box with warp reductions, a warp that
+// spans a boundary sends each lane's box on its own, and the first six threads fold the
+// warps' boxes run by run of equal instances.  Every thread of the block must call it;
+// s_box holds 6 * (blockDim / 32) words and s_inst blockDim / 32.
+__device__ __forceinline__ void reduce_disp_box_inst(const DispBox& b, unsigned* iw,
+                                                     unsigned* s_box, int* s_inst) {
+    const int warps = (int)(blockDim.x >> 5), w = (int)(threadIdx.x >> 5);
+    const int lead = __reduce_max_sync(0xffffffffu, b.inst);
+    const bool uniform = __all_sync(0xffffffffu, b.inst < 0 || b.inst == lead);
+    if (!uniform) b.flush(iw);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const unsigned l = __reduce_min_sync(0xffffffffu, uniform ? b.lo[c] : 0xffffffffu);
+        const unsigned h = __reduce_max_sync(0xffffffffu, uniform ? b.hi[c] : 0u);
+        if ((threadIdx.x & 31) == 0) {
+            s_box[c * warps + w] = l;
+            s_box[(3 + c) * warps + w] = h;
         }
     }
+    if ((threadIdx.x & 31) == 0) s_inst[w] = uniform ? lead : -1;
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = (int)threadIdx.x;
+        int cur = -1;
+        unsigned v = 0u;
+        for (int q = 0; q < warps; q++) {
+            const int bq = s_inst[q];
+            if (bq < 0) continue;
+            const unsigned u = s_box[c * warps + q];
+            if (bq != cur) {
+                if (cur >= 0) fold_corner(inst_words(iw, cur) + IW_BOX + c, c, v);
+                cur = bq;
+                v = u;
+            } else {
+                v = c < 3 ? min(v, u) : max(v, u);
+            }
+        }
+        if (cur >= 0) fold_corner(inst_words(iw, cur) + IW_BOX + c, c, v);
+    }
+}
+
+// Fold a block's displacement boxes: into the one box (disp) or, with KParams::inst_boxes,
+// into the boxes of the instances (disp = the instance words).
+template <class KP>
+__device__ __forceinline__ void reduce_disp(const KP& k, const DispBox& b, unsigned* disp,
+                                            unsigned* s_box, int* s_inst) {
+    if (k.inst_boxes) reduce_disp_box_inst(b, disp, s_box, s_inst);
+    else reduce_disp_box(b, disp, s_box);
 }
 
 }  // namespace sph

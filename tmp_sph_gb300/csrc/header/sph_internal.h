@@ -127,6 +127,11 @@ struct NbrList {
     // boundary particle keeps fluid neighbours only, so one with no such cell among its 27
     // has an empty list without walking them.
     const unsigned char* fluid_cells = nullptr;
+    // per-instance decisions (KParams::inst_boxes): the instance words and the instance of
+    // every slot; the build skips the particles of instances that keep their lists.  NULL:
+    // every particle is rebuilt at cut2
+    const unsigned* iw = nullptr;
+    const int* inst = nullptr;
 };
 // List slots per particle: 1.5x the lattice particles within kh (1 + skin), rounded up to 16.
 int nbr_capacity_for(const sph_params& p, double skin = 0.0);
@@ -305,6 +310,10 @@ struct sph_ctx {
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
     int opt_reach = 1;       // cells per list cutoff (SPH_OPT_CELL_DIVISIONS): walk reach
     bool opt_reach_set = false;  // set by the caller (else the precision's default)
+    int opt_inst_decisions = 1;  // batched instances rebuild on their own decisions
+    // per-instance rebuild words (IW_*, sph_device.cuh): a header and IW_STRIDE words for each
+    // of up to SPH_MAX_INSTANCES instances
+    unsigned* iw = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
     int graph_n = -1;

@@ -490,6 +490,7 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
     using T = typename P::T;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     DispBox box;
+    unsigned* const iw = kp.inst_boxes ? disp : nullptr;  // per-instance boxes
     if (k < kp.n) {
         const int r = dst.id[k];
         if ((unsigned)r < (unsigned)kp.n) {
@@ -525,15 +526,16 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
             const bool out_now = inactive_key(kp, nk);
             const bool moved_out = out_now != inactive_key(kp, key);
             if (moved_out) {
-                box.add(3.0e38f, 3.0e38f, 3.0e38f);
-                box.add(-3.0e38f, -3.0e38f, -3.0e38f);
+                if (iw) atomicOr(iw + IW_ALL, 1u);  // later slots move: every instance rebuilds
+                box.add_at(iw, inst, 3.0e38f, 3.0e38f, 3.0e38f);
+                box.add_at(iw, inst, -3.0e38f, -3.0e38f, -3.0e38f);
             }
             dst.rec[2 * (size_t)k] = a;
             dst.xyz[k] = make4<T>(a.x, a.y, a.z, srho > T(0) ? T(1) : T(-1));
             raise_flags(err, f);
             if (xb && !out_now && !moved_out) {
                 const float4 b = xb[k];
-                box.add((float)a.x - b.x, (float)a.y - b.y, (float)a.z - b.z);
+                box.add_at(iw, inst, (float)a.x - b.x, (float)a.y - b.y, (float)a.z - b.z);
             }
         } else {
             atomicOr(force, 1u);  // a consistent permutation never takes this
@@ -541,7 +543,8 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
     }
     // blockDim is 256, every thread gets here
     __shared__ unsigned s_box[6 * 8];
-    reduce_disp_box(box, disp, s_box);
+    __shared__ int s_inst[8];
+    reduce_disp(kp, box, disp, s_box, s_inst);
 }
 
 // Cell keys of a resident set on the current grid (after the grid changed under it).

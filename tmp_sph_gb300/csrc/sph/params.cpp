@@ -79,6 +79,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
     k.park_inactive = p.park_inactive;
+    k.inst_boxes = 0;
     return k;
 }
 
@@ -145,6 +146,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.park_y = p.escape_park[1];
     k.park_z = p.escape_park[2];
     k.park_inactive = p.park_inactive;
+    k.inst_boxes = 0;
     return k;
 }
 

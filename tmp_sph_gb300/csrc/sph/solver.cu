@@ -147,6 +147,8 @@ void release(sph_ctx* c) {
     c->nl = NbrList{};
     cudaFree(c->rb);
     c->rb = nullptr;
+    cudaFree(c->iw);
+    c->iw = nullptr;
     cudaFree(c->probe_acc);
     c->probe_acc = nullptr;
     cudaFree(c->inst_off);
@@ -204,11 +206,24 @@ bool params_ok(const sph_params* p) {
 constexpr int EV_PER_HALF = PH_COUNT + 1;
 
 
+// Batched instances with a neighbour list rebuild on their own decisions (per-instance
+// displacement boxes, skins and rebuild flags in c->iw).
+bool per_instance(const sph_ctx* c) {
+    return c->n_inst > 1 && c->opt_inst_decisions && c->opt_nbr_list && c->nl.idx;
+}
+
 // The neighbour list to use this half step, or NULL to walk the cells in every pass.
 const NbrList* list_for(sph_ctx* c) {
     c->nl.fluid_cells = c->fluid_cells;
+    const bool pi = per_instance(c);
+    c->nl.iw = pi ? c->iw : nullptr;
+    c->nl.inst = pi ? (c->prec == SPH_PREC_FP64 ? c->yd.inst : c->y.inst) : nullptr;
     return (c->opt_nbr_list && c->nl.idx) ? &c->nl : nullptr;
 }
+
+// Where pass 2 and an upload into the cell order put the displacements: the instance words
+// or the one box of the rebuild block.
+unsigned* disp_words(sph_ctx* c) { return per_instance(c) ? c->iw : c->rb + RB_DISP; }
 
 // The resident solver's own grid: the caller's grid box with cells of kh (1 + skin) / reach,
 // so a walk of the reach cells on each side of a particle's cell at the last rebuild still
@@ -296,6 +311,7 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.list_win = k.lanes > 1;
     k.reach = c->opt_reach;
     k.gz_stride = c->n_inst > 1 ? instance_stride(c->gz_inst, c->opt_reach) : c->gz_inst;
+    k.inst_boxes = per_instance(c) ? 1 : 0;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * k.gz_stride : 0;
     const double cut = (double)c->P.kh * (1.0 + (c->skin > 0.0 ? c->skin : 0.0));
     k.kh2_list = (T)(cut * cut);
@@ -317,12 +333,43 @@ struct SkinControl {
     int adapt;
 };
 
-__device__ __forceinline__ void set_skin(unsigned* rb, const SkinControl& sc, float s) {
+// Skin s for the next lists: the words of the list cutoff and of the rebuild threshold, and
+// the half-step count restarted.
+__device__ __forceinline__ void write_skin(unsigned* skin, unsigned* cut2, unsigned* thr,
+                                           unsigned* hs, const SkinControl& sc, float s) {
     const float cut = sc.kh * (1.f + s), half = 0.5f * s * sc.kh;
-    rb[RB_SKIN] = __float_as_uint(s);
-    rb[RB_CUT2] = __float_as_uint(cut * cut);
-    rb[RB_THR] = __float_as_uint(half * half);
-    rb[RB_HS] = 0u;
+    *skin = __float_as_uint(s);
+    *cut2 = __float_as_uint(cut * cut);
+    *thr = __float_as_uint(half * half);
+    *hs = 0u;
+}
+__device__ __forceinline__ void set_skin(unsigned* rb, const SkinControl& sc, float s) {
+    write_skin(rb + RB_SKIN, rb + RB_CUT2, rb + RB_THR, rb + RB_HS, sc, s);
+}
+__device__ __forceinline__ void set_inst_skin(unsigned* w, const SkinControl& sc, float s) {
+    write_skin(w + IW_SKIN, w + IW_CUT2, w + IW_THR, w + IW_HS, sc, s);
+}
+
+// Skin of the lists a rebuild makes after lists of skin s lasted hs half steps (adaptive).
+__device__ __forceinline__ float next_skin(const SkinControl& sc, float s, unsigned hs) {
+    const float want = sqrtf(sc.ratio * s / (float)hs);
+    return fminf(fmaxf(sqrtf(s * want), sc.s_min), sc.s_max);
+}
+
+// Squared half-diagonal of a displacement box (lo x, y, z, hi x, y, z, `stride` words apart),
+// which is emptied for the next half step.
+__device__ __forceinline__ float take_box(unsigned* box, int stride) {
+    float hd2 = 0.f;
+    for (int c = 0; c < 3; c++) {
+        const unsigned lo = box[c * stride], hi = box[(3 + c) * stride];
+        if (lo <= hi) {  // else no particle counted
+            const float r = 0.5f * (ord_value(hi) - ord_value(lo));
+            hd2 = fma_rn(r, r, hd2);
+        }
+        box[c * stride] = 0xffffffffu;
+        box[(3 + c) * stride] = 0u;
+    }
+    return hd2;
 }
 
 // Skin of the first lists after an upload or a change of parameters.
@@ -340,8 +387,12 @@ SkinControl skin_control(const sph_ctx* c) {
     return sc;
 }
 
+__global__ void k_inst_reset(unsigned* iw, int n_inst, SkinControl sc, int skin_too,
+                             int counts_too);
+
 cudaError_t reset_skin(sph_ctx* c, cudaStream_t s) {
     k_skin_init<<<1, 32, 0, s>>>(c->rb, skin_control(c));
+    if (c->n_inst > 1) k_inst_reset<<<1, 256, 0, s>>>(c->iw, c->n_inst, skin_control(c), 1, 0);
     return cudaGetLastError();
 }
 
@@ -363,17 +414,7 @@ cudaError_t reset_skin_sync(sph_ctx* c) {
 // rebuild launches none of them.
 __global__ void k_decide(unsigned* rb, SkinControl sc, int always,
                          cudaGraphConditionalHandle cond, int set_cond) {
-    unsigned* box = rb + RB_DISP;
-    float hd2 = 0.f;
-    for (int c = 0; c < 3; c++) {
-        const unsigned lo = box[c * DISP_STRIDE], hi = box[(3 + c) * DISP_STRIDE];
-        if (lo <= hi) {  // else no particle counted
-            const float r = 0.5f * (ord_value(hi) - ord_value(lo));
-            hd2 += r * r;
-        }
-        box[c * DISP_STRIDE] = 0xffffffffu;
-        box[(3 + c) * DISP_STRIDE] = 0u;
-    }
+    const float hd2 = take_box(rb + RB_DISP, DISP_STRIDE);
     const bool forced = rb[2] != 0u;
     const bool rebuild = always || forced || !(hd2 <= __uint_as_float(rb[RB_THR]));
     const unsigned hs = rb[RB_HS] + 1u;
@@ -381,10 +422,7 @@ __global__ void k_decide(unsigned* rb, SkinControl sc, int always,
     rb[1] = __float_as_uint(hd2);
     if (rebuild) {
         float s = __uint_as_float(rb[RB_SKIN]);
-        if (sc.adapt && !always && !forced && s > 0.f) {
-            const float want = sqrtf(sc.ratio * s / (float)hs);
-            s = fminf(fmaxf(sqrtf(s * want), sc.s_min), sc.s_max);
-        }
+        if (sc.adapt && !always && !forced && s > 0.f) s = next_skin(sc, s, hs);
         set_skin(rb, sc, s);
         rb[2] = 0u;
         rb[3] += 1u;
@@ -392,6 +430,95 @@ __global__ void k_decide(unsigned* rb, SkinControl sc, int always,
         rb[RB_HS] = hs;
     }
     if (set_cond) cudaGraphSetConditional(cond, rebuild ? 1u : 0u);
+}
+
+// The same decision for each instance of a batch on its own box and skin (one block): an
+// instance rebuilds when forced (rb[2], or IW_ALL when a particle left or rejoined the search
+// and the slots after it moved) or when its own box has outgrown its own lists, exactly as
+// k_decide decides for it alone.  rb[0] (the gate of the rebuild kernels, and the condition)
+// is set when any instance rebuilds; rb[1] and RB_SKIN report the largest box and skin, rb[3]
+// counts the half steps that rebuilt any.
+__global__ void k_decide_inst(unsigned* rb, unsigned* iw, int n_inst, SkinControl sc,
+                              cudaGraphConditionalHandle cond, int set_cond) {
+    __shared__ unsigned s_max[2 * 32];
+    const bool forced = rb[2] != 0u || iw[IW_ALL] != 0u;
+    int any = 0;
+    unsigned hd2_max = 0u, skin_max = 0u;  // float bits of non-negative values
+    for (int b = (int)threadIdx.x; b < n_inst; b += (int)blockDim.x) {
+        unsigned* w = inst_words(iw, b);
+        const float hd2 = take_box(w + IW_BOX, 1);
+        const bool rebuild = forced || !(hd2 <= __uint_as_float(w[IW_THR]));
+        const unsigned hs = w[IW_HS] + 1u;
+        w[IW_REBUILD] = rebuild ? 1u : 0u;
+        w[IW_HD2] = __float_as_uint(hd2);
+        if (rebuild) {
+            float s = __uint_as_float(w[IW_SKIN]);
+            if (sc.adapt && !forced && s > 0.f) s = next_skin(sc, s, hs);
+            set_inst_skin(w, sc, s);
+            w[IW_COUNT] += 1u;
+        } else {
+            w[IW_HS] = hs;
+        }
+        any |= rebuild ? 1 : 0;
+        hd2_max = max(hd2_max, hd2 == hd2 ? __float_as_uint(hd2) : 0x7f800000u);
+        skin_max = max(skin_max, w[IW_SKIN]);
+    }
+    any = __syncthreads_or(any);
+    hd2_max = __reduce_max_sync(0xffffffffu, hd2_max);
+    skin_max = __reduce_max_sync(0xffffffffu, skin_max);
+    if ((threadIdx.x & 31) == 0) {
+        s_max[threadIdx.x >> 5] = hd2_max;
+        s_max[32 + (threadIdx.x >> 5)] = skin_max;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+            hd2_max = max(hd2_max, s_max[q]);
+            skin_max = max(skin_max, s_max[32 + q]);
+        }
+        rb[0] = any ? 1u : 0u;
+        rb[1] = hd2_max;
+        rb[RB_SKIN] = skin_max;
+        if (any) {
+            rb[2] = 0u;
+            iw[IW_ALL] = 0u;
+            rb[3] += 1u;
+        }
+        if (set_cond) cudaGraphSetConditional(cond, any ? 1u : 0u);
+    }
+}
+
+// Per-instance words of the n_inst instances: the first skin and the half-step counts
+// (skin_too), empty boxes, and with counts_too no rebuild pending or counted.
+__global__ void k_inst_reset(unsigned* iw, int n_inst, SkinControl sc, int skin_too,
+                             int counts_too) {
+    for (int b = (int)threadIdx.x; b < n_inst; b += (int)blockDim.x) {
+        unsigned* w = inst_words(iw, b);
+        if (skin_too) set_inst_skin(w, sc, sc.adapt ? sc.s_min : sc.s_max);
+        for (int c = 0; c < 3; c++) {
+            w[IW_BOX + c] = 0xffffffffu;
+            w[IW_BOX + 3 + c] = 0u;
+        }
+        if (counts_too) {
+            w[IW_REBUILD] = 0u;
+            w[IW_COUNT] = 0u;
+            w[IW_HD2] = 0u;
+        }
+    }
+    if (threadIdx.x == 0 && counts_too) iw[IW_ALL] = 0u;
+}
+
+// Per-instance rebuilds: the slots of the instances that keep their lists are sorted on the
+// keys they were sorted on last time.  Those keys are in order and each instance's keys lie in
+// its own key range, so the stable sort leaves these slots where they are, and their lists,
+// list-build positions and cell offsets stay valid.
+__global__ void k_keep_keys(int n, const int* __restrict__ inst, const unsigned* __restrict__ iw,
+                            const unsigned* __restrict__ keys_sorted, unsigned* __restrict__ hash,
+                            const unsigned* gate) {
+    if (gated_off(gate)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!iw[IW_STRIDE * (inst[i] + 1) + IW_REBUILD]) hash[i] = keys_sorted[i];
 }
 
 // Empty displacement box (before an upload fills it, and at allocation).
@@ -416,6 +543,11 @@ cudaError_t rebuild_lists(sph_ctx* c, const KParamsT<typename P::T>& k, cudaStre
     const NbrList* nl = list_for(c);
     const unsigned* gate = c->rb;
     cudaError_t e;
+    if (per_instance(c)) {
+        k_keep_keys<<<(c->n + 255) / 256, 256, 0, s>>>(c->n, State<P>::y(c).inst, c->iw,
+                                                       c->keys_sorted, c->hash_x, gate);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     e = radix_sort_pairs(c->hash_x, nullptr, c->keys_sorted, c->perm, c->n, bits, c->sort_scratch,
                          c->sort_scratch_bytes, c->err, s, gate);
     if (e != cudaSuccess) return e;
@@ -480,8 +612,12 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     const NbrList* nl = list_for(c);
     cudaError_t e;
     if (ev) cudaEventRecord(ev[PH_SORT], s);
-    k_decide<<<1, 1, 0, s>>>(c->rb, skin_control(c), nl ? 0 : 1, cc ? cc->handle : 0,
-                             cc ? 1 : 0);
+    if (per_instance(c))
+        k_decide_inst<<<1, 256, 0, s>>>(c->rb, c->iw, c->n_inst, skin_control(c),
+                                        cc ? cc->handle : 0, cc ? 1 : 0);
+    else
+        k_decide<<<1, 1, 0, s>>>(c->rb, skin_control(c), nl ? 0 : 1, cc ? cc->handle : 0,
+                                 cc ? 1 : 0);
     e = cc ? capture_conditional_rebuild<P>(c, k, s, *cc) : rebuild_lists<P>(c, k, s, ev);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[PH_PASS1], s);
@@ -491,7 +627,7 @@ cudaError_t half_step(sph_ctx* c, HalfStep half, cudaStream_t s, cudaEvent_t* ev
     if (ev) cudaEventRecord(ev[PH_PASS2], s);
     // in place: pass 2 reads its neighbours from the pass-1 records
     e = launch_pass2_step<P>(k, half, y, c->keys_sorted, c->cell_start, nl, p1, y, c->hash_x,
-                             c->err, c->rb + RB_DISP, s);
+                             c->err, disp_words(c), s);
     if (ev) cudaEventRecord(ev[PH_COUNT], s);
     return e;
 }
@@ -602,6 +738,9 @@ extern "C" int sph_create(const sph_params* p, int capacity, sph_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = dalloc(&c->rb, RB_WORDS);
     if (e == cudaSuccess) e = cudaMemset(c->rb, 0, RB_WORDS * sizeof(unsigned));
+    if (e == cudaSuccess) e = dalloc(&c->iw, (size_t)(SPH_MAX_INSTANCES + 1) * IW_STRIDE);
+    if (e == cudaSuccess)
+        e = cudaMemset(c->iw, 0, (size_t)(SPH_MAX_INSTANCES + 1) * IW_STRIDE * sizeof(unsigned));
     if (e == cudaSuccess) {
         k_disp_reset<<<1, 32>>>(c->rb);
         e = cudaGetLastError();
@@ -728,6 +867,16 @@ extern "C" int sph_ctx_set_option(sph_ctx* c, int option, int value) {
             break;  // the slot order of the lists changed: rebuild
         }
         case SPH_OPT_WALL_RATES: c->opt_wall_rates = value != 0; return SPH_OK;
+        case SPH_OPT_INSTANCE_DECISIONS: {
+            const int v = value != 0;
+            if (v == c->opt_inst_decisions) return SPH_OK;
+            c->opt_inst_decisions = v;
+            drop_graph(c);
+            // the boxes move between the rebuild block and the instance words: new lists
+            return force_rebuild(c, nullptr) == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess
+                       ? SPH_OK
+                       : SPH_ERR_CUDA;
+        }
         case SPH_OPT_CELL_DIVISIONS: {
             // 0: the precision's default
             if (value < 0 || value > 3) return SPH_ERR_ARG;
@@ -814,6 +963,7 @@ extern "C" int sph_ctx_get_option(const sph_ctx* c, int option, int* value) {
         case SPH_OPT_PARTICLES_PER_THREAD: *value = c->opt_ppt; break;
         case SPH_OPT_ADAPTIVE_SKIN: *value = c->opt_adaptive_skin; break;
         case SPH_OPT_CELL_DIVISIONS: *value = c->opt_reach; break;
+        case SPH_OPT_INSTANCE_DECISIONS: *value = c->opt_inst_decisions; break;
         case SPH_OPT_LANES_PER_PARTICLE:
         case SPH_OPT_PASS1_LANES: *value = pass1_lanes(c); break;
         default: return SPH_ERR_ARG;
@@ -888,6 +1038,8 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
         // the displacement box restarts from the uploaded positions; a pending forced rebuild
         // (rb[2]) stays
         k_disp_reset<<<1, 32, 0, s>>>(c->rb);
+        if (c->n_inst > 1)
+            k_inst_reset<<<1, 256, 0, s>>>(c->iw, c->n_inst, skin_control(c), 0, 0);
         if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
         const NbrList* nl = list_for(c);
         return to_status(with_prec(c, [&](auto tag) {
@@ -895,7 +1047,7 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
             return launch_upload_sorted<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho,
                                            dp, dtype, c->keys_sorted, nl ? nl->xb : nullptr,
                                            State<P>::y(c), c->hash_x, c->err,
-                                           c->rb + RB_DISP, c->rb + 2, s);
+                                           disp_words(c), c->rb + 2, s);
         }));
     }
     // the state goes straight into the live set, hashed on the solver's grid; the first half
@@ -903,6 +1055,10 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
     if (cudaMemsetAsync(c->rb, 0, 4 * sizeof(unsigned), s) != cudaSuccess ||
         reset_skin(c, s) != cudaSuccess || force_rebuild(c, s) != cudaSuccess)
         return SPH_ERR_CUDA;
+    if (n_inst > 1) {
+        k_inst_reset<<<1, 256, 0, s>>>(c->iw, n_inst, skin_control(c), 0, 1);
+        if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
+    }
     return to_status(with_prec(c, [&](auto tag) {
         using P = decltype(tag);
         return launch_upload_convert<P>(resident_kparams<typename P::T>(c), dpos, dvel, drho, dp,
@@ -1274,6 +1430,25 @@ extern "C" int sph_read_list_skin(sph_ctx* c, float* skin, void* stream) {
         cudaStreamSynchronize(s) != cudaSuccess)
         return SPH_ERR_CUDA;
     std::memcpy(skin, &h, sizeof(float));
+    return SPH_OK;
+}
+
+extern "C" int sph_read_instance_rebuild_counts(sph_ctx* c, unsigned* counts, int n,
+                                                void* stream) {
+    if (!c || !counts || n < 1 || n > c->n_inst) return SPH_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (c->n_inst == 1 || !per_instance(c)) {
+        // one decision for all: every instance rebuilt with the whole set
+        unsigned h = 0;
+        if (sph_read_rebuild_count(c, &h, stream) != SPH_OK) return SPH_ERR_CUDA;
+        for (int b = 0; b < n; b++) counts[b] = h;
+        return SPH_OK;
+    }
+    if (cudaMemcpy2DAsync(counts, sizeof(unsigned), c->iw + IW_STRIDE + IW_COUNT,
+                          IW_STRIDE * sizeof(unsigned), sizeof(unsigned), (size_t)n,
+                          cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SPH_ERR_CUDA;
     return SPH_OK;
 }
 

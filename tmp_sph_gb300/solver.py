@@ -158,6 +158,12 @@ class Solver:
         call("sph_read_rebuild_count", self.handle, C.byref(v), _stream(stream))
         return v.value
 
+    def instance_rebuild_counts(self, n: int, stream=None) -> np.ndarray:
+        """List rebuilds of each of the first n instances of a batch since the upload."""
+        out = np.zeros(n, np.uint32)
+        call("sph_read_instance_rebuild_counts", self.handle, ptr(out), n, _stream(stream))
+        return out
+
     def list_skin(self, stream=None) -> float:
         """Skin of the current neighbour lists, as a fraction of kh."""
         v = C.c_float(0)

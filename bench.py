@@ -781,9 +781,10 @@ def main():
     ap.add_argument("--divisions", type=int, default=0, choices=[0, 1, 2, 3],
                     help="cells per list cutoff (SPH_OPT_CELL_DIVISIONS; 0: the library's "
                          "default)")
-    ap.add_argument("--instance-decisions", type=int, default=1, choices=[0, 1],
-                    help="batches: each instance rebuilds its lists on its own displacement "
-                         "box and skin (SPH_OPT_INSTANCE_DECISIONS; 0: one decision for all)")
+    ap.add_argument("--instance-decisions", type=int, default=0, choices=[0, 1],
+                    help="batches: 1 rebuilds each instance's lists on its own displacement "
+                         "box and skin (SPH_OPT_INSTANCE_DECISIONS; 0, the default: one "
+                         "decision for all)")
     ap.add_argument("--adaptive-skin", type=int, default=1, choices=[0, 1],
                     help="lists take a skin up to --skin chosen at each rebuild (0: always --skin)")
     ap.add_argument("--skin", type=int, default=100,

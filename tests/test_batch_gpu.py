@@ -1,12 +1,12 @@
 """GPU tests of batched instances (sph_upload_instances): several independent dam breaks
 advanced by the same launches.  The instances are stacked in one grid with empty cell layers
 between them, so every instance sees exactly the neighbours, in exactly the order, it would see
-alone when its lists are rebuilt on the same schedule.  With per-instance decisions (the
-default) each instance keeps its own displacement box and skin and rebuilds exactly when it
-would alone, so each instance of a batched run equals its solo run bit for bit, with the skin
-on or off.  With one decision for the batch (SPH_OPT_INSTANCE_DECISIONS 0) the batch rebuilds
-when any instance needs it, so summation orders — not the pairs — can differ from a solo run:
-agreement to FP32 rounding."""
+alone when its lists are rebuilt on the same schedule.  With per-instance decisions
+(SPH_OPT_INSTANCE_DECISIONS 1) each instance keeps its own displacement box and skin and
+rebuilds exactly when it would alone, so each instance of a batched run equals its solo run bit
+for bit, with the skin on or off.  With one decision for the batch (the default) the batch
+rebuilds when any instance needs it, so summation orders — not the pairs — can differ from a
+solo run: agreement to FP32 rounding, bit for bit without a skin."""
 from __future__ import annotations
 
 import ctypes

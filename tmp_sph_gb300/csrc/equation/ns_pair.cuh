@@ -222,6 +222,25 @@ __device__ __forceinline__ dvec4 ld_pos(const dvec4* __restrict__ X, size_t j) {
     return a;
 }
 
+// (ax - bx, ay - by) in one two-lane FP32 instruction (sub.rn.f32x2, sm_100 family), each lane
+// rounded as __fsub_rn rounds it: the x and y components of a record sit in adjacent registers
+// of its vector load, so the pair costs no moves.
+__device__ __forceinline__ void sub2_rn(float ax, float ay, float bx, float by, float& dx,
+                                        float& dy) {
+    asm("{.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;}"
+        : "=f"(dx), "=f"(dy)
+        : "f"(ax), "f"(ay), "f"(bx), "f"(by));
+}
+__device__ __forceinline__ void sub2_rn(double ax, double ay, double bx, double by, double& dx,
+                                        double& dy) {
+    dx = sub_rn(ax, bx);
+    dy = sub_rn(ay, by);
+}
+
 // Relative position r = x_i - x_j of a pair: from absolute positions, or (mixed precision)
 // from the offsets from their anchor cells and j's anchor relative to i's (anchor steps of
 // reach cells).
@@ -236,14 +255,15 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
         const int rz = ((int)(code >> 4) - 1) * k.reach;
         const int ry = ((int)((code >> 2) & 3u) - 1) * k.reach;
         const int rx = ((int)(code & 3u) - 1) * k.reach;
-        dx = fma_rn(-(float)rx, k.cell, sub_rn(pi.x, pj.x));
-        dy = fma_rn(-(float)ry, k.cell, sub_rn(pi.y, pj.y));
+        float ox, oy;
+        sub2_rn(pi.x, pi.y, pj.x, pj.y, ox, oy);
+        dx = fma_rn(-(float)rx, k.cell, ox);
+        dy = fma_rn(-(float)ry, k.cell, oy);
         dz = fma_rn(-(float)rz, k.cell, sub_rn(pi.z, pj.z));
     } else {
         (void)k;
         (void)code;
-        dx = sub_rn(pi.x, pj.x);
-        dy = sub_rn(pi.y, pj.y);
+        sub2_rn(pi.x, pi.y, pj.x, pj.y, dx, dy);
         dz = sub_rn(pi.z, pj.z);
     }
 }
@@ -288,8 +308,9 @@ __device__ __forceinline__ float4 as_float4(const dvec4& v) {
 // (v_i - v_j) . r with explicit rounding: x, then y and z fused in.
 template <class V, class T>
 __device__ __forceinline__ T dot_rn(const V& vi, const V& vj, T dx, T dy, T dz) {
-    return fma_rn(sub_rn(vi.z, vj.z), dz,
-                  fma_rn(sub_rn(vi.y, vj.y), dy, mul_rn(sub_rn(vi.x, vj.x), dx)));
+    T ux, uy;
+    sub2_rn(vi.x, vi.y, vj.x, vj.y, ux, uy);
+    return fma_rn(sub_rn(vi.z, vj.z), dz, fma_rn(uy, dy, mul_rn(ux, dx)));
 }
 
 // Pass-1 state of one particle: its own record and the three neighbour sums.

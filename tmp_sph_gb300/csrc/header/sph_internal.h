@@ -310,7 +310,7 @@ struct sph_ctx {
     int opt_adaptive_skin = 1;  // list skin chosen at each rebuild, up to `skin`
     int opt_reach = 1;       // cells per list cutoff (SPH_OPT_CELL_DIVISIONS): walk reach
     bool opt_reach_set = false;  // set by the caller (else the precision's default)
-    int opt_inst_decisions = 1;  // batched instances rebuild on their own decisions
+    int opt_inst_decisions = 0;  // batched instances rebuild on their own decisions
     // per-instance rebuild words (IW_*, sph_device.cuh): a header and IW_STRIDE words for each
     // of up to SPH_MAX_INSTANCES instances
     unsigned* iw = nullptr;

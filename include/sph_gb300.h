@@ -275,8 +275,8 @@ typedef struct sph_ctx sph_ctx;
 #define SPH_OPT_LANES_PER_PARTICLE 12  /* lanes of a warp per particle in list pass 1 (the
                              wall extrapolation and velocity divergence): 1 (one thread per
                              particle), 2, 4, 8 or 16 (a group of lanes shares a particle's list
-                             and reduces its sums); 0 (default): 2 in FP32 with a list skin,
-                             else 1.  With groups the lists store their entries interleaved in
+                             and reduces its sums); 0 (default): 2 in FP32 with a list skin
+                             on cells of the list cutoff (SPH_OPT_CELL_DIVISIONS 1), else 1.  With groups the lists store their entries interleaved in
                              windows of eight (a change rebuilds them).  Pass 2 runs one lane
                              per particle (groups were slower there at every size measured) */
 #define SPH_OPT_PASS1_LANES 14  /* the same as SPH_OPT_LANES_PER_PARTICLE */

@@ -22,10 +22,13 @@ def test_autotune_small_case(sphlib, cuda, report):
     # skin 0 rebuilds every half step of the profiled steps
     assert all(m["rebuilds_seen"] == 4 for m in best["table"] if m["skin_permille"] == 0)
     assert {m["divisions"] for m in best["table"]} == {1, 2}
-    # the choice is the fastest of the confirmation runs, which include the default
+    # the choice is the fastest of the confirmation runs, which include the default, unless
+    # that one beats the default by less than 1%
     conf = best["confirm"]
     assert any(c["default"] for c in conf) and 2 <= len(conf) <= 4
-    assert best["ms_per_step"] == min(c["ms_per_step"] for c in conf)
+    fastest = min(c["ms_per_step"] for c in conf)
+    base = next(c["ms_per_step"] for c in conf if c["default"])
+    assert best["ms_per_step"] == (fastest if fastest <= 0.99 * base else base)
     summ = autotune.summary(best)
     assert summ["ms_per_step"] <= summ["default_ms_per_step"]
     report("autotune small best ms per step", best["ms_per_step"])

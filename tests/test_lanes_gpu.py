@@ -88,6 +88,8 @@ def test_lanes_switch(sphlib, cuda, report):
     counts = {}
     for keep_g in (False, True):
         with S.Solver(p, len(st["rho"])) as sol:
+            # cells of the list cutoff, where the FP32 default is two lanes
+            sol.set_option(api.SPH_OPT_CELL_DIVISIONS, 1)
             sol.set_option(api.SPH_OPT_LANES_PER_PARTICLE, 1)
             sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
             counts[keep_g] = []
@@ -114,12 +116,15 @@ def test_lanes_switch(sphlib, cuda, report):
 
 
 def test_lanes_defaults(sphlib, cuda):
-    """Pass 1 takes two lanes per particle in FP32 while the lists have a skin, one without a
-    skin and in the other precisions."""
+    """Pass 1 takes two lanes per particle in FP32 on cells of the list cutoff while the lists
+    have a skin; one on the default FP32 cells of a third of the cutoff, without a skin and in
+    the other precisions."""
     from tmp_sph_gb300 import api, solver as S
     st, p = small()
     for prec, want in (("fp32", 2), ("mixed", 1), ("mixed_comp", 1), ("fp64", 1)):
         with S.Solver(p, len(st["rho"]), precision=prec) as sol:
+            assert sol.get_option(api.SPH_OPT_PASS1_LANES) == 1, prec
+            sol.set_option(api.SPH_OPT_CELL_DIVISIONS, 1)
             assert sol.get_option(api.SPH_OPT_PASS1_LANES) == want, prec
             sol.set_option(api.SPH_OPT_SKIN_PERMILLE, 0)
             assert sol.get_option(api.SPH_OPT_PASS1_LANES) == 1, prec

@@ -270,13 +270,16 @@ bool stacked_params(const sph_params& P, double skin, int reach, int n_inst, sph
     return true;
 }
 
-// Lanes per particle of list pass 1: the option, or by default 2 in FP32 while the lists have
-// a skin (4.96M-particle dam break: pass 1 −4%, step −1.6%), else 1: without a skin the lists
-// are rebuilt every half step and the build of interleaved windows costs 17% more (the step
-// 6%), and mixed precision and FP64 gain nothing (mixed: 3.640 ms per step either way).
+// Lanes per particle of list pass 1: the option, or by default 2 in FP32 on cells of the list
+// cutoff while the lists have a skin (4.96M-particle dam break: pass 1 −4%, step −1.6%), else
+// 1.  On the default FP32 cells of a third of the cutoff the particles of a warp already
+// gather shifted copies of each other's neighbour rows and one lane wins (pass 1 0.552
+// against 0.600 ms, 1000 steps from rest 2.83 against 2.91 ms per step); without a skin the
+// lists are rebuilt every half step and the build of interleaved windows costs 17% more (the
+// step 6%); mixed precision and FP64 gain nothing (mixed: 3.64 ms per step either way).
 static int pass1_lanes(const sph_ctx* c) {
     if (c->opt_lanes > 0) return c->opt_lanes;
-    return c->prec == SPH_PREC_FP32 && c->skin > 0.0 ? 2 : 1;
+    return c->prec == SPH_PREC_FP32 && c->skin > 0.0 && c->opt_reach == 1 ? 2 : 1;
 }
 
 // Threads per block of the neighbour kernels: the option, or by default 256 in FP32 (their

@@ -412,12 +412,14 @@ def configured_run(sol, stream, st, n: int, n_fluid: int, run_steps: int, steps:
 
 
 def set_lanes(sol, args) -> None:
-    """Lanes per particle of list pass 1 (--pass1-lanes; 0: the precision's default) and the
-    cell size (--divisions; 0: the library's default)."""
+    """Lanes per particle of list pass 1 (--pass1-lanes; 0: the precision's default), the cell
+    size (--divisions; 0: the library's default) and the threads per block of the neighbour
+    kernels (--threads; 0: the precision's default)."""
     from tmp_sph_gb300 import api
     sol.set_option(api.SPH_OPT_PASS1_LANES, args.pass1_lanes)
     if args.divisions:
         sol.set_option(api.SPH_OPT_CELL_DIVISIONS, args.divisions)
+    sol.set_option(api.SPH_OPT_BLOCK_THREADS, args.threads)
 
 
 def lanes_in_effect(sol) -> dict:
@@ -778,6 +780,9 @@ def main():
                          "autotuner first (overrides --skin)")
     ap.add_argument("--pass1-lanes", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
                     help="lanes per particle in list pass 1 (0: 2 in FP32 with a skin, else 1)")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="threads per block of the neighbour kernels (SPH_OPT_BLOCK_THREADS; "
+                         "0: the precision's default)")
     ap.add_argument("--divisions", type=int, default=0, choices=[0, 1, 2, 3],
                     help="cells per list cutoff (SPH_OPT_CELL_DIVISIONS; 0: the library's "
                          "default)")

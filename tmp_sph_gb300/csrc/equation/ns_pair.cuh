@@ -30,14 +30,17 @@ __device__ __forceinline__ int make_slot(int j, unsigned code) {
 // Code of a neighbour cell (xj, yj, zj) seen from cell (xi, yi, zi), both within one walk:
 // the difference of their anchors (anchor_of) in anchor steps, each in {-1, 0, 1}, two bits
 // per axis, (dz+1) << 4 | (dy+1) << 2 | (dx+1).
+// One axis of it: 0, 1 or 2 as cell c lies before, in or after the anchor column starting at
+// cell a (a = anchor_of of i's cell, c within the walk).
+__device__ __forceinline__ unsigned anchor_step(int c, int a, int r) {
+    return c < a ? 0u : (c < a + r ? 1u : 2u);
+}
 template <class KP>
 __device__ __forceinline__ unsigned cell_code(const KP& k, int xi, int yi, int zi, int xj, int yj,
                                               int zj) {
     const int r = k.reach;
-    const int dx = (anchor_of(xj, r) - anchor_of(xi, r)) / r;
-    const int dy = (anchor_of(yj, r) - anchor_of(yi, r)) / r;
-    const int dz = (anchor_of(zj, r) - anchor_of(zi, r)) / r;
-    return (unsigned)(((dz + 1) << 4) | ((dy + 1) << 2) | (dx + 1));
+    return (anchor_step(zj, anchor_of(zi, r), r) << 4) |
+           (anchor_step(yj, anchor_of(yi, r), r) << 2) | anchor_step(xj, anchor_of(xi, r), r);
 }
 
 // Column of particle i in the warp-interleaved list: slots 4g .. 4g+3 of i are the int4 at
@@ -153,15 +156,20 @@ struct Sum {
 };
 
 // Visit every candidate slot j of the (2 reach + 1)^3 cells around (cx, cy, cz): f(j, code).
-// Without CODES each x-strip is one range and code is 0; with CODES the strip's cells are
-// visited one by one and code = cell_code of j's cell seen from (cx, cy, cz).  Both visit the
-// same slots in the same order.
+// Without CODES each x-strip is one range and code is 0; with CODES the strip is visited in
+// the runs of its cells that share an anchor column and code = cell_code of j's cell seen from
+// (cx, cy, cz).  Both visit the same slots in the same order.
 template <bool CODES, class KP, class F>
 __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
                                                    int cx, int cy, int cz, F&& f) {
     const int r = k.reach;
     const int xl = cx > r - 1 ? cx - r : 0;
     const int xh = cx < k.gx - r ? cx + r : k.gx - 1;
+    // anchors of i's cell (CODES): the walk spans at most the anchor columns before, at and
+    // after them on each axis
+    const int ax = CODES ? anchor_of(cx, r) : 0;
+    const int ay = CODES ? anchor_of(cy, r) : 0;
+    const int az = CODES ? anchor_of(cz, r) : 0;
 #pragma unroll 1
     for (int dz = -r; dz <= r; dz++) {
         const int z = cz + dz;
@@ -172,15 +180,17 @@ __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __res
             if ((unsigned)y >= (unsigned)k.gy) continue;
             const int row = (z * k.gy + y) * k.gx;
             if constexpr (CODES) {
-                // the strip in runs of cells that share an anchor column (one code per run)
+                // the strip in its (at most three) runs of cells that share an anchor column,
+                // one code per run
+                const unsigned cyz = (anchor_step(z, az, r) << 4) | (anchor_step(y, ay, r) << 2);
 #pragma unroll 1
-                for (int xa = xl; xa <= xh;) {
-                    const int xb = min(anchor_of(xa, r) + r - 1, xh);
-                    const unsigned code = cell_code(k, cx, cy, cz, xa, y, z);
+                for (unsigned sx = 0; sx < 3u; sx++) {
+                    const int xa = max(xl, ax + ((int)sx - 1) * r);
+                    const int xb = min(xh, ax + (int)sx * r - 1);
+                    if (xa > xb) continue;
                     const int j0 = max(__ldg(cs + row + xa), 0);
                     const int j1 = min(__ldg(cs + row + xb + 1), k.n);  // bounds guard only
-                    for (int j = j0; j < j1; j++) f(j, code);
-                    xa = xb + 1;
+                    for (int j = j0; j < j1; j++) f(j, cyz | sx);
                 }
             } else {
                 const int j0 = max(__ldg(cs + row + xl), 0);
@@ -252,14 +262,18 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
     if constexpr (P::kMixed) {
         // one explicitly rounded difference and one fused multiply-add per axis, so every
         // caller (list, cell walk, list build) gets the same bits whatever the compiler hoists
-        const int rz = ((int)(code >> 4) - 1) * k.reach;
-        const int ry = ((int)((code >> 2) & 3u) - 1) * k.reach;
-        const int rx = ((int)(code & 3u) - 1) * k.reach;
+        // each 2-bit field f of the code as the float f - 1 without an integer conversion:
+        // the float with bits 0x4B000000 | f is 2^23 + f; times the reach (exact small
+        // integers), the same values as the integer form
+        const float rf = (float)k.reach;
+        const float fx = sub_rn(__uint_as_float(0x4B000000u | (code & 3u)), 8388609.0f);
+        const float fy = sub_rn(__uint_as_float(0x4B000000u | ((code >> 2) & 3u)), 8388609.0f);
+        const float fz = sub_rn(__uint_as_float(0x4B000000u | (code >> 4)), 8388609.0f);
         float ox, oy;
         sub2_rn(pi.x, pi.y, pj.x, pj.y, ox, oy);
-        dx = fma_rn(-(float)rx, k.cell, ox);
-        dy = fma_rn(-(float)ry, k.cell, oy);
-        dz = fma_rn(-(float)rz, k.cell, sub_rn(pi.z, pj.z));
+        dx = fma_rn(-mul_rn(fx, rf), k.cell, ox);
+        dy = fma_rn(-mul_rn(fy, rf), k.cell, oy);
+        dz = fma_rn(-mul_rn(fz, rf), k.cell, sub_rn(pi.z, pj.z));
     } else {
         (void)k;
         (void)code;

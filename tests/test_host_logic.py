@@ -44,9 +44,15 @@ def test_autotune_cost_model():
     st = {"type": np.array([1, 1, 0]), "pos": np.array([[0, 0, 0.1], [0, 0, 0.3], [0, 0, 0.9]])}
     assert math.isclose(autotune.surge_speed([st], -9.81), 2 * math.sqrt(9.81 * 0.3))
     # the default the confirmation runs compare against
-    assert autotune.default_choice("fp32") == {"threads": 256, "ppt": 1, "lanes": 2,
+    assert autotune.default_choice("fp32") == {"threads": 256, "ppt": 1, "lanes": 1,
                                                "skin_permille": 100, "divisions": 3}
     assert autotune.default_choice("mixed")["threads"] == 128
+    # a candidate replaces the default only when it is at least `margin` faster
+    runs = [{"ms_per_step": 2.70, "default": True}, {"ms_per_step": 2.69, "default": False}]
+    assert autotune.pick(runs, 0.01)["default"]
+    runs[1]["ms_per_step"] = 2.60
+    assert not autotune.pick(runs, 0.01)["default"]
+    assert autotune.pick(runs[:1], 0.01)["default"]
 
 
 def test_launch_count():

@@ -133,6 +133,14 @@ def timed_run(p, states, choice: dict, precision: str, steps: int, stream) -> fl
         return e0.elapsed_time(e1) / steps
 
 
+def pick(confirm: list, margin: float) -> dict:
+    """The fastest of the confirmation runs, or the default's run (the one marked "default")
+    when the fastest beats it by less than the fraction `margin`."""
+    best = min(confirm, key=lambda c: c["ms_per_step"])
+    base = next(c for c in confirm if c["default"])
+    return best if best["ms_per_step"] <= (1.0 - margin) * base["ms_per_step"] else base
+
+
 def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=SKINS,
          lanes=LANES, divisions=DIVISIONS, speed: float | None = None,
          confirm_steps: int = 100, confirm_top: int = 3, margin: float = 0.01) -> dict:
@@ -184,10 +192,7 @@ def tune(p, states, *, precision: str = "fp32", threads=THREADS, ppt=PPT, skins=
         c["ms_per_step"] = timed_run(p, states, c, precision, confirm_steps, stream)
         c["default"] = _key(c) == _key(dflt)
         confirm.append(c)
-    best = min(confirm, key=lambda c: c["ms_per_step"])
-    base = next(c for c in confirm if c["default"])
-    if best["ms_per_step"] > (1.0 - margin) * base["ms_per_step"]:
-        best = base
+    best = pick(confirm, margin)
     out = {k: best[k] for k in ("threads", "ppt", "lanes", "skin_permille", "divisions")}
     out.update({"speed_m_s": v, "precision": precision, "ms_per_step": best["ms_per_step"],
                 "confirm_steps": confirm_steps, "confirm": confirm, "table": table})

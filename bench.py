@@ -19,7 +19,10 @@ Printed: one JSON line (rank 0) with
                  counts of the initial state) / step time, over the FP32 FMA peak measured now
   configured_run the configured 1000 steps from rest, all timed, then the developed flow
   batched        config 4: 64 dam breaks of uneven size in one batched mixed-precision solver
-                 (graph replay), beside the plain FP32 single-instance value above
+                 (graph replay), beside the plain FP32 single-instance value above, and the
+                 same batch in FP32 (short window)
+  drop_in_step_loop  the reference's own step loop through the library's C-ABI drop-ins
+                 (calcHash ... recover every half step, on the reference grid)
   reference_cuda the reference's own CUDA versions (opt_src_v4, the best, and src/) on the
                  same state and GPU, from kernels compiled out of its sources (oracle/_ref)
   cpu_baseline   the oracle (C restatement of the reference, OpenMP) on a bounded sample
@@ -309,6 +312,57 @@ def fp32_peak(stream) -> dict:
              C.byref(ms), C.c_void_p(stream.cuda_stream))
     return {"tflops": fl.value / (ms.value / 1e3) / 1e12, "ms": ms.value, "blocks": blocks,
             "how": "sph_measure_fp32_peak: 8 independent FMA chains per thread, CUDA events"}
+
+
+def dropin_measure(st: dict, p, stream, steps: int = 10, warmup: int = 3) -> dict:
+    """The reference's own step loop (src/sph/sph_run.cu:285-336: calcHash, sortParticles,
+    reorder, SPH_NS_simpleversion, PC_prediction / PC_correction and recover every half step,
+    on the reference's grid and AoS arrays) run through this library's C-ABI drop-ins on the
+    same state: what the reference's driver gets by linking the library instead of its own
+    kernels, timed by CUDA events on `stream`."""
+    import torch
+    from tmp_sph_gb300 import api, solver as S
+    n = len(st["rho"])
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+    d = {k: dev(st[k]) for k in ("pos", "vel", "rho", "p", "type")}
+    s = {k: torch.empty_like(v) for k, v in d.items()}
+    h = torch.empty(n, dtype=torch.int32, device="cuda")
+    idx = torch.empty_like(h)
+    cs = torch.empty(p.num_cells, dtype=torch.int32, device="cuda")
+    ce = torch.empty_like(cs)
+    rdt, dofv = torch.zeros(n, device="cuda"), torch.zeros(n, device="cuda")
+    vdt = torch.zeros((n, 3), device="cuda")
+    tmp = (torch.zeros((n, 3), device="cuda"), torch.zeros((n, 3), device="cuda"),
+           torch.zeros(n, device="cuda"))
+    scratch = torch.empty(api.sort_scratch_bytes(n), dtype=torch.uint8, device="cuda")
+    with S.Solver(p, n) as sol:  # sph_ns takes its constants from a context
+        def half(k):
+            S.calc_hash(p, d["pos"], h, idx, n, stream)
+            S.sort_particles(h, idx, n, 32, scratch, stream)  # the shim's full-int sort
+            S.reorder(p, d["pos"], d["vel"], d["rho"], d["p"], d["type"], None, s["pos"],
+                      s["vel"], s["rho"], s["p"], s["type"], None, h, idx, cs, ce, n, stream)
+            sol.ns(s["pos"], s["vel"], s["rho"], s["p"], s["type"], rdt, vdt, cs, ce, n, h, dofv,
+                   stream=stream)
+            pc = S.pc_prediction if k == 0 else S.pc_correction
+            pc(p, s["pos"], s["vel"], s["rho"], s["p"], rdt, vdt, idx, *tmp, n, s["type"], stream)
+            S.recover(d["pos"], d["vel"], d["rho"], d["p"], n, idx, d["type"], None, s["pos"],
+                      s["vel"], s["rho"], s["p"], s["type"], None, stream)
+        for _ in range(warmup):
+            half(0)
+            half(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            half(0)
+            half(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    return {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "warmup": warmup, "path": "calcHash, sortParticles (32-bit keys), reorder, "
+            "SPH_NS_simpleversion (27-cell walks on the reference grid), PC_prediction / "
+            "PC_correction, recover through the C ABI, every half step"}
 
 
 def reference_cuda_leg(st: dict, p, versions=(("v4", 1, 10), ("src", 0, 2))) -> dict:
@@ -994,12 +1048,28 @@ def main():
         batched["launch_gap_share"] = 6 * gap / (1e3 * batched["ms_per_step"])
         batched["launch_gap_share_plain_fp32"] = 6 * gap / (1e3 * ms / args.steps)
 
+    if args.batch_instances > 0 and ws == 1 and args.precision == "fp32":
+        # the same batch in plain FP32 (short window): what batching alone gives, beside the
+        # mixed-precision batch
+        bf = batch_measure(args.batch_instances, "fp32", args, stream, args.steps, args.warmup)
+        batched["fp32_same_batch"] = {k: bf[k] for k in ("value", "ms_per_step", "steps",
+                                                           "device_error_flags")}
+        batched["fp32_same_batch"]["cell_divisions"] = bf["config"]["cell_divisions"]
+        batched["fp32_same_batch"]["vs_plain_fp32"] = bf["value"] / value
+
+    dropin = None
+    if rank == 0 and ws == 1 and args.precision == "fp32":
+        dropin = dropin_measure(st, p, stream)
+        dropin["resident_over_dropin"] = value / dropin["value"]
+
     ref_cuda = None
     if rank == 0 and ws == 1 and not args.no_reference_cuda:
         ref_cuda = reference_cuda_leg(st, p)
         for v in ("v4", "src"):
             if isinstance(ref_cuda.get(v), dict) and "value" in ref_cuda[v]:
                 ref_cuda[v]["this_over_reference"] = value / ref_cuda[v]["value"]
+                if dropin:
+                    dropin[f"over_reference_{v}"] = dropin["value"] / ref_cuda[v]["value"]
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -1023,6 +1093,7 @@ def main():
         "phases": phases,
         "cpu_baseline": cpu,
         "reference_cuda": ref_cuda,
+        "drop_in_step_loop": dropin,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
         "gpu_launches": count_launches(sol_cells, 2 * args.steps, rebuilds, args.graph_mode),

@@ -320,8 +320,9 @@ k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
 }
 
 // The same kernel held to CAP registers (one particle per thread): the FP32 step kernel fits
-// in 48 with an 8-byte stack frame, keeping ten 128-thread blocks resident per SM where the
-// unconstrained 53 keeps nine; the mixed-precision one in 56 (nine blocks instead of eight).
+// in 48 without spills (five 256-thread blocks per SM; 40 registers, six blocks, spilled 40
+// bytes and measured the same: 0.7255 against 0.7250 ms at 4.96M), the mixed-precision one in
+// 56 (nine 128-thread blocks instead of eight).
 template <class P, int MODE, int LIST, bool GS, int CAP>
 __global__ void __maxnreg__(CAP)
 k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,

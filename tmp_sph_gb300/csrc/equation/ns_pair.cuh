@@ -262,18 +262,16 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
     if constexpr (P::kMixed) {
         // one explicitly rounded difference and one fused multiply-add per axis, so every
         // caller (list, cell walk, list build) gets the same bits whatever the compiler hoists
-        // each 2-bit field f of the code as the float f - 1 without an integer conversion:
-        // the float with bits 0x4B000000 | f is 2^23 + f; times the reach (exact small
-        // integers), the same values as the integer form
-        const float rf = (float)k.reach;
+        // each 2-bit field f of the code as the float f - 1 without an integer conversion (the
+        // float with bits 0x4B000000 | f is 2^23 + f), times one anchor step reach * cell
         const float fx = sub_rn(__uint_as_float(0x4B000000u | (code & 3u)), 8388609.0f);
         const float fy = sub_rn(__uint_as_float(0x4B000000u | ((code >> 2) & 3u)), 8388609.0f);
         const float fz = sub_rn(__uint_as_float(0x4B000000u | (code >> 4)), 8388609.0f);
         float ox, oy;
         sub2_rn(pi.x, pi.y, pj.x, pj.y, ox, oy);
-        dx = fma_rn(-mul_rn(fx, rf), k.cell, ox);
-        dy = fma_rn(-mul_rn(fy, rf), k.cell, oy);
-        dz = fma_rn(-mul_rn(fz, rf), k.cell, sub_rn(pi.z, pj.z));
+        dx = fma_rn(-fx, k.reach_cell, ox);
+        dy = fma_rn(-fy, k.reach_cell, oy);
+        dz = fma_rn(-fz, k.reach_cell, sub_rn(pi.z, pj.z));
     } else {
         (void)k;
         (void)code;

@@ -63,6 +63,7 @@ struct KParamsT {
     int list_win;  // list entries interleaved in windows of eight (for lane groups; ns_pair.cuh)
     T gmin_x, gmin_y, gmin_z;
     T cell;              // cell edge (gridSize)
+    T reach_cell;        // reach * cell, rounded once: one anchor step of mixed precision
     T inv_cell;          // 1 / cell (the FP64 and mixed solvers' hash scales by it)
     T h, inv_h, kh, kh2;
     T kh2_list;          // squared list cutoff (support radius + skin); kh2 without a skin

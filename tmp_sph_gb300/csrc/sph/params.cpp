@@ -36,6 +36,7 @@ KParams make_kparams(const sph_params& p, int n) {
     k.gz_stride = p.grid_dim[2];
     k.inst_cells = 0;
     k.reach = 1;
+    k.reach_cell = k.cell;
     k.threads = 128;
     k.ppt = 1;
     k.lanes = 1;
@@ -102,6 +103,7 @@ KParamsT<double> make_kparams_t<double>(const sph_params& p, int n) {
     k.gz_stride = p.grid_dim[2];
     k.inst_cells = 0;
     k.reach = 1;
+    k.reach_cell = k.cell;
     k.threads = 128;
     k.ppt = 1;
     k.lanes = 1;

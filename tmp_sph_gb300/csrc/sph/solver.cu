@@ -313,6 +313,7 @@ KParamsT<T> resident_kparams(const sph_ctx* c) {
     k.lanes = groups ? pass1_lanes(c) : 1;
     k.list_win = k.lanes > 1;
     k.reach = c->opt_reach;
+    k.reach_cell = (T)c->opt_reach * k.cell;
     k.gz_stride = c->n_inst > 1 ? instance_stride(c->gz_inst, c->opt_reach) : c->gz_inst;
     k.inst_boxes = per_instance(c) ? 1 : 0;
     k.inst_cells = c->n_inst > 1 ? c->Pi.grid_dim[0] * c->Pi.grid_dim[1] * k.gz_stride : 0;

@@ -392,13 +392,16 @@ int sph_steps_taken(const sph_ctx* ctx, long long* steps);
 /* Accumulated milliseconds and launch counts per phase under SPH_OPT_PROFILE
  * (arrays of SPH_PHASE_COUNT); reset != 0 clears them. */
 int sph_profile_read(sph_ctx* ctx, double* ms, long long* launches, int reset);
-/* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream). */
+/* Cell-list / neighbour-list rebuilds since the last upload (synchronises the stream); with
+ * per-instance decisions (SPH_OPT_INSTANCE_DECISIONS), the half steps in which any instance
+ * rebuilt. */
 int sph_read_rebuild_count(sph_ctx* ctx, unsigned* count, void* stream);
 /* List rebuilds of each of the first n instances of a batch since the upload (host array of n;
  * synchronises the stream).  Without per-instance decisions every instance reports the count
  * of sph_read_rebuild_count. */
 int sph_read_instance_rebuild_counts(sph_ctx* ctx, unsigned* counts, int n, void* stream);
-/* Skin of the current neighbour lists as a fraction of kh (synchronises the stream). */
+/* Skin of the current neighbour lists as a fraction of kh (synchronises the stream); with
+ * per-instance decisions, the largest skin of the instances. */
 int sph_read_list_skin(sph_ctx* ctx, float* skin, void* stream);
 
 /* ---------------------------------------------------------------- probes and reductions */

@@ -212,11 +212,38 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
         }
     }
     SlotWriter<WIN> w(nl.idx + nbr_col(nl, i), nl.cap, stage);
-    walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
-                     [&](int j, unsigned code, const vec4_t<T>& pj, T, T, T, T) {
-        if (keep_all || fluid_rec(pj.w))
-            w.put(P::kMixed ? make_slot(j, code) : j);
-    });
+    if constexpr (P::kMixed) {
+        // i's offsets moved into each run's anchor frame once per run instead of decoding the
+        // code for every candidate.  That rounds differently from the passes' decode, so the
+        // cutoff is widened by 2^-16: every pair the passes would put inside it is listed, and
+        // the passes test r < kh with their own decode, so they still evaluate exactly the
+        // pairs of a cell walk.
+        const unsigned key = keys[i];
+        if (!inactive_key(k, key)) {
+            int cx, cy, cz;
+            cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+            const T cut2w = cut2 * (T(1) + T(1.0 / 65536.0));
+            for_each_run<true>(k, cs, cx, cy, cz, [&](int j0, int j1, unsigned code) {
+                float fx, fy, fz;
+                code_steps(code, fx, fy, fz);
+                const float sx = fma_rn(-fx, k.reach_cell, pi.x);
+                const float sy = fma_rn(-fy, k.reach_cell, pi.y);
+                const float sz = fma_rn(-fz, k.reach_cell, pi.z);
+#pragma unroll 4
+                for (int j = j0; j < j1; j++) {
+                    const vec4_t<T> pj = ld_pos(X, (size_t)j);
+                    const T r2 = dist2(sub_rn(sx, pj.x), sub_rn(sy, pj.y), sub_rn(sz, pj.z));
+                    if (r2 < cut2w && j != i && (keep_all || fluid_rec(pj.w)))
+                        w.put(make_slot(j, code));
+                }
+            });
+        }
+    } else {
+        walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
+                         [&](int j, unsigned, const vec4_t<T>& pj, T, T, T, T) {
+            if (keep_all || fluid_rec(pj.w)) w.put(j);
+        });
+    }
     w.flush();
     nl.count[i] = w.cnt;
     raise_flags(err, w.cnt > nl.cap ? SPH_FLAG_NEIGHBOR_OVERFLOW : 0u);

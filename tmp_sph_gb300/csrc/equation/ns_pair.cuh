@@ -155,13 +155,14 @@ struct Sum {
     }
 };
 
-// Visit every candidate slot j of the (2 reach + 1)^3 cells around (cx, cy, cz): f(j, code).
-// Without CODES each x-strip is one range and code is 0; with CODES the strip is visited in
-// the runs of its cells that share an anchor column and code = cell_code of j's cell seen from
-// (cx, cy, cz).  Both visit the same slots in the same order.
+// Visit the candidate slots of the (2 reach + 1)^3 cells around (cx, cy, cz) as contiguous
+// ranges: run(j0, j1, code) for slots j0 .. j1 - 1.  Without CODES each x-strip is one range
+// and code is 0; with CODES the strip is split into the runs of its cells that share an anchor
+// column and code = cell_code of their cells seen from (cx, cy, cz).  Both visit the same
+// slots in the same order.
 template <bool CODES, class KP, class F>
-__device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
-                                                   int cx, int cy, int cz, F&& f) {
+__device__ __forceinline__ void for_each_run(const KP& k, const int* __restrict__ cs, int cx,
+                                             int cy, int cz, F&& run) {
     const int r = k.reach;
     const int xl = cx > r - 1 ? cx - r : 0;
     const int xh = cx < k.gx - r ? cx + r : k.gx - 1;
@@ -190,16 +191,33 @@ __device__ __forceinline__ void for_each_candidate(const KP& k, const int* __res
                     if (xa > xb) continue;
                     const int j0 = max(__ldg(cs + row + xa), 0);
                     const int j1 = min(__ldg(cs + row + xb + 1), k.n);  // bounds guard only
-                    for (int j = j0; j < j1; j++) f(j, cyz | sx);
+                    run(j0, j1, cyz | sx);
                 }
             } else {
                 const int j0 = max(__ldg(cs + row + xl), 0);
                 const int j1 = min(__ldg(cs + row + xh + 1), k.n);  // bounds guard only
-#pragma unroll 4
-                for (int j = j0; j < j1; j++) f(j, 0u);
+                run(j0, j1, 0u);
             }
         }
     }
+}
+
+// Every candidate slot of that walk: f(j, code).
+template <bool CODES, class KP, class F>
+__device__ __forceinline__ void for_each_candidate(const KP& k, const int* __restrict__ cs,
+                                                   int cx, int cy, int cz, F&& f) {
+    for_each_run<CODES>(k, cs, cx, cy, cz, [&](int j0, int j1, unsigned code) {
+#pragma unroll 4
+        for (int j = j0; j < j1; j++) f(j, code);
+    });
+}
+
+// The anchor steps of a mixed-precision cell code as floats: each 2-bit field f as f - 1,
+// without an integer conversion (the float with bits 0x4B000000 | f is 2^23 + f).
+__device__ __forceinline__ void code_steps(unsigned code, float& fx, float& fy, float& fz) {
+    fx = __fsub_rn(__uint_as_float(0x4B000000u | (code & 3u)), 8388609.0f);
+    fy = __fsub_rn(__uint_as_float(0x4B000000u | ((code >> 2) & 3u)), 8388609.0f);
+    fz = __fsub_rn(__uint_as_float(0x4B000000u | (code >> 4)), 8388609.0f);
 }
 
 // One record (two vec4) in single 256-bit read-only loads: a neighbour gather touches one L1
@@ -262,11 +280,9 @@ __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const 
     if constexpr (P::kMixed) {
         // one explicitly rounded difference and one fused multiply-add per axis, so every
         // caller (list, cell walk, list build) gets the same bits whatever the compiler hoists
-        // each 2-bit field f of the code as the float f - 1 without an integer conversion (the
-        // float with bits 0x4B000000 | f is 2^23 + f), times one anchor step reach * cell
-        const float fx = sub_rn(__uint_as_float(0x4B000000u | (code & 3u)), 8388609.0f);
-        const float fy = sub_rn(__uint_as_float(0x4B000000u | ((code >> 2) & 3u)), 8388609.0f);
-        const float fz = sub_rn(__uint_as_float(0x4B000000u | (code >> 4)), 8388609.0f);
+        // the anchor steps of the code times one anchor step reach * cell
+        float fx, fy, fz;
+        code_steps(code, fx, fy, fz);
         float ox, oy;
         sub2_rn(pi.x, pi.y, pj.x, pj.y, ox, oy);
         dx = fma_rn(-fx, k.reach_cell, ox);

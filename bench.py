@@ -19,8 +19,9 @@ Printed: one JSON line (rank 0) with
                  counts of the initial state) / step time, over the FP32 FMA peak measured now
   configured_run the configured 1000 steps from rest, all timed, then the developed flow
   batched        config 4: 64 dam breaks of uneven size in one batched mixed-precision solver
-                 (graph replay), beside the plain FP32 single-instance value above, and the
-                 same batch in FP32 (short window)
+                 (graph replay; FP64 integration, FP32 sums on FP32 positions by default,
+                 --batch-precision), beside the plain FP32 single-instance value above, and
+                 the same batch in FP32 and in the other mixed form (short windows)
   drop_in_step_loop  the reference's own step loop through the library's C-ABI drop-ins
                  (calcHash ... recover every half step, on the reference grid)
   reference_cuda the reference's own CUDA versions (opt_src_v4, the best, and src/) on the
@@ -559,7 +560,7 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
     out = {"value": n_all * steps / (ms / 1e3), "unit": UNIT,
            "fluid_value": n_fluid_all * steps / (ms / 1e3), "ms_per_step": ms / steps,
            "steps": steps, "warmup": warmup,
-           "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+           "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64", "mixed_abs": "f32+f64",
                      "fp64": "f64"}[precision],
            "config": {"workload": f"dam_break_batch{n_inst}_{precision}", "instances": n_inst,
                       "instances_this_rank": hi - lo, "particles": n_all,
@@ -827,7 +828,8 @@ def main():
     ap.add_argument("--graph-mode", default="conditional", choices=["conditional", "gated"],
                     help="rebuild kernels of the step graph under conditional nodes, or launched "
                          "every half step and returning at once when the lists are kept")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "mixed_comp", "fp64"],
+    ap.add_argument("--precision", default="fp32",
+                    choices=["fp32", "mixed", "mixed_comp", "mixed_abs", "fp64"],
                     help="precision of the timed solver (the other two are timed beside it)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick threads per block, particles per thread and skin with the "
@@ -840,6 +842,11 @@ def main():
     ap.add_argument("--divisions", type=int, default=0, choices=[0, 1, 2, 3],
                     help="cells per list cutoff (SPH_OPT_CELL_DIVISIONS; 0: the library's "
                          "default)")
+    ap.add_argument("--batch-precision", default="mixed_abs",
+                    choices=["mixed_abs", "mixed", "mixed_comp", "fp32"],
+                    help="precision of the batched block of the default line: mixed_abs (FP64 "
+                         "integration, FP32 sums on FP32 positions; the default) or mixed "
+                         "(FP32 sums on cell-local offsets)")
     ap.add_argument("--instance-decisions", type=int, default=0, choices=[0, 1],
                     help="batches: 1 rebuilds each instance's lists on its own displacement "
                          "box and skin (SPH_OPT_INSTANCE_DECISIONS; 0, the default: one "
@@ -964,7 +971,8 @@ def main():
         return out
 
     variants = {prec: time_precision(prec, min(args.steps, 10 if prec == "fp64" else 50))
-                for prec in ("fp32", "mixed", "mixed_comp", "fp64") if prec != args.precision}
+                for prec in ("fp32", "mixed", "mixed_comp", "mixed_abs", "fp64")
+                if prec != args.precision}
 
     hbm_peak, peak_kind = peaks()
     phases = {}
@@ -1037,8 +1045,8 @@ def main():
     # plain FP32 single-instance drop-in above
     batched = None
     if args.batch_instances > 0 and ws == 1:
-        batched = batch_measure(args.batch_instances, "mixed", args, stream, args.steps,
-                                args.warmup, run_steps=args.run_steps,
+        batched = batch_measure(args.batch_instances, args.batch_precision, args, stream,
+                                args.steps, args.warmup, run_steps=args.run_steps,
                                 clocks=ClockSampler(gpu_uuid(local)))
         batched["vs_plain_fp32"] = batched["value"] / value
         # what a persistent kernel could save: the graph's launch gaps (three kernel nodes per
@@ -1049,13 +1057,15 @@ def main():
         batched["launch_gap_share_plain_fp32"] = 6 * gap / (1e3 * ms / args.steps)
 
     if args.batch_instances > 0 and ws == 1 and args.precision == "fp32":
-        # the same batch in plain FP32 (short window): what batching alone gives, beside the
-        # mixed-precision batch
-        bf = batch_measure(args.batch_instances, "fp32", args, stream, args.steps, args.warmup)
-        batched["fp32_same_batch"] = {k: bf[k] for k in ("value", "ms_per_step", "steps",
-                                                           "device_error_flags")}
-        batched["fp32_same_batch"]["cell_divisions"] = bf["config"]["cell_divisions"]
-        batched["fp32_same_batch"]["vs_plain_fp32"] = bf["value"] / value
+        # the same batch in plain FP32 (what batching alone gives) and in the other mixed form
+        # (cell-local offsets, or FP32 positions), short windows, beside the batched block
+        other = "mixed" if args.batch_precision == "mixed_abs" else "mixed_abs"
+        for prec in ("fp32", other):
+            bf = batch_measure(args.batch_instances, prec, args, stream, args.steps, args.warmup)
+            blk = {k: bf[k] for k in ("value", "ms_per_step", "steps", "device_error_flags")}
+            blk["cell_divisions"] = bf["config"]["cell_divisions"]
+            blk["vs_plain_fp32"] = bf["value"] / value
+            batched[f"{prec}_same_batch"] = blk
 
     dropin = None
     if rank == 0 and ws == 1 and args.precision == "fp32":
@@ -1080,7 +1090,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64", "mixed_abs": "f32+f64",
                   "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
         "config": config_block(args, p, n, lanes),

@@ -313,6 +313,11 @@ typedef struct sph_ctx sph_ctx;
                              the time integration; n < 2^26 */
 #define SPH_PREC_MIXED_COMP 3  /* SPH_PREC_MIXED with compensated (Neumaier) accumulation of the
                              density and force sums */
+#define SPH_PREC_MIXED_ABS 4  /* FP64 master positions and density perturbation for the time
+                             integration, as SPH_PREC_MIXED, but the neighbour sums run on FP32
+                             positions in the simulation's own frame (rounded from the FP64
+                             ones every half step) instead of cell-local offsets: the FP32
+                             pair arithmetic, no per-pair cell code */
 
 /* Phases reported by sph_profile_read: [0] radix sort, [1] gather + cell starts,
  * [2] neighbour-list build, [3] neighbour pass 1, [4] neighbour pass 2 + integrator;

@@ -33,7 +33,8 @@ def solo(st, p, nsteps, precision, skin=100):
 
 
 @pytest.mark.parametrize("precision,skin,own", [("fp32", 0, 1), ("mixed", 0, 1), ("fp32", 100, 1),
-                                                ("mixed", 100, 1), ("fp32", 100, 0)])
+                                                ("mixed", 100, 1), ("mixed_abs", 100, 1),
+                                                ("fp32", 100, 0)])
 def test_batched_instances_equal_solo_runs(sphlib, cuda, report, precision, skin, own):
     import torch
     from tmp_sph_gb300 import api, cases, solver as S

@@ -65,7 +65,7 @@ def test_divisions_list_equals_walk(sphlib, cuda, div):
 
 
 @pytest.mark.parametrize("div", [2, 3])
-@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("precision", ["fp32", "mixed", "mixed_abs"])
 def test_divisions_batch_equals_solo(sphlib, cuda, div, precision):
     """Mixed precision anchors a particle's offsets at a cell whose coordinates are multiples of
     the reach; the instances are stacked every multiple of the reach, so an instance's anchors,
@@ -120,11 +120,13 @@ def test_divisions_switch_and_checks(sphlib, cuda):
 
 
 def test_divisions_defaults(sphlib, cuda):
-    """Cells of a third of the list cutoff in FP32, of the cutoff in the other precisions; a
-    precision change moves the default along unless the caller set the cell size."""
+    """Cells of a third of the list cutoff with the FP32 pair arithmetic (FP32 and mixed on
+    FP32 positions), of the cutoff in the other precisions; a precision change moves the
+    default along unless the caller set the cell size."""
     from tmp_sph_gb300 import api, cases, solver as S
     _, p = cases.build("small", physics="config", dx=0.04)
-    for prec, want in (("fp32", 3), ("mixed", 1), ("mixed_comp", 1), ("fp64", 1)):
+    for prec, want in (("fp32", 3), ("mixed", 1), ("mixed_comp", 1), ("mixed_abs", 3),
+                       ("fp64", 1)):
         with S.Solver(p, 1000, precision=prec) as sol:
             assert sol.get_option(api.SPH_OPT_CELL_DIVISIONS) == want, prec
     with S.Solver(p, 1000) as sol:

@@ -2,9 +2,9 @@
 
 * FP64 is the accuracy reference: it must agree with the oracle's FP64 restatement of the
   reference step loop to FP64 rounding growth.
-* FP32 and mixed precision are measured against the FP64 run of the same solver; the bar is
-  1e-3 relative L2 on the flow fields after 1000 steps.
-* The mixed-precision neighbour list and cell walk visit the same pairs in the same order, so
+* FP32 and the mixed precisions are measured against the FP64 run of the same solver; the bar
+  is 1e-3 relative L2 on the flow fields after 1000 steps.
+* The mixed-precision neighbour lists and cell walks visit the same pairs in the same order, so
   they agree bit for bit, as in FP32."""
 from __future__ import annotations
 
@@ -77,7 +77,7 @@ def test_fp32_and_mixed_against_fp64(sphlib, cuda, report):
     ref = run_prec(st, p, steps, "fp64")
     assert ref["flags"] == 0
     res = {}
-    for prec in ("fp32", "mixed", "mixed_comp"):
+    for prec in ("fp32", "mixed", "mixed_comp", "mixed_abs"):
         out = run_prec(st, p, steps, prec)
         assert out["flags"] == 0, prec
         res[prec] = errors(out["f64"], ref["f64"], st)
@@ -87,17 +87,18 @@ def test_fp32_and_mixed_against_fp64(sphlib, cuda, report):
         assert all(v < 1e-3 for v in e.values()), (prec, e)
 
 
-def test_mixed_list_matches_cell_walk(sphlib, cuda):
-    """Mixed precision: one-lane list passes and walking passes (cell codes from the walk)
-    agree bit for bit; an overflowing list falls back to the same walk."""
+@pytest.mark.parametrize("precision", ["mixed", "mixed_abs"])
+def test_mixed_list_matches_cell_walk(sphlib, cuda, precision):
+    """Mixed precision: one-lane list passes and walking passes (cell codes from the walk, or
+    FP32 positions) agree bit for bit; an overflowing list falls back to the same walk."""
     from tmp_sph_gb300 import api, cases
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
     one = {api.SPH_OPT_LANES_PER_PARTICLE: 1}
-    a = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_SKIN_PERMILLE: 0})
-    b = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_SKIN_PERMILLE: 0,
-                                     api.SPH_OPT_NEIGHBOR_LIST: 0})
-    c = run_prec(st, p, 5, "mixed", {**one, api.SPH_OPT_NEIGHBOR_CAP: 8})
-    d = run_prec(st, p, 5, "mixed", one)
+    a = run_prec(st, p, 5, precision, {**one, api.SPH_OPT_SKIN_PERMILLE: 0})
+    b = run_prec(st, p, 5, precision, {**one, api.SPH_OPT_SKIN_PERMILLE: 0,
+                                       api.SPH_OPT_NEIGHBOR_LIST: 0})
+    c = run_prec(st, p, 5, precision, {**one, api.SPH_OPT_NEIGHBOR_CAP: 8})
+    d = run_prec(st, p, 5, precision, one)
     assert a["flags"] == 0 and b["flags"] == 0 and d["flags"] == 0
     assert c["flags"] & api.SPH_FLAG_NEIGHBOR_OVERFLOW
     for k in ("pos", "vel", "rho", "p"):
@@ -105,7 +106,7 @@ def test_mixed_list_matches_cell_walk(sphlib, cuda):
         assert np.array_equal(c[k], d[k]), k
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_abs"])
 def test_graph_replay_bitwise(sphlib, cuda, precision):
     from tmp_sph_gb300 import cases
     from gpu_util import perturbed

@@ -49,8 +49,9 @@ SPH_OPT_ADAPTIVE_SKIN = 13
 SPH_OPT_CELL_DIVISIONS = 16
 SPH_OPT_INSTANCE_DECISIONS = 17
 SPH_PREC_FP32, SPH_PREC_FP64, SPH_PREC_MIXED, SPH_PREC_MIXED_COMP = 0, 1, 2, 3
+SPH_PREC_MIXED_ABS = 4
 PRECISIONS = {"fp32": SPH_PREC_FP32, "fp64": SPH_PREC_FP64, "mixed": SPH_PREC_MIXED,
-              "mixed_comp": SPH_PREC_MIXED_COMP}
+              "mixed_comp": SPH_PREC_MIXED_COMP, "mixed_abs": SPH_PREC_MIXED_ABS}
 SPH_FLAG_NEIGHBOR_OVERFLOW = 0x8
 SPH_PHASE_COUNT = 5
 PHASE_NAMES = ("sort", "gather_cells", "nbr_build", "pass1", "pass2_integrate")

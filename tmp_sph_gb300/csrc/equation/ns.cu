@@ -152,11 +152,11 @@ __device__ __forceinline__ void visit_records(const KParamsT<typename P::T>& k,
         const int cnt = __ldg(nl.count + i);
         if (cnt <= nl.cap) {
             auto one = [&](int e) {
-                const int j = P::kMixed ? slot_index(e) : e;
+                const int j = P::kCodes ? slot_index(e) : e;
                 V a, b;
                 ld_rec(R, j, a, b);
                 T dx, dy, dz;
-                rel_pos<P>(k, pi, a, P::kMixed ? slot_code(e) : 0u, dx, dy, dz);
+                rel_pos<P>(k, pi, a, P::kCodes ? slot_code(e) : 0u, dx, dy, dz);
                 const T r2 = dist2(dx, dy, dz);
                 if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
             };
@@ -212,7 +212,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
         }
     }
     SlotWriter<WIN> w(nl.idx + nbr_col(nl, i), nl.cap, stage);
-    if constexpr (P::kMixed) {
+    if constexpr (P::kCodes) {
         // i's offsets moved into each run's anchor frame once per run instead of decoding the
         // code for every candidate.  That rounds differently from the passes' decode, so the
         // cutoff is widened by 2^-16: every pair the passes would put inside it is listed, and
@@ -427,7 +427,7 @@ void pass2_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typena
     auto with_list = [&](auto mode) {
         constexpr int L = decltype(mode)::value;
         if constexpr (MODE != MODE_RATES && !GS && (P::kId == SPH_PREC_FP32 || P::kMixed)) {
-            constexpr int cap = P::kId == SPH_PREC_FP32 ? 48 : 56;
+            constexpr int cap = P::kCodes ? 56 : 48;
             k_pass2_cap<P, MODE, L, GS, cap><<<b, k.threads, 0, s>>>(
                 k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
         } else {
@@ -554,6 +554,7 @@ SPH_NS_INSTANTIATE(PrecF32)
 SPH_NS_INSTANTIATE(PrecF64)
 SPH_NS_INSTANTIATE(PrecMix)
 SPH_NS_INSTANTIATE(PrecMixC)
+SPH_NS_INSTANTIATE(PrecMixA)
 #undef SPH_NS_INSTANTIATE
 
 }  // namespace sph

@@ -85,11 +85,11 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
     const int cnt = __ldg(nl.count + i);
     if (cnt <= nl.cap) {
         auto one = [&](int e) {
-            const int j = P::kMixed ? slot_index(e) : e;
+            const int j = P::kCodes ? slot_index(e) : e;
             V a, b;
             ld_rec(R, j, a, b);
             T dx, dy, dz;
-            rel_pos<P>(k, pi, a, P::kMixed ? slot_code(e) : 0u, dx, dy, dz);
+            rel_pos<P>(k, pi, a, P::kCodes ? slot_code(e) : 0u, dx, dy, dz);
             const T r2 = dist2(dx, dy, dz);
             if (r2 < k.kh2) f(j, a, b, dx, dy, dz, r2);
         };
@@ -120,7 +120,7 @@ __device__ __forceinline__ void visit_group(const KParamsT<typename P::T>& k,
             const int row = (z * k.gy + y) * k.gx;
 #pragma unroll 1
             for (int xc = xl; xc <= xh; xc++) {
-                const unsigned code = P::kMixed ? cell_code(k, cx, cy, cz, xc, y, z) : 0u;
+                const unsigned code = P::kCodes ? cell_code(k, cx, cy, cz, xc, y, z) : 0u;
                 const int j0 = max(__ldg(cs + row + xc), 0);
                 const int j1 = min(__ldg(cs + row + xc + 1), k.n);  // bounds guard only
 #pragma unroll 1
@@ -229,6 +229,7 @@ SPH_NS_GROUPS_INSTANTIATE(PrecF32)
 SPH_NS_GROUPS_INSTANTIATE(PrecF64)
 SPH_NS_GROUPS_INSTANTIATE(PrecMix)
 SPH_NS_GROUPS_INSTANTIATE(PrecMixC)
+SPH_NS_GROUPS_INSTANTIATE(PrecMixA)
 #undef SPH_NS_GROUPS_INSTANTIATE
 
 }  // namespace sph

@@ -269,15 +269,15 @@ __device__ __forceinline__ void sub2_rn(double ax, double ay, double bx, double 
     dy = sub_rn(ay, by);
 }
 
-// Relative position r = x_i - x_j of a pair: from absolute positions, or (mixed precision)
-// from the offsets from their anchor cells and j's anchor relative to i's (anchor steps of
-// reach cells).
+// Relative position r = x_i - x_j of a pair: from positions in the simulation's frame, or
+// (cell codes) from the offsets from their anchor cells and j's anchor relative to i's
+// (anchor steps of reach cells).
 template <class P, class V>
 __device__ __forceinline__ void rel_pos(const KParamsT<typename P::T>& k, const V& pi,
                                         const V& pj, unsigned code, typename P::T& dx,
                                         typename P::T& dy, typename P::T& dz) {
     using T = typename P::T;
-    if constexpr (P::kMixed) {
+    if constexpr (P::kCodes) {
         // one explicitly rounded difference and one fused multiply-add per axis, so every
         // caller (list, cell walk, list build) gets the same bits whatever the compiler hoists
         // the anchor steps of the code times one anchor step reach * cell
@@ -311,7 +311,7 @@ __device__ __forceinline__ void walk_pairs(const KParamsT<typename P::T>& k,
     if (inactive_key(k, key)) return;  // outside the neighbour search (park_inactive)
     int cx, cy, cz;
     cell_of_key(k.gx, k.gy, key, cx, cy, cz);
-    for_each_candidate<P::kMixed>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
+    for_each_candidate<P::kCodes>(k, cs, cx, cy, cz, [&](int j, unsigned code) {
         const vec4_t<T> pj = ld_pos(X, (size_t)STRIDE * (size_t)j);
         T dx, dy, dz;
         rel_pos<P>(k, pi, pj, code, dx, dy, dz);
@@ -548,9 +548,8 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
             nrho = rhoi;
             tv = nv;
         }
-        double ox, oy, oz;
-        cell_origin(k, keys[i], ox, oy, oz);
-        const float px = (float)(nxm.x - ox), py = (float)(nxm.y - oy), pz = (float)(nxm.z - oz);
+        const float3 q = record_pos<P>(k, keys[i], nxm.x, nxm.y, nxm.z);
+        const float px = q.x, py = q.y, pz = q.z;
         out.rec[2 * (size_t)i] = make_float4(px, py, pz, npres);
         out.rec[2 * (size_t)i + 1] = make_float4(nv.x, nv.y, nv.z, fi ? nrho : -nrho);
         if (out.xyz) out.xyz[i] = make_float4(px, py, pz, fi ? 1.f : -1.f);

@@ -43,31 +43,67 @@ cudaError_t build_cell_starts(const unsigned* sorted_keys, int n, int num_cells,
 //  PrecMix — FP32 neighbour sums on relative positions rebuilt from cell-local offsets; FP64
 //            master positions and density perturbation rho - rho0 for the integration.
 //  PrecMixC — PrecMix with compensated (Neumaier) accumulation of the density and force sums.
+//  PrecMixA — PrecMix's FP64 integration with the pair arithmetic of PrecF32: the neighbour
+//            sums run on FP32 positions in the simulation's frame, rounded from the FP64 master
+//            positions every half step (no cell-local offsets, no cell codes in the lists).
+// kMixed: FP64 master positions and rho - rho0 (xm); kCodes: records hold cell-local offsets
+// and list slots carry the neighbour's anchor cell (the relative-position decode).
 struct PrecF32 {
     using T = float;
     static constexpr bool kMixed = false;
+    static constexpr bool kCodes = false;
     static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_FP32;
 };
 struct PrecF64 {
     using T = double;
     static constexpr bool kMixed = false;
+    static constexpr bool kCodes = false;
     static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_FP64;
 };
 struct PrecMix {
     using T = float;
     static constexpr bool kMixed = true;
+    static constexpr bool kCodes = true;
     static constexpr bool kComp = false;
     static constexpr int kId = SPH_PREC_MIXED;
 };
 struct PrecMixC {
     using T = float;
     static constexpr bool kMixed = true;
+    static constexpr bool kCodes = true;
     static constexpr bool kComp = true;
     static constexpr int kId = SPH_PREC_MIXED_COMP;
 };
+struct PrecMixA {
+    using T = float;
+    static constexpr bool kMixed = true;
+    static constexpr bool kCodes = false;
+    static constexpr bool kComp = false;
+    static constexpr int kId = SPH_PREC_MIXED_ABS;
+};
 inline bool prec_is_mixed(int prec) {
+    return prec == SPH_PREC_MIXED || prec == SPH_PREC_MIXED_COMP || prec == SPH_PREC_MIXED_ABS;
+}
+// Position a record of a policy with FP64 master positions holds for the neighbour sums: the
+// offsets from the anchor cell of resident key `key` (cell codes), or the FP64 position
+// rounded to FP32 (PrecMixA).
+template <class P, class KT>
+__device__ __forceinline__ float3 record_pos(const KParamsT<KT>& k, unsigned key, double x,
+                                             double y, double z) {
+    if constexpr (P::kCodes) {
+        double ox, oy, oz;
+        cell_origin(k, key, ox, oy, oz);
+        return make_float3((float)(x - ox), (float)(y - oy), (float)(z - oz));
+    } else {
+        (void)k;
+        (void)key;
+        return make_float3((float)x, (float)y, (float)z);
+    }
+}
+// The list slots carry a cell code above a 26-bit neighbour index.
+inline bool prec_has_codes(int prec) {
     return prec == SPH_PREC_MIXED || prec == SPH_PREC_MIXED_COMP;
 }
 

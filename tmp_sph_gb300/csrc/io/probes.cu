@@ -239,6 +239,7 @@ SPH_PROBE_INSTANTIATE(PrecF32)
 SPH_PROBE_INSTANTIATE(PrecF64)
 SPH_PROBE_INSTANTIATE(PrecMix)
 SPH_PROBE_INSTANTIATE(PrecMixC)
+SPH_PROBE_INSTANTIATE(PrecMixA)
 #undef SPH_PROBE_INSTANTIATE
 
 }  // namespace sph

@@ -384,13 +384,13 @@ __device__ __forceinline__ T signed_rho_t(int type, T rho) {
     return type == SPH_TYPE_FLUID ? rho : -rho;
 }
 
-// Cell-local offsets of an FP64 position in the cell `key` (mixed precision).
-template <class KT>
+// Record position of an FP64 position for slot key `key` (policies with FP64 masters):
+// cell-local offsets (cell codes) or the rounded position (record_pos).
+template <class P, class KT>
 __device__ __forceinline__ float4 offsets_in_cell(const KParamsT<KT>& k, unsigned key,
                                                   const dvec4& xm, float w) {
-    double ox, oy, oz;
-    cell_origin(k, key, ox, oy, oz);
-    return make_float4((float)(xm.x - ox), (float)(xm.y - oy), (float)(xm.z - oz), w);
+    const float3 q = record_pos<P>(k, key, xm.x, xm.y, xm.z);
+    return make_float4(q.x, q.y, q.z, w);
 }
 
 // Permute (perm) or copy (perm == NULL) a particle set.  Mixed precision: a permuting gather
@@ -413,7 +413,7 @@ __global__ void k_gather(KParamsT<typename P::T> kp, const int* __restrict__ per
         const dvec4 xm = src.xm[s];
         dst.xm[k] = xm;
         if (with_tmp) dst.txm[k] = src.txm[s];
-        if (perm) a = offsets_in_cell(kp, keys[k], xm, a.w);
+        if (perm && P::kCodes) a = offsets_in_cell<P>(kp, keys[k], xm, a.w);
     } else {
         (void)keys;
         if (with_tmp) dst.tpos[k] = src.tpos[s];
@@ -463,7 +463,7 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
         const unsigned h = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
         dst.xm[i] = xm;
         dst.txm[i] = xm;
-        dst.rec[2 * (size_t)i] = offsets_in_cell(kp, h, xm, p[i]);
+        dst.rec[2 * (size_t)i] = offsets_in_cell<P>(kp, h, xm, p[i]);
         hash[i] = h;
     } else {
         dst.rec[2 * (size_t)i] = make4<T>(x, y, z, (T)p[i]);
@@ -511,7 +511,7 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
                 const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[r] - (double)kp.rho0};
                 dst.xm[k] = xm;
                 dst.txm[k] = xm;
-                a = offsets_in_cell(kp, key, xm, p[r]);
+                a = offsets_in_cell<P>(kp, key, xm, p[r]);
                 nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
             } else {
                 a = make4<T>(x, y, z, (T)p[r]);
@@ -764,7 +764,7 @@ cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,
                           int with_tmp, const unsigned* keys, cudaStream_t s,
                           const unsigned* gate) {
     if (k.n <= 0) return cudaSuccess;
-    if (P::kMixed && perm && !keys) return cudaErrorInvalidValue;
+    if (P::kCodes && perm && !keys) return cudaErrorInvalidValue;
     k_gather<P><<<blocks_for(k.n, 256), 256, 0, s>>>(k, perm, src, dst, with_tmp, keys, gate);
     return cudaGetLastError();
 }
@@ -846,6 +846,7 @@ SPH_MESH_INSTANTIATE(PrecF32)
 SPH_MESH_INSTANTIATE(PrecF64)
 SPH_MESH_INSTANTIATE(PrecMix)
 SPH_MESH_INSTANTIATE(PrecMixC)
+SPH_MESH_INSTANTIATE(PrecMixA)
 #undef SPH_MESH_INSTANTIATE
 
 cudaError_t launch_aos_to_set(const KParams& k, const float* s_pos, const float* s_vel,

@@ -123,6 +123,7 @@ auto with_prec(const sph_ctx* c, F&& f) {
         case SPH_PREC_FP64: return f(PrecF64{});
         case SPH_PREC_MIXED: return f(PrecMix{});
         case SPH_PREC_MIXED_COMP: return f(PrecMixC{});
+        case SPH_PREC_MIXED_ABS: return f(PrecMixA{});
         default: return f(PrecF32{});
     }
 }
@@ -282,6 +283,10 @@ static int pass1_lanes(const sph_ctx* c) {
     return c->prec == SPH_PREC_FP32 && c->skin > 0.0 && c->opt_reach == 1 ? 2 : 1;
 }
 
+// The FP32 pair arithmetic without cell codes: FP32 and the mixed policy on FP32 positions
+// (SPH_PREC_MIXED_ABS), which share the FP32 defaults below.
+static bool fp32_pairs(int prec) { return prec == SPH_PREC_FP32 || prec == SPH_PREC_MIXED_ABS; }
+
 // Threads per block of the neighbour kernels: the option, or by default 256 in FP32 (their
 // static shared memory is sized for 256 threads, so 128-thread blocks pack twice as much per
 // SM and leave L1 less room: 4.96M dam break 3.26 against 3.32 ms per step, 7.50 against 7.60
@@ -289,15 +294,15 @@ static int pass1_lanes(const sph_ctx* c) {
 // pass 2 keeps 36 warps per SM in 128-thread blocks, 32 in 256: 3.64 against 3.75 ms).
 static int block_threads(const sph_ctx* c) {
     if (c->opt_threads > 0) return c->opt_threads;
-    return c->prec == SPH_PREC_FP32 ? 256 : 128;
+    return fp32_pairs(c->prec) ? 256 : 128;
 }
 
 // Cells per list cutoff by default: 3 in FP32 (cells of about dx at h = 1.3 dx: the
 // cell-sorted state is ordered along rows of single particles, so the lanes of a warp hold
 // neighbours whose lists are shifted copies of each other and gather common lines; 4.96M dam
-// break 2.85 against 3.28 ms per step), 1 in the other precisions (mixed precision's passes
-// gain less and its list build walks the finer cells in more runs).
-static int default_reach(int prec) { return prec == SPH_PREC_FP32 ? 3 : 1; }
+// break 2.85 against 3.28 ms per step), 1 in the other precisions (the passes of the
+// cell-code precisions gain less, and FP64's are bound by its arithmetic).
+static int default_reach(int prec) { return fp32_pairs(prec) ? 3 : 1; }
 
 // Lane groups read interleaved list windows, one lane per particle plain ones.
 static bool list_windows(const sph_ctx* c) { return pass1_lanes(c) > 1; }
@@ -982,7 +987,7 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
     // mixed-precision list slots keep the neighbour index in 26 bits
-    if (prec_is_mixed(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
+    if (prec_has_codes(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
     if (n_inst < 1 || n_inst > SPH_MAX_INSTANCES) return SPH_ERR_ARG;
     if (n_inst > 1) {
         if (!offsets || offsets[0] != 0 || offsets[n_inst] != n) return SPH_ERR_ARG;

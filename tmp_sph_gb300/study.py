@@ -135,7 +135,8 @@ def main(argv=None) -> None:
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--every", type=int, default=50)
     ap.add_argument("--probe", type=float, nargs=3, default=(1.0, 0.25, 0.05))
-    ap.add_argument("--precisions", nargs="+", default=["fp64", "fp32", "mixed", "mixed_comp"])
+    ap.add_argument("--precisions", nargs="+",
+                    default=["fp64", "fp32", "mixed", "mixed_comp", "mixed_abs"])
     ap.add_argument("--compare-at", type=int, nargs="*", default=[1000],
                     help="also compare the fields after these step counts")
     ap.add_argument("--gauges", type=float, nargs="*", default=[],

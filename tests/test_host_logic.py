@@ -47,6 +47,7 @@ def test_autotune_cost_model():
     assert autotune.default_choice("fp32") == {"threads": 256, "ppt": 1, "lanes": 1,
                                                "skin_permille": 100, "divisions": 3}
     assert autotune.default_choice("mixed")["threads"] == 128
+    assert autotune.default_choice("mixed_abs") == autotune.default_choice("fp32")
     # a candidate replaces the default only when it is at least `margin` faster
     runs = [{"ms_per_step": 2.70, "default": True}, {"ms_per_step": 2.69, "default": False}]
     assert autotune.pick(runs, 0.01)["default"]

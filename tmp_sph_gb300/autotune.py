@@ -103,10 +103,10 @@ def step_cost(m: dict, p, v: float) -> float:
 
 
 def default_choice(precision: str) -> dict:
-    """The library's default: in FP32 256 threads and cells of a third of the list cutoff,
-    otherwise 128 threads and cells of the cutoff; one pass-1 lane, one particle per thread and
-    skin 0.1 kh in all."""
-    fp32 = precision == "fp32"
+    """The library's default: with the FP32 pair arithmetic (FP32, and mixed precision on FP32
+    positions) 256 threads and cells of a third of the list cutoff, otherwise 128 threads and
+    cells of the cutoff; one pass-1 lane, one particle per thread and skin 0.1 kh in all."""
+    fp32 = precision in ("fp32", "mixed_abs")
     return {"threads": 256 if fp32 else 128, "ppt": 1, "lanes": 1,
             "skin_permille": DEFAULT_SKIN, "divisions": 3 if fp32 else 1}
 

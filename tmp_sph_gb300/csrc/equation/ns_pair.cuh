@@ -507,7 +507,9 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
         float npres, nrho;
         const double hdt = (double)k.half_dt;
         if (fi) {
-            if (escaped(k, xm.x, xm.y, xm.z)) {
+            // the escape test and the hash on the FP32 positions of the records when the passes
+            // use them (fewer FP64 operations; every hash of such a particle is the FP32 one)
+            if (P::kCodes ? escaped(k, xm.x, xm.y, xm.z) : escaped(k, pi.x, pi.y, pi.z)) {
                 nxm = dvec4{(double)k.park_x, (double)k.park_y, (double)k.park_z, 0.0};
                 nv = make_float4(0.f, 0.f, 0.f, 0.f);
                 txm = nxm;
@@ -564,7 +566,8 @@ __device__ __forceinline__ void pass2_finish(const KParamsT<typename P::T>& k, i
         const int inst = k.inst_cells ? in.inst[i] : 0;
         if (k.inst_cells) out.inst[i] = inst;
         unsigned f = 0;
-        const unsigned nk = slot_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f);
+        const unsigned nk = P::kCodes ? slot_key(k, inst, fi, nxm.x, nxm.y, nxm.z, &f)
+                                       : slot_key(k, inst, fi, px, py, pz, &f);
         out_hash[i] = nk;
         raise_flags(err, f);
         if (k.park_inactive) {

@@ -460,7 +460,9 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
     dst.rec[2 * (size_t)i + 1] = make4<T>(vx, vy, vz, signed_rho_t<T>(t, (T)rho[i]));
     if constexpr (P::kMixed) {
         const dvec4 xm = {(double)x, (double)y, (double)z, (double)rho[i] - (double)kp.rho0};
-        const unsigned h = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
+        // the FP32 hash of the FP32 positions where the passes use them (record_pos)
+        const unsigned h = P::kCodes ? slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f)
+                                     : slot_key(kp, inst, t == SPH_TYPE_FLUID, x, y, z, &f);
         dst.xm[i] = xm;
         dst.txm[i] = xm;
         dst.rec[2 * (size_t)i] = offsets_in_cell<P>(kp, h, xm, p[i]);
@@ -512,7 +514,8 @@ __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restr
                 dst.xm[k] = xm;
                 dst.txm[k] = xm;
                 a = offsets_in_cell<P>(kp, key, xm, p[r]);
-                nk = slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f);
+                nk = P::kCodes ? slot_key(kp, inst, t == SPH_TYPE_FLUID, xm.x, xm.y, xm.z, &f)
+                               : slot_key(kp, inst, t == SPH_TYPE_FLUID, x, y, z, &f);
             } else {
                 a = make4<T>(x, y, z, (T)p[r]);
                 dst.tpos[k] = make4<T>(x, y, z, (T)rho[r]);
@@ -556,7 +559,7 @@ __global__ void k_rehash(KParamsT<typename P::T> kp, ParticleSetT<typename P::T>
     unsigned f = 0;
     const int inst = set.inst ? set.inst[i] : 0;
     const bool fluid = set.type[i] == SPH_TYPE_FLUID;
-    if constexpr (P::kMixed) {
+    if constexpr (P::kCodes) {  // the FP64 hash where the records hold cell-local offsets
         const dvec4 q = set.xm[i];
         hash[i] = slot_key(kp, inst, fluid, q.x, q.y, q.z, &f);
     } else {

@@ -113,9 +113,10 @@ inline bool prec_has_codes(int prec) {
 // aligned record (32 bytes in FP32), the unit a neighbour gather reads.  type keeps the
 // particle kind as given (0 wall, 1 fluid, 2 rigid, ...), id the original particle index;
 // tpos/tvel hold the predictor's saved step-n state (x, y, z, rho) / (vx, vy, vz, 0).
-// Mixed precision: x, y, z in rec and xyz are offsets from the origin of the particle's cell
-// at the last list build (its sorted key); xm holds the FP64 position and rho - rho0, txm the
-// predictor's save of it (tpos is unused).
+// Mixed precision (kMixed): xm holds the FP64 position and rho - rho0, txm the predictor's save
+// of it (tpos is unused); x, y, z in rec and xyz are the offsets from the origin of the
+// particle's anchor cell at the last list build (kCodes) or the FP64 position rounded to FP32
+// (PrecMixA).
 template <class T>
 struct ParticleSetT {
     vec4_t<T>* rec = nullptr;
@@ -145,12 +146,12 @@ enum HalfStep { HALF_PREDICT = 0, HALF_CORRECT = 1 };
 // Neighbour list: slot c of particle i at idx[(i / 32) * cap * 32 + (c / 4) * 128 + (i % 32) * 4
 // + c % 4] (each warp of 32 consecutive particles owns a block of cap x 32 slots, its particles'
 // slots four to an int4, side by side), count[i] entries, and xb[i]
-// the position i had when the list was built (cell-local offset in mixed precision).  The list
+// the position i had when the list was built (its record position).  The list
 // holds every pair closer than the list cutoff (KParams::kh2_list, the support radius plus a
 // skin), in candidate-walk order; count[i] > cap means the list overflowed for i and the
-// passes walk the cells for it instead.  Mixed precision stores with each slot, in bits 26-31,
-// the neighbour's cell relative to i's ((dz+1) << 4 | (dy+1) << 2 | (dx+1)), from which the
-// passes rebuild relative positions out of the cell-local offsets.
+// passes walk the cells for it instead.  With cell codes (kCodes) each slot also holds, in
+// bits 26-31, the neighbour's anchor relative to i's ((dz+1) << 4 | (dy+1) << 2 | (dx+1)),
+// from which the passes rebuild relative positions out of the cell-local offsets.
 struct NbrList {
     int* idx = nullptr;
     int* count = nullptr;
@@ -207,7 +208,7 @@ cudaError_t launch_pass2_step(const KParamsT<typename P::T>& k, HalfStep half,
                               unsigned* disp, cudaStream_t s);
 
 // Resident-state glue (lib/mesh.cu), one instantiation per precision policy P.
-// perm == NULL copies slot for slot.  Mixed precision: a permuting gather recomputes the
+// perm == NULL copies slot for slot.  With cell codes a permuting gather recomputes the
 // cell-local offsets from the FP64 positions for the cells in `keys` (the new sorted keys).
 template <class P>
 cudaError_t launch_gather(const KParamsT<typename P::T>& k, const int* perm,

@@ -393,7 +393,7 @@ __device__ __forceinline__ float4 offsets_in_cell(const KParamsT<KT>& k, unsigne
     return make_float4(q.x, q.y, q.z, w);
 }
 
-// Permute (perm) or copy (perm == NULL) a particle set.  Mixed precision: a permuting gather
+// Permute (perm) or copy (perm == NULL) a particle set.  With cell codes a permuting gather
 // re-expresses positions as offsets in the new cells keys[k].
 template <class P>
 __global__ void k_gather(KParamsT<typename P::T> kp, const int* __restrict__ perm,
@@ -481,7 +481,8 @@ __global__ void k_upload_convert(KParamsT<typename P::T> kp, const float* __rest
 // the displacement box `disp` (the half step's rebuild test then decides, as after a pass-2
 // update), and a particle whose kind changed (boundary lists hold fluid neighbours only) sets
 // *force.
-// Mixed precision: positions become offsets in the slot's sorted cell, as pass 2 writes them.
+// Mixed precision: record positions as pass 2 writes them (record_pos: offsets in the slot's
+// sorted cell, or the rounded FP64 position).
 template <class P>
 __global__ void k_upload_sorted(KParamsT<typename P::T> kp, const float* __restrict__ pos,
                                 const float* __restrict__ vel, const float* __restrict__ rho,

@@ -986,7 +986,7 @@ static int upload_impl(sph_ctx* c, const float* pos, const float* vel, const flo
                        int from_host, void* stream) {
     if (!c || n < 0 || n > c->capacity) return SPH_ERR_ARG;
     if (n > 0 && (!pos || !vel || !rho || !p || !type)) return SPH_ERR_ARG;
-    // mixed-precision list slots keep the neighbour index in 26 bits
+    // list slots with cell codes keep the neighbour index in 26 bits
     if (prec_has_codes(c->prec) && n >= (1 << 26)) return SPH_ERR_ARG;
     if (n_inst < 1 || n_inst > SPH_MAX_INSTANCES) return SPH_ERR_ARG;
     if (n_inst > 1) {

@@ -223,6 +223,7 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
             int cx, cy, cz;
             cell_of_key(k.gx, k.gy, key, cx, cy, cz);
             const T cut2w = cut2 * (T(1) + T(1.0 / 65536.0));
+            const StripWindow win = strip_window<P>(k, pi, cx, cy, cz, cut2w);
             for_each_run<true>(k, cs, cx, cy, cz, [&](int j0, int j1, unsigned code) {
                 float fx, fy, fz;
                 code_steps(code, fx, fy, fz);
@@ -236,13 +237,27 @@ __device__ __forceinline__ void nbr_build_one(const KParamsT<typename P::T>& k,
                     if (r2 < cut2w && j != i && (keep_all || fluid_rec(pj.w)))
                         w.put(make_slot(j, code));
                 }
-            });
+            }, win);
         }
     } else {
-        walk_pairs<P, 1>(k, cs, keys, X, i, pi, cut2,
-                         [&](int j, unsigned, const vec4_t<T>& pj, T, T, T, T) {
-            if (keep_all || fluid_rec(pj.w)) w.put(j);
-        });
+        // the cell walk of walk_pairs, narrowed to the cells the cutoff sphere reaches (the
+        // same slots pass the distance test, in the same order)
+        const unsigned key = keys[i];
+        if (!inactive_key(k, key)) {
+            int cx, cy, cz;
+            cell_of_key(k.gx, k.gy, key, cx, cy, cz);
+            const StripWindow win = strip_window<P>(k, pi, cx, cy, cz, cut2);
+            for_each_run<false>(k, cs, cx, cy, cz, [&](int j0, int j1, unsigned) {
+#pragma unroll 4
+                for (int j = j0; j < j1; j++) {
+                    const vec4_t<T> pj = ld_pos(X, (size_t)j);
+                    T dx, dy, dz;
+                    rel_pos<P>(k, pi, pj, 0u, dx, dy, dz);
+                    const T r2 = dist2(dx, dy, dz);
+                    if (r2 < cut2 && j != i && (keep_all || fluid_rec(pj.w))) w.put(j);
+                }
+            }, win);
+        }
     }
     w.flush();
     nl.count[i] = w.cnt;

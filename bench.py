@@ -1041,7 +1041,7 @@ def main():
     flags |= sol.error_flags(stream=stream)
     sol.close()
 
-    # the spec comparison on one line: batched mixed precision (config 4) against the
+    # the batch comparison on one line: batched mixed precision (config 4) against the
     # plain FP32 single-instance drop-in above
     batched = None
     if args.batch_instances > 0 and ws == 1:

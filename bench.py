@@ -18,7 +18,7 @@ Printed: one JSON line (rank 0) with
   roofline_fp32  flops of the evaluated pairs per step (counted from the pair algebra, pair
                  counts of the initial state) / step time, over the FP32 FMA peak measured now
   configured_run the configured 1000 steps from rest, all timed, then the developed flow
-  batched        config 4: 64 dam breaks of uneven size in one batched mixed-precision solver
+  batched        the 64-instance batch: dam breaks of uneven size in one batched mixed-precision solver
                  (graph replay; FP64 integration, FP32 sums on FP32 positions by default,
                  --batch-precision), beside the plain FP32 single-instance value above, and
                  the same batch in FP32 and in the other mixed form (short windows)
@@ -498,7 +498,7 @@ def config_block(args, p, n, lanes=None):
 
 def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup: int,
                   run_steps: int = 0, ws: int = 1, rank: int = 0, clocks=None) -> dict:
-    """Config 4: n_inst independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water blocks
+    """The batched workload: n_inst independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water blocks
     of width U[0.2, 0.6] m and height U[0.15, 0.45] m drawn from the seed) advanced together by
     one batched solver: every half step of all instances is the same few launches, replayed as
     one CUDA graph.  With ws > 1 ranks the one batch is split by instance (contiguous blocks of
@@ -1041,7 +1041,7 @@ def main():
     flags |= sol.error_flags(stream=stream)
     sol.close()
 
-    # the batch comparison on one line: batched mixed precision (config 4) against the
+    # the batch comparison on one line: batched mixed precision (the 64-instance batch) against the
     # plain FP32 single-instance drop-in above
     batched = None
     if args.batch_instances > 0 and ws == 1:

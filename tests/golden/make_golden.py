@@ -12,20 +12,20 @@ generator, and stores inputs and outputs as compressed .npz files next to this s
   ref_pc_<case>.npz     PC_prediction then PC_correction with given rates
   ref_run_<case>.npz    whole steps of the src step loop: state after 1 and after 5 steps
 
-and, with --baseline-configs, the fixtures at the benchmark configurations:
+and, with --full-size, the fixtures of the full-size workloads:
 
-  ref_cells_config2.json   calcHash -> sortParticles -> reorder of the reference on the
+  ref_cells_dam_4963548.json   calcHash -> sortParticles -> reorder of the reference on the
                            4,963,548-particle dam break (dx 2.5 mm, seeded jitter): SHA-256
                            digests of the input positions and of every output array (hash
                            unsorted and sorted, index, cellStart, cellEnd of the occupied cells,
                            the gathered arrays), with a few sampled values
-  ref_run_config1.npz      the reference's src step loop on the 133,968-particle dam break
+  ref_run_dam_133968.npz      the reference's src step loop on the 133,968-particle dam break
                            (dx 1 cm, h = 1.3 dx, c0 = 24.26 m/s, delta 0.1, alpha 0.02,
                            dt = 0.25 h / c0, the reference's linear EOS): the fluid state after
                            200 steps
 
 Usage (on a machine with a CUDA GPU and the fatbin):
-    python tests/golden/make_golden.py [--baseline-configs] [outdir]
+    python tests/golden/make_golden.py [--full-size] [outdir]
 """
 from __future__ import annotations
 
@@ -143,10 +143,10 @@ def digest(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-CONFIG1_STEPS = 200
+REF_RUN_STEPS = 200
 
 
-def baseline_configs(outdir=HERE):
+def full_size(outdir=HERE):
     import json
     import torch
     from tmp_sph_gb300 import cases
@@ -155,7 +155,7 @@ def baseline_configs(outdir=HERE):
     cuda = torch.device("cuda:0")
     host = lambda t: t.detach().cpu().numpy()
     H = RefHarness()
-    # ---- config 2: the reference's cell list on the full 4,963,548-particle state
+    # ---- the reference's cell list on the full 4,963,548-particle state
     st, p = cases.build("large", physics="config")
     P = O.params_like(p)
     P.eos = 0
@@ -186,32 +186,32 @@ def baseline_configs(outdir=HERE):
                       "hash_first": host(w["hash"])[:8].tolist(),
                       "hash_last": host(w["hash"])[-8:].tolist(),
                       "cell_start_first_occupied": int(np.flatnonzero(occ)[0])}}
-    with open(os.path.join(outdir, "ref_cells_config2.json"), "w") as f:
+    with open(os.path.join(outdir, "ref_cells_dam_4963548.json"), "w") as f:
         json.dump(rec, f, indent=1)
-    print(f"config2 cells: n={n} cells={P.num_cells} occupied={int(occ.sum())}", flush=True)
+    print(f"4,963,548-particle cells: n={n} cells={P.num_cells} occupied={int(occ.sum())}", flush=True)
     del d, s, w, tmp
     torch.cuda.empty_cache()
-    # ---- config 1: 200 steps of the reference's src step loop
+    # ---- 200 steps of the reference's src step loop on the 133,968-particle dam break
     st, p = cases.build("small", physics="config")
     P = O.params_like(p)
     P.eos = 0
     n = len(st["rho"])
     H.set_params(P, n)
     d, s, w, tmp = H.alloc(st, cuda)
-    H.step(d, s, w, tmp, CONFIG1_STEPS)
+    H.step(d, s, w, tmp, REF_RUN_STEPS)
     H.sync()
     fl = st["type"] == 1
     out = {k: host(d[k])[fl] for k in ("pos", "vel", "rho", "p")}
-    np.savez_compressed(os.path.join(outdir, "ref_run_config1.npz"), steps=CONFIG1_STEPS,
+    np.savez_compressed(os.path.join(outdir, "ref_run_dam_133968.npz"), steps=REF_RUN_STEPS,
                         in_pos_digest=digest(st["pos"]), particles=n,
                         **{"step_" + k: v for k, v in out.items()})
-    print(f"config1 run: n={n} steps={CONFIG1_STEPS} finite={np.isfinite(out['vel']).all()}",
+    print(f"133,968-particle run: n={n} steps={REF_RUN_STEPS} finite={np.isfinite(out['vel']).all()}",
           flush=True)
 
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    if "--baseline-configs" in sys.argv:
-        baseline_configs(args[0] if args else HERE)
+    if "--full-size" in sys.argv:
+        full_size(args[0] if args else HERE)
     else:
         main(args[0] if args else HERE)

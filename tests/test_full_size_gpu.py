@@ -1,16 +1,16 @@
 """Parity at the benchmark configurations themselves (not only at the small fixture sizes).
 
-* config 2 (4,963,548 particles, dx 2.5 mm, seeded jitter): the drop-in calcHash ->
+* the 4,963,548-particle dam break (dx 2.5 mm, seeded jitter): the drop-in calcHash ->
   sortParticles -> reorder chain gives the reference's own output bit for bit (SHA-256
   digests of every array its kernels produced on the same input, tests/golden/
-  ref_cells_config2.json); one resident FP32 step matches the oracle's step; the project's
+  ref_cells_dam_4963548.json); one resident FP32 step matches the oracle's step; the project's
   radix sort equals a stable argsort on the real cell keys of this state.
-* the batched workload (config 4, 64 dam breaks, 48.9M particles): the radix sort equals a
+* the batched workload (64 dam breaks, 48.9M particles): the radix sort equals a
   stable argsort on the stacked instance keys (25 bits).
-* config 1 (133,968 particles, dx 1 cm, h = 1.3 dx, the reference's linear EOS): 200 resident
+* the 133,968-particle dam break (dx 1 cm, h = 1.3 dx, the reference's linear EOS): 200 resident
   steps against 200 steps of the reference's own src step loop (tests/golden/
-  ref_run_config1.npz).
-* config 3 (765,828 particles, dx 5 mm): mixed precision within 1e-3 of the FP64 solver after
+  ref_run_dam_133968.npz).
+* the 765,828-particle dam break (dx 5 mm): mixed precision within 1e-3 of the FP64 solver after
   1000 steps.
 """
 from __future__ import annotations
@@ -40,13 +40,13 @@ def large():
     return cases.build("large", physics="config")
 
 
-def test_config2_cells_match_reference(sphlib, cuda, large):
+def test_dam_4963548_cells_match_reference(sphlib, cuda, large):
     """calcHash -> sortParticles -> reorder (src/lib/mesh.cu:26-159) through the drop-in C ABI
-    at the full config-2 size: hash, index, cellStart, cellEnd of the occupied cells and every
+    at the full 4,963,548-particle size: hash, index, cellStart, cellEnd of the occupied cells and every
     gathered array identical to the reference's."""
     import torch
     from tmp_sph_gb300 import api, solver as S
-    with open(os.path.join(GOLD, "ref_cells_config2.json")) as f:
+    with open(os.path.join(GOLD, "ref_cells_dam_4963548.json")) as f:
         ref = json.load(f)
     st, p = large
     p.eos = api.SPH_EOS_LINEAR
@@ -79,8 +79,8 @@ def test_config2_cells_match_reference(sphlib, cuda, large):
         assert digest(host(out[k])) == ref["digest"]["s_" + k], k
 
 
-def test_config2_keys_radix_sort_matches_stable_argsort(sphlib, cuda, large):
-    """The project's radix sort on the 4,963,548 real cell keys of config 2 (22-bit range),
+def test_dam_4963548_keys_radix_sort_matches_stable_argsort(sphlib, cuda, large):
+    """The project's radix sort on the 4,963,548 real cell keys of the 4.96M dam break (22-bit range),
     against numpy's stable argsort, with the key width the solver uses and with 32 bits."""
     import torch
     from tmp_sph_gb300 import solver as S
@@ -131,7 +131,7 @@ def test_batch_keys_radix_sort_matches_stable_argsort(sphlib, cuda):
     assert np.array_equal(host(hk), keys[order])
 
 
-def test_config2_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
+def test_dam_4963548_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
     """One resident FP32 step of the 4,963,548-particle dam break against one step of the
     oracle (the C restatement of src/sph/sph_run.cu:285-336) on the same input: relative L2 of
     the fluid velocity and density perturbation below 1e-4 (float rounding of sums taken in
@@ -155,25 +155,25 @@ def test_config2_one_step_matches_oracle(sphlib, oracle, cuda, report, large):
     ulps = float(np.max(np.abs(out["pos"][fl].astype(np.float64) - ref["pos"][fl]) / spacing))
     e_v = rel_l2(out["vel"][fl], ref["vel"][fl])
     e_r = rel_l2(out["rho"][fl] - 1000.0, ref["rho"][fl] - 1000.0)
-    report("config2_step1_pos_max_ulps", ulps, 8)
-    report("config2_step1_vel", e_v, 1e-4)
-    report("config2_step1_drho", e_r, 1e-4)
+    report("dam4963548_step1_pos_max_ulps", ulps, 8)
+    report("dam4963548_step1_vel", e_v, 1e-4)
+    report("dam4963548_step1_drho", e_r, 1e-4)
     assert ulps <= 8 and e_v < 1e-4 and e_r < 1e-4, (ulps, e_v, e_r)
 
 
-CONFIG1_TOL = 2e-4  # measured 1.2e-5 / 6.0e-6 / 4.0e-5 / 4.0e-5 on a GB300
+REF_RUN_TOL = 2e-4  # measured 1.2e-5 / 6.0e-6 / 4.0e-5 / 4.0e-5 on a GB300
 
 
-def test_config1_200_steps_match_reference(sphlib, cuda, report):
-    """200 resident FP32 steps of config 1 against 200 steps of the reference's own src step
+def test_dam_133968_200_steps_match_reference(sphlib, cuda, report):
+    """200 resident FP32 steps of the 133,968-particle dam break against 200 steps of the reference's own src step
     loop (its kernels compiled from its sources, run on a GB300: tests/golden/
-    ref_run_config1.npz), same input and constants (h = 1.3 dx, c0 = 24.26 m/s, delta 0.1,
+    ref_run_dam_133968.npz), same input and constants (h = 1.3 dx, c0 = 24.26 m/s, delta 0.1,
     alpha 0.02, dt = 0.25 h / c0, linear EOS).  Relative L2 over the fluid of displacement,
-    velocity, rho - rho0 and p within CONFIG1_TOL (the sums run in another order, and the
+    velocity, rho - rho0 and p within REF_RUN_TOL (the sums run in another order, and the
     differences grow with the flow)."""
     import torch
     from tmp_sph_gb300 import api, cases, solver as S
-    d = np.load(os.path.join(GOLD, "ref_run_config1.npz"))
+    d = np.load(os.path.join(GOLD, "ref_run_dam_133968.npz"))
     st, p = cases.build("small", physics="config")
     p.eos = api.SPH_EOS_LINEAR
     n = len(st["rho"])
@@ -193,11 +193,11 @@ def test_config1_200_steps_match_reference(sphlib, cuda, report):
             "drho": rel_l2(out["rho"][fl] - 1000.0, d["step_rho"] - 1000.0),
             "p": rel_l2(out["p"][fl], d["step_p"])}
     for k, v in errs.items():
-        report(f"config1_{steps}steps_{k}", v, CONFIG1_TOL)
-    assert all(v < CONFIG1_TOL for v in errs.values()), errs
+        report(f"dam133968_{steps}steps_{k}", v, REF_RUN_TOL)
+    assert all(v < REF_RUN_TOL for v in errs.values()), errs
 
 
-def test_config3_mixed_within_1e3_of_fp64_after_1000_steps(sphlib, cuda, report):
+def test_dam_765828_mixed_within_1e3_of_fp64_after_1000_steps(sphlib, cuda, report):
     """The precision claim at its configuration: 765,828 particles, 1000 steps; mixed precision
     (FP32 neighbour sums on cell-relative positions, FP64 positions and rho - rho0) and its
     variant on FP32 positions (mixed_abs) against the FP64 solver, relative L2 over the fluid of
@@ -224,5 +224,5 @@ def test_config3_mixed_within_1e3_of_fp64_after_1000_steps(sphlib, cuda, report)
                 "drho": rel_l2(a["rho"][fl] - 1000.0, b["rho"][fl] - 1000.0),
                 "p": rel_l2(a["p"][fl], b["p"][fl])}
         for k, v in errs.items():
-            report(f"config3_{prec}_vs_fp64_1000_{k}", v, 1e-3)
+            report(f"dam765828_{prec}_vs_fp64_1000_{k}", v, 1e-3)
         assert all(v < 1e-3 for v in errs.values()), (prec, errs)

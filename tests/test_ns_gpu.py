@@ -86,7 +86,7 @@ def test_ns_matches_oracle(sphlib, oracle, cuda, report, physics, pert):
 
 
 def test_ns_full_small_case(sphlib, oracle, cuda, report):
-    """Config-1 geometry at full size (133,968 particles), perturbed state."""
+    """The 133,968-particle dam break at full size, perturbed state."""
     from tmp_sph_gb300 import cases
     st, p = cases.build("small", physics="reference")
     s, r, gpu, _ = run_both(oracle, cuda, perturbed(st), p)

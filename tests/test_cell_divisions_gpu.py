@@ -34,7 +34,7 @@ def run(st, p, nsteps, precision="fp32", opts=None):
 
 
 @pytest.mark.parametrize("div", [2, 3])
-@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+@pytest.mark.parametrize("precision", ["fp32", "mixed", "mixed_abs"])
 def test_divisions_match_oracle(sphlib, oracle, cuda, report, div, precision):
     from tmp_sph_gb300 import api, cases
     from gpu_util import perturbed

@@ -16,12 +16,12 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def run_gpu(st, p, nsteps, graph=True, stream=None):
+def run_gpu(st, p, nsteps, graph=True, stream=None, precision="fp32"):
     import torch
     from tmp_sph_gb300 import api, solver as S
     n = len(st["rho"])
     s = stream or torch.cuda.Stream()
-    with S.Solver(p, n) as sol:
+    with S.Solver(p, n, precision=precision) as sol:
         sol.set_option(api.SPH_OPT_USE_GRAPH, int(graph))
         with torch.cuda.stream(s):
             sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
@@ -356,19 +356,39 @@ def test_launch_shape_options_are_checked(sphlib):
 
 def test_obstacle_case_matches_oracle(sphlib, oracle, cuda, report):
     """The obstacle geometry (rigid box particles, kind 2, act as boundary particles as in the
-    reference): 10 resident steps against the oracle at dx = 3 cm (66,279 particles)."""
-    from tmp_sph_gb300 import cases
+    reference): 10 resident steps against the oracle at dx = 3 cm (66,279 particles), in FP32
+    and in mixed precision on FP32 positions."""
+    import torch
+    from tmp_sph_gb300 import cases, solver as S
     st, p = cases.build("obstacle", physics="config", dx=0.03)
     assert (st["type"] == 2).sum() > 0
+    rig = st["type"] == 2
     out, flags = run_gpu(st, p, 10)
     ref = oracle.run(oracle.params_like(p), st, 10)
     assert flags == 0
     e = field_errors(out, ref, st)
     for k, v in e.items():
-        report(f"obstacle 10 steps {k}", v, 2e-4)
+        report(f"obstacle fp32 10 steps {k}", v, 2e-4)
     assert all(v < 2e-4 for v in e.values()), e
-    rig = st["type"] == 2
     assert np.array_equal(out["pos"][rig], st["pos"][rig])
+    # mixed precision on FP32 positions integrates in FP64: against the FP64 oracle, in full
+    # precision (a displacement of 10 steps from rest is below the float spacing of positions)
+    s = torch.cuda.Stream()
+    with S.Solver(p, len(st["rho"]), precision="mixed_abs") as sol:
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(10, stream=s)
+        outd = sol.download_f64(stream=s)
+        assert sol.error_flags(stream=s) == 0
+    refd = oracle.run(oracle.params_like(p), st, 10, dtype=np.float64)
+    fl = st["type"] == 1
+    x0 = st["pos"][fl].astype(np.float64)
+    ed = {"disp": rel_l2(outd["pos"][fl] - x0, refd["pos"][fl] - x0),
+          "vel": rel_l2(outd["vel"][fl], refd["vel"][fl], floor=1e-3 * np.sqrt(fl.sum())),
+          "drho": rel_l2(outd["rho"][fl] - 1000.0, refd["rho"][fl] - 1000.0)}
+    for k, v in ed.items():
+        report(f"obstacle mixed_abs vs fp64 oracle 10 steps {k}", v, 1e-4)
+    assert all(v < 1e-4 for v in ed.values()), ed
+    assert np.array_equal(outd["pos"][rig], st["pos"][rig].astype(np.float64))
 
 
 def test_rebuild_test_follows_relative_motion(sphlib, oracle, cuda, report):

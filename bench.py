@@ -18,7 +18,8 @@ Printed: one JSON line (rank 0) with
   roofline_fp32  flops of the evaluated pairs per step (counted from the pair algebra, pair
                  counts of the initial state) / step time, over the FP32 FMA peak measured now
   configured_run the configured 1000 steps from rest, all timed, then the developed flow
-  batched        the 64-instance batch: dam breaks of uneven size in one batched mixed-precision solver
+  batched        the 64-instance batch: dam breaks of uneven size in one batched
+                 mixed-precision solver
                  (graph replay; FP64 integration, FP32 sums on FP32 positions by default,
                  --batch-precision), beside the plain FP32 single-instance value above, and
                  the same batch in FP32 and in the other mixed form (short windows)
@@ -498,14 +499,13 @@ def config_block(args, p, n, lanes=None):
 
 def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup: int,
                   run_steps: int = 0, ws: int = 1, rank: int = 0, clocks=None) -> dict:
-    """The batched workload: n_inst independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water blocks
-    of width U[0.2, 0.6] m and height U[0.15, 0.45] m drawn from the seed) advanced together by
-    one batched solver: every half step of all instances is the same few launches, replayed as
-    one CUDA graph.  With ws > 1 ranks the one batch is split by instance (contiguous blocks of
-    about equal particle counts, replicas.partition) and each rank advances its share: no
-    collective on the data path, strong scaling.  `steps` timed after `warmup`, then, with
-    run_steps, the configured run from rest (run_steps steps timed) continued into the
-    developed flow."""
+    """The batched workload: n_inst independent dam breaks (tank 1.0 x 0.5 x 0.6 m, dx 5 mm, water
+    blocks of width U[0.2, 0.6] m and height U[0.15, 0.45] m drawn from the seed) advanced together
+    by one batched solver: every half step of all instances is the same few launches, replayed as
+    one CUDA graph. With ws > 1 ranks the one batch is split by instance (contiguous blocks of about
+    equal particle counts, replicas.partition) and each rank advances its share: no collective on
+    the data path, strong scaling. `steps` timed after `warmup`, then, with run_steps, the
+    configured run from rest (run_steps steps timed) continued into the developed flow."""
     import torch
     from tmp_sph_gb300 import api, cases, replicas, solver as S
     states, p = cases.batch(n_inst, seed=20240611)
@@ -560,8 +560,8 @@ def batch_measure(n_inst: int, precision: str, args, stream, steps: int, warmup:
     out = {"value": n_all * steps / (ms / 1e3), "unit": UNIT,
            "fluid_value": n_fluid_all * steps / (ms / 1e3), "ms_per_step": ms / steps,
            "steps": steps, "warmup": warmup,
-           "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64", "mixed_abs": "f32+f64",
-                     "fp64": "f64"}[precision],
+           "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+                     "mixed_abs": "f32+f64", "fp64": "f64"}[precision],
            "config": {"workload": f"dam_break_batch{n_inst}_{precision}", "instances": n_inst,
                       "instances_this_rank": hi - lo, "particles": n_all,
                       "particles_this_rank": n, "fluid_particles": n_fluid_all,
@@ -1090,8 +1090,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64", "mixed_abs": "f32+f64",
-                  "fp64": "f64"}[args.precision],
+        "dtype": {"fp32": "f32", "mixed": "f32+f64", "mixed_comp": "f32+f64",
+                  "mixed_abs": "f32+f64", "fp64": "f64"}[args.precision],
         "data": "synthetic (seeded dam-break generator)",
         "config": config_block(args, p, n, lanes),
         "fluid_particle_steps_per_s": n_fluid * ws * args.steps / (ms / 1e3),

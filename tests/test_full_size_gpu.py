@@ -42,8 +42,8 @@ def large():
 
 def test_dam_4963548_cells_match_reference(sphlib, cuda, large):
     """calcHash -> sortParticles -> reorder (src/lib/mesh.cu:26-159) through the drop-in C ABI
-    at the full 4,963,548-particle size: hash, index, cellStart, cellEnd of the occupied cells and every
-    gathered array identical to the reference's."""
+    at the full 4,963,548-particle size: hash, index, cellStart, cellEnd of the occupied cells and
+    every gathered array identical to the reference's."""
     import torch
     from tmp_sph_gb300 import api, solver as S
     with open(os.path.join(GOLD, "ref_cells_dam_4963548.json")) as f:
@@ -80,8 +80,8 @@ def test_dam_4963548_cells_match_reference(sphlib, cuda, large):
 
 
 def test_dam_4963548_keys_radix_sort_matches_stable_argsort(sphlib, cuda, large):
-    """The project's radix sort on the 4,963,548 real cell keys of the 4.96M dam break (22-bit range),
-    against numpy's stable argsort, with the key width the solver uses and with 32 bits."""
+    """The project's radix sort on the 4,963,548 real cell keys of the 4.96M dam break (22-bit
+    range), against numpy's stable argsort, with the key width the solver uses and with 32 bits."""
     import torch
     from tmp_sph_gb300 import solver as S
     st, p = large
@@ -165,12 +165,12 @@ REF_RUN_TOL = 2e-4  # measured 1.2e-5 / 6.0e-6 / 4.0e-5 / 4.0e-5 on a GB300
 
 
 def test_dam_133968_200_steps_match_reference(sphlib, cuda, report):
-    """200 resident FP32 steps of the 133,968-particle dam break against 200 steps of the reference's own src step
-    loop (its kernels compiled from its sources, run on a GB300: tests/golden/
-    ref_run_dam_133968.npz), same input and constants (h = 1.3 dx, c0 = 24.26 m/s, delta 0.1,
-    alpha 0.02, dt = 0.25 h / c0, linear EOS).  Relative L2 over the fluid of displacement,
-    velocity, rho - rho0 and p within REF_RUN_TOL (the sums run in another order, and the
-    differences grow with the flow)."""
+    """200 resident FP32 steps of the 133,968-particle dam break against 200 steps of the
+    reference's own src step loop (its kernels compiled from its sources, run on a GB300:
+    tests/golden/ref_run_dam_133968.npz), same input and constants (h = 1.3 dx, c0 = 24.26 m/s,
+    delta 0.1, alpha 0.02, dt = 0.25 h / c0, linear EOS). Relative L2 over the fluid of
+    displacement, velocity, rho - rho0 and p within REF_RUN_TOL (the sums run in another order, and
+    the differences grow with the flow)."""
     import torch
     from tmp_sph_gb300 import api, cases, solver as S
     d = np.load(os.path.join(GOLD, "ref_run_dam_133968.npz"))

@@ -62,7 +62,7 @@ PHASE_BYTES = {"sort": B_SORT, "gather_cells": B_PERMUTE, "nbr_build": 16, "pass
 PHASE_KERNEL = {"sort": "k_rs_upsweep/k_rs_scan/k_rs_downsweep",
                 "gather_cells": "k_gather + k_cell_mark/k_cell_fill",
                 "nbr_build": "k_nbr_build (one cell walk; positions read once = 16 B)",
-                "pass1": "k_pass1_g<2 lanes> (k_pass1 with one lane)",
+                "pass1": "k_pass1 (k_pass1_g with two or four lanes)",
                 "pass2_integrate": "k_pass2<MODE_PRED|MODE_CORR>"}
 
 
@@ -982,6 +982,9 @@ def main():
         phases[name] = {"ms_per_launch": per_launch_ms, "algorithmic_gbs": ach,
                         "share": v["ms"] / max(1e-9, sum(x["ms"] for x in prof.values())),
                         "kernels": PHASE_KERNEL[name]}
+    lanes1 = lanes["lanes_per_particle_pass1_pass2"][0]
+    if "pass1" in phases:
+        phases["pass1"]["kernels"] = "k_pass1" if lanes1 == 1 else f"k_pass1_g<{lanes1} lanes>"
     dom = max(phases, key=lambda k: phases[k]["ms_per_launch"])
     dom_ms = phases[dom]["ms_per_launch"]
     workload = f"dam_break_{args.case}_{args.precision}"

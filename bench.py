@@ -453,17 +453,36 @@ def configured_run(sol, stream, st, n: int, n_fluid: int, run_steps: int, steps:
     """The configured run on a fresh solver `sol`: the initial state uploaded, all `run_steps`
     steps timed (the flow develops and the lists are rebuilt more often than in a short window
     from rest), then `steps` more steps of the developed flow timed alone."""
+    from tmp_sph_gb300 import api
     sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=stream)
     ms, rb = time_run(sol, stream, run_steps)
+    skin_run = sol.list_skin(stream=stream)
     ms2, rb2 = time_run(sol, stream, steps)
+    skin_dev = sol.list_skin(stream=stream)
+    # device time per phase over a window of the developed flow (kernels launched one by
+    # one with events around every phase; the rebuild kernels of a half step that keeps its
+    # lists return at once)
+    k = min(steps, 50)
+    sol.set_option(api.SPH_OPT_PROFILE, 1)
+    sol.profile(reset=True)
+    rb3 = sol.rebuild_count(stream=stream)
+    sol.step(k, stream=stream)
+    prof = sol.profile(reset=True)
+    rb3 = sol.rebuild_count(stream=stream) - rb3
+    sol.set_option(api.SPH_OPT_PROFILE, 0)
+    phases = {name: v["ms"] / k for name, v in prof.items() if v["launches"]}
     return {"run": {"steps": run_steps, "ms_per_step": ms / run_steps,
                     "value": n * run_steps / (ms / 1e3),
                     "fluid_value": n_fluid * run_steps / (ms / 1e3),
-                    "list_rebuilds": rb, "half_steps": 2 * run_steps},
+                    "list_rebuilds": rb, "half_steps": 2 * run_steps,
+                    "list_skin_over_kh_at_end": skin_run},
             "developed_flow": {"after_steps": run_steps, "steps": steps,
                                "ms_per_step": ms2 / steps, "value": n * steps / (ms2 / 1e3),
                                "fluid_value": n_fluid * steps / (ms2 / 1e3),
-                               "list_rebuilds": rb2, "half_steps": 2 * steps},
+                               "list_rebuilds": rb2, "half_steps": 2 * steps,
+                               "list_skin_over_kh_at_end": skin_dev,
+                               "phase_ms_per_step": {"steps": k, "list_rebuilds": rb3,
+                                                     **phases}},
             "device_error_flags": sol.error_flags(stream=stream)}
 
 
@@ -922,6 +941,7 @@ def main():
         ms = float(t.item())
     flags = sol.error_flags(stream=stream)
     rebuilds = sol.rebuild_count(stream=stream) - rebuilds0
+    skin_end = sol.list_skin(stream=stream)
     value = n * ws * args.steps / (ms / 1e3)
 
     # per-kernel device time from CUDA events around every phase, same stream
@@ -979,7 +999,8 @@ def main():
     for name, v in prof.items():
         per_launch_ms = v["ms"] / max(1, v["launches"])
         ach = PHASE_BYTES[name] * n / (per_launch_ms / 1e3) / 1e9
-        phases[name] = {"ms_per_launch": per_launch_ms, "algorithmic_gbs": ach,
+        phases[name] = {"ms_per_launch": per_launch_ms, "ms_per_step": v["ms"] / prof_steps,
+                        "algorithmic_gbs": ach,
                         "share": v["ms"] / max(1e-9, sum(x["ms"] for x in prof.values())),
                         "kernels": PHASE_KERNEL[name]}
     lanes1 = lanes["lanes_per_particle_pass1_pass2"][0]
@@ -1111,7 +1132,7 @@ def main():
                 "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
         "gpu_launches": count_launches(sol_cells, 2 * args.steps, rebuilds, args.graph_mode),
         "list_rebuilds": {"timed": rebuilds, "half_steps": 2 * args.steps,
-                          "skin_permille": args.skin},
+                          "skin_permille": args.skin, "list_skin_over_kh_at_end": skin_end},
         "configured_run": run,
         "rebuild_every_half_step": no_reuse,
         "batched": batched,

@@ -361,10 +361,13 @@ k_pass2(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
     reduce_disp(k, box, disp, s_box, s_inst);
 }
 
-// The same kernel held to CAP registers (one particle per thread): the FP32 step kernel fits
-// in 48 without spills (five 256-thread blocks per SM; 40 registers, six blocks, spilled 40
-// bytes and measured the same: 0.7255 against 0.7250 ms at 4.96M), the mixed-precision one in
-// 56 (nine 128-thread blocks instead of eight).
+// The same kernel held to CAP registers (one particle per thread).  The FP32 step kernel (and
+// the one of mixed precision on FP32 positions) runs in 40: six 256-thread blocks per SM
+// instead of the five of its spill-free 48, for 40 bytes of spill
+// (0.610 against 0.634 ms at 4.96M particles; before the pair approximations were taken in
+// their flush-to-zero forms, with more instructions per pair to hide the gathers, the two
+// measured the same).  The mixed-precision kernel on cell-local offsets runs in 56 (nine
+// 128-thread blocks instead of eight).
 template <class P, int MODE, int LIST, bool GS, int CAP>
 __global__ void __maxnreg__(CAP)
 k_pass2_cap(KParamsT<typename P::T> k, ParticleSetT<typename P::T> in,
@@ -442,7 +445,7 @@ void pass2_launch_gs(const KParamsT<typename P::T>& k, const ParticleSetT<typena
     auto with_list = [&](auto mode) {
         constexpr int L = decltype(mode)::value;
         if constexpr (MODE != MODE_RATES && !GS && (P::kId == SPH_PREC_FP32 || P::kMixed)) {
-            constexpr int cap = P::kCodes ? 56 : 48;
+            constexpr int cap = P::kCodes ? 56 : 40;
             k_pass2_cap<P, MODE, L, GS, cap><<<b, k.threads, 0, s>>>(
                 k, in, keys, cs, *nl, p1, rho_dt, vel_dt, wall_rates, out, out_hash, err, disp);
         } else {

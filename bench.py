@@ -17,7 +17,9 @@ Printed: one JSON line (rank 0) with
                  with the DRAM traffic of a committed ncu capture at the same launch shape
   roofline_fp32  flops of the evaluated pairs per step (counted from the pair algebra, pair
                  counts of the initial state) / step time, over the FP32 FMA peak measured now
-  configured_run the configured 1000 steps from rest, all timed, then the developed flow
+  configured_run the configured 1000 steps from rest, all timed, then the developed flow,
+                 each with the list skin at its end, and the developed flow's device time
+                 per phase (phase_ms_per_step)
   batched        the 64-instance batch: dam breaks of uneven size in one batched
                  mixed-precision solver
                  (graph replay; FP64 integration, FP32 sums on FP32 positions by default,

@@ -215,6 +215,30 @@ def test_upload_download_roundtrip(sphlib, cuda):
         assert np.array_equal(out[k], st[k]), k
 
 
+def test_download_into_device_memory(sphlib, cuda):
+    """sph_download with to_host = 0 writes the same state, in original order, into device
+    arrays as the host download; a NULL array is skipped."""
+    import torch
+    from tmp_sph_gb300 import cases, solver as S
+    st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
+    n = len(st["rho"])
+    s = torch.cuda.Stream()
+    with S.Solver(p, n) as sol:
+        sol.upload(st["pos"], st["vel"], st["rho"], st["p"], st["type"], stream=s)
+        sol.step(2, stream=s)
+        host = sol.download(stream=s)
+        dev = {"pos": torch.full((n, 3), -1.0, device=cuda),
+               "vel": torch.full((n, 3), -1.0, device=cuda),
+               "rho": torch.full((n,), -1.0, device=cuda),
+               "type": torch.full((n,), -7, dtype=torch.int32, device=cuda)}
+        torch.cuda.synchronize()  # the fills above ran on torch's stream, the download runs on s
+        sol.download_device(dev, stream=s)
+        s.synchronize()
+        assert sol.error_flags(stream=s) == 0
+    for k in ("pos", "vel", "rho", "type"):
+        assert np.array_equal(dev[k].cpu().numpy(), host[k]), k
+
+
 def test_step_host_matches_device_path(sphlib, cuda):
     import torch
     from tmp_sph_gb300 import cases, solver as S

@@ -1025,9 +1025,9 @@ def main():
             "dram_gbs_at_traffic": (traffic / (dom_ms / 1e3) / 1e9) if traffic else None,
             "bytes_per_particle": PHASE_BYTES[dom],
             "l1_data_pipe_pct": cap.get("l1_data_pipe_pct"),
-            "note": "the neighbour kernels are issue- or L1-throughput bound (sparse gather "
-                    "of neighbour data), not HBM bound; frac is algorithmic bytes over the "
-                    "measured copy bandwidth"}
+            "note": "the neighbour kernels are bound by instruction issue and the latency "
+                    "of their neighbour-record gathers (sparse gathers), not by HBM; frac is "
+                    "algorithmic bytes over the measured copy bandwidth"}
 
     # FP32 arithmetic roofline: flops of the evaluated pairs (counted at the initial state)
     # over the FP32 FMA peak measured on this GPU now

@@ -12,7 +12,6 @@ pytestmark = pytest.mark.gpu
 
 
 def test_prediction_and_correction(sphlib, oracle, cuda):
-    import torch
     from tmp_sph_gb300 import cases, solver as S
     st, p = cases.build("small", physics="config", dx=0.02, jitter=0.01)
     st = perturbed(st)
